@@ -1,0 +1,168 @@
+/*
+ * gwn.h -- C ABI of libgwn.so, the GB300 (sm_103a) generalized winding number
+ * library.  Plain pointers and sizes only; every entry point returns a status
+ * code (GWN_OK on success) and never throws across the ABI.  The message of
+ * the last failure on the calling thread is available from gwn_last_error().
+ *
+ * Memory kinds: every call that takes arrays takes `mem`:
+ *   GWN_HOST   -- pointers are host memory; the call is synchronous (copies in,
+ *                 computes on the GPU, copies out, waits).
+ *   GWN_DEVICE -- pointers are device memory of the current CUDA device; work
+ *                 is enqueued on `stream` (a cudaStream_t, NULL = legacy
+ *                 default stream) and the call returns without waiting.
+ * Arrays are row-major and contiguous: V[i*3+d], F[f*3+c], Q[i*3+d].
+ *
+ * Precision modes:
+ *   GWN_PLAIN_FP64 -- every term, sum and far-field expansion in FP64.
+ *   GWN_MIXED      -- FP32 bulk arithmetic; FP64 for (i) exact terms of
+ *                     queries within 1e-3 * bbox-diagonal of a primitive,
+ *                     (ii) moment accumulation, (iii) full re-evaluation of
+ *                     any query whose FP32 result lies within 1e-3 of 0.5.
+ *
+ * This header replaces, for C/C++ callers, the libigl entry points cited at
+ * each declaration (paths inside the libigl source tree).  The igl::
+ * signatures themselves are provided as inline templates over this ABI in
+ * include/igl_gb300/.
+ */
+#ifndef GWN_H
+#define GWN_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GWN_VERSION 100
+
+enum gwn_status {
+  GWN_OK = 0,
+  GWN_ERR_INVALID_ARGUMENT = 1,
+  GWN_ERR_CUDA = 2,
+  GWN_ERR_OUT_OF_MEMORY = 3,
+  GWN_ERR_NO_DEVICE = 4,
+  GWN_ERR_TIMEOUT = 5, /* a bounded device-side wait gave up */
+  GWN_ERR_BUSY = 6,
+  GWN_ERR_INTERNAL = 7
+};
+
+enum gwn_dtype { GWN_F32 = 0, GWN_F64 = 1 };
+enum gwn_precision { GWN_PLAIN_FP64 = 0, GWN_MIXED = 1 };
+enum gwn_mem { GWN_HOST = 0, GWN_DEVICE = 1 };
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* gwn_last_error(void);
+int gwn_version(void);
+
+/* Device-memory (GWN_DEVICE) calls never synchronize, so failures detected
+ * inside kernels (an out-of-range index, a bounded wait that gave up) are
+ * recorded in a sticky per-device word.  This call synchronizes the current
+ * device, returns the recorded GWN_STATUS_* bits in *flags and clears them if
+ * `clear` is non-zero.  Host-memory calls report such failures directly. */
+#define GWN_STATUS_WAIT_TIMEOUT 1u
+#define GWN_STATUS_BAD_INPUT 2u
+int gwn_device_status(unsigned int* flags, int clear);
+
+/* ------------------------------------------------------------------------
+ * Exact generalized winding number.
+ * Replaces igl::winding_number(V,F,O,W)      include/igl/winding_number.h:35-44
+ *   (implementation include/igl/winding_number.cpp:17-56) and, per query,
+ *   igl::winding_number(V,F,p)                include/igl/winding_number.h:53-60
+ *   (winding_number.cpp:58-89, solid_angle.cpp:5-55, signed_angle.cpp:5-46).
+ * dim = 3: V is nV x 3, F is nF x 3 (triangles), O is nO x 3.
+ * dim = 2: V is nV x 2, F is nF x 2 (edges),     O is nO x 2.
+ * W (nO) receives sum over elements of solid angle / 4pi (or angle / 2pi).
+ * ---------------------------------------------------------------------- */
+int gwn_winding_number(const double* V, int64_t nV, int dim, const int32_t* F, int64_t nF,
+                       const void* O, int o_dtype, int64_t nO, void* W, int w_dtype,
+                       int precision, int mem, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Triangle-soup fast winding number (Barnes-Hut over a GPU-built BVH with the
+ * HDK order-0/1/2 far field).
+ * gwn_soup_build replaces the precompute overload
+ *   igl::fast_winding_number(V,F,order,fwn_bvh)  include/igl/fast_winding_number.h:176-181
+ *   (fast_winding_number.cpp:380-416; UT_SolidAngle::init,
+ *    FastWindingNumberForSoups.h:6543-7133).
+ * gwn_soup_eval replaces the evaluate overloads
+ *   igl::fast_winding_number(fwn_bvh,accuracy_scale,Q,W)  fast_winding_number.h:189-194
+ *   igl::fast_winding_number(fwn_bvh,accuracy_scale,p)    fast_winding_number.h:201-205
+ *   (fast_winding_number.cpp:418-455; UT_SolidAngle::computeSolidAngle,
+ *    FastWindingNumberForSoups.h:7148-7284).
+ * The handle plays the role of struct igl::FastWindingNumberBVH
+ *   (fast_winding_number.h:140-147): it owns device copies of V and F.
+ * ---------------------------------------------------------------------- */
+typedef struct gwn_soup gwn_soup;
+
+typedef struct gwn_soup_stats {
+  int64_t num_triangles;   /* triangles kept (non-finite boxes excluded) */
+  int64_t num_nodes;       /* binary tree nodes, leaves included          */
+  int64_t device_bytes;    /* device memory held by the handle            */
+  int32_t order;
+  int32_t max_depth;
+} gwn_soup_stats;
+
+int gwn_soup_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, int order,
+                   int mem, void* stream, gwn_soup** out);
+int gwn_soup_eval(const gwn_soup* soup, float accuracy_scale, const void* Q, int q_dtype,
+                  int64_t nQ, void* W, int w_dtype, int precision, int mem, void* stream);
+int gwn_soup_stats_get(const gwn_soup* soup, gwn_soup_stats* out);
+void gwn_soup_free(gwn_soup* soup);
+
+/* ------------------------------------------------------------------------
+ * Octree over a point cloud, bit-exact with igl::octree.
+ * Replaces igl::octree(P,point_indices,CH,CN,W)  include/igl/octree.h:44-50
+ *   (include/igl/octree.cpp:5-170).
+ * point_indices is exported in CSR form: cell c holds
+ *   pi_indices[pi_offsets[c] .. pi_offsets[c+1]).
+ * ---------------------------------------------------------------------- */
+typedef struct gwn_octree gwn_octree;
+
+int gwn_octree_build(const double* P, int64_t nP, int mem, void* stream, gwn_octree** out);
+int gwn_octree_sizes(const gwn_octree* tree, int64_t* num_cells, int64_t* num_indices,
+                     int32_t* max_depth);
+int gwn_octree_export(const gwn_octree* tree, int64_t* pi_offsets, int32_t* pi_indices,
+                      int32_t* CH, double* CN, double* W, int mem, void* stream);
+void gwn_octree_free(gwn_octree* tree);
+
+/* ------------------------------------------------------------------------
+ * Point-cloud fast winding number (order-2 dipole expansion, Barnes-Hut).
+ * gwn_cloud_build replaces the precompute overload
+ *   igl::fast_winding_number(P,N,A,point_indices,CH,expansion_order,CM,R,EC)
+ *     include/igl/fast_winding_number.h:35-53 (fast_winding_number.cpp:17-124)
+ * computing it on the device from an octree handle; gwn_cloud_export returns
+ * CM (ncells x 3), R (ncells), EC (ncells x num_terms).
+ * gwn_cloud_eval replaces the evaluate overload
+ *   igl::fast_winding_number(P,N,A,point_indices,CH,CM,R,EC,Q,beta,WN)
+ *     fast_winding_number.h:76-99 (fast_winding_number.cpp:126-311);
+ * beta <= 0 selects the direct O(P*Q) sum (fast_winding_number.cpp:300-310).
+ * ---------------------------------------------------------------------- */
+typedef struct gwn_cloud gwn_cloud;
+
+int gwn_cloud_build(const gwn_octree* tree, const double* P, const double* N, const double* A,
+                    int order, int mem, void* stream, gwn_cloud** out);
+int gwn_cloud_export(const gwn_cloud* cloud, double* CM, double* R, double* EC, int mem,
+                     void* stream);
+int gwn_cloud_eval(const gwn_cloud* cloud, double beta, const void* Q, int q_dtype, int64_t nQ,
+                   void* W, int w_dtype, int precision, int mem, void* stream);
+void gwn_cloud_free(gwn_cloud* cloud);
+
+/* Drop-in forms over caller-held arrays (all host memory, synchronous): the
+ * octree / precompute outputs may come from igl::octree or anywhere else.
+ * CH has ncells rows of 8 child ids (-1 for leaves). */
+int gwn_cloud_precompute_arrays(const double* P, const double* N, const double* A, int64_t nP,
+                                const int64_t* pi_offsets, const int32_t* pi_indices,
+                                const int32_t* CH, int64_t ncells, int order, double* CM,
+                                double* R, double* EC);
+int gwn_cloud_eval_arrays(const double* P, const double* N, const double* A, int64_t nP,
+                          const int64_t* pi_offsets, const int32_t* pi_indices,
+                          const int32_t* CH, int64_t ncells, const double* CM, const double* R,
+                          const double* EC, int order, const double* Q, int64_t nQ,
+                          double beta, double* W, int precision);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GWN_H */

@@ -1,0 +1,30 @@
+// Internal interfaces between the C-ABI layer (gwn_api.cu) and the kernel
+// translation units.  All pointers here are device pointers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "gwn_common.cuh"
+
+namespace gwn {
+
+struct ExactArgs {
+  const double* V;
+  int64_t nV;
+  int dim;
+  const int32_t* F;
+  int64_t nF;
+  const void* Q;
+  int q_dtype;
+  int64_t nQ;
+  void* W;
+  int w_dtype;
+  int precision;
+  bool host_mode;
+};
+
+void run_exact(const ExactArgs& a, cudaStream_t st);
+
+}  // namespace gwn

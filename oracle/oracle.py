@@ -1,0 +1,264 @@
+"""ctypes front end of the CPU oracle (test infrastructure only).
+
+``liboracle.so`` is compiled from ``oracle/gwn_oracle.cpp`` (a restatement of
+libigl's FP64 winding-number algorithms); ``oracle/_ref/libref_soup.so`` is the
+reference's own soup code compiled from the reference tree, present only where
+that tree exists.  Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU
+baseline / reference arm use this module, always as the checker or the timed
+CPU baseline, never as the thing measured on the GPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB_PATH = os.path.join(BUILD_DIR, "liboracle.so")
+REF_SOUP_PATH = os.path.join(HERE, "_ref", "libref_soup.so")
+
+_SOURCES = ["gwn_oracle.cpp", "soup_port.cpp", "wn_hier.cpp"]
+
+
+def build(force: bool = False) -> str:
+    """Compile liboracle.so (g++, no FMA contraction, so results match on x86 and Arm)."""
+    srcs = [os.path.join(HERE, s) for s in _SOURCES if os.path.exists(os.path.join(HERE, s))]
+    if not force and os.path.exists(LIB_PATH):
+        lib_m = os.path.getmtime(LIB_PATH)
+        if all(os.path.getmtime(s) <= lib_m for s in srcs):
+            return LIB_PATH
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    cmd = ["g++", "-O3", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", *srcs,
+           "-o", LIB_PATH, "-lpthread"]
+    subprocess.run(cmd, check=True)
+    return LIB_PATH
+
+
+def build_ref() -> str | None:
+    """Compile the reference soup wrapper where the reference tree exists."""
+    subprocess.run(["bash", os.path.join(HERE, "build_ref.sh")], check=True)
+    return REF_SOUP_PATH if os.path.exists(REF_SOUP_PATH) else None
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        p = C.c_void_p
+        i64 = C.c_int64
+        L.oracle_winding_number.argtypes = [p, i64, p, i64, C.c_int, p, i64, p, C.c_int]
+        L.oracle_winding_number.restype = C.c_int
+        L.oracle_solid_angle.argtypes = [p, p, p, p]
+        L.oracle_solid_angle.restype = C.c_double
+        L.oracle_octree_build.argtypes = [p, i64]
+        L.oracle_octree_build.restype = p
+        L.oracle_octree_sizes.argtypes = [p, p, p]
+        L.oracle_octree_export.argtypes = [p, p, p, p, p, p]
+        L.oracle_octree_free.argtypes = [p]
+        L.oracle_cloud_precompute.argtypes = [p, p, p, p, p, p, i64, C.c_int, p, p, p, C.c_int]
+        L.oracle_cloud_precompute.restype = C.c_int
+        L.oracle_cloud_eval.argtypes = [p, p, p, i64, p, p, p, i64, p, p, p, C.c_int, p, i64,
+                                        C.c_double, p, C.c_int]
+        L.oracle_cloud_eval.restype = C.c_int
+        L.oracle_num_threads.argtypes = [C.c_int]
+        L.oracle_num_threads.restype = C.c_int
+        if hasattr(L, "oracle_soup_build"):
+            L.oracle_soup_build.argtypes = [p, i64, p, i64, C.c_int]
+            L.oracle_soup_build.restype = p
+            L.oracle_soup_eval.argtypes = [p, C.c_float, p, i64, p, C.c_int]
+            L.oracle_soup_free.argtypes = [p]
+            L.oracle_soup_nodes.argtypes = [p]
+            L.oracle_soup_nodes.restype = i64
+        if hasattr(L, "oracle_winding_number_hier"):
+            L.oracle_winding_number_hier.argtypes = [p, i64, p, i64, p, i64, p, C.c_int]
+            L.oracle_winding_number_hier.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _d(a, dtype=np.float64):
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def num_threads(requested: int = 0) -> int:
+    return lib().oracle_num_threads(requested)
+
+
+def winding_number(V, F, O, nthreads: int = 0) -> np.ndarray:
+    """Brute-force exact GWN (FP64), dim taken from F.shape[1] (2 or 3)."""
+    V, O = _d(V), _d(O)
+    F = _d(F, np.int32)
+    dim = F.shape[1]
+    W = np.empty(O.shape[0], np.float64)
+    rc = lib().oracle_winding_number(_ptr(V), V.shape[0], _ptr(F), F.shape[0], dim, _ptr(O),
+                                     O.shape[0], _ptr(W), nthreads)
+    if rc:
+        raise ValueError("oracle_winding_number failed")
+    return W
+
+
+def winding_number_hier(V, F, O, nthreads: int = 0) -> np.ndarray:
+    """Hierarchical exact GWN (restated WindingNumberAABB), 3D only."""
+    V, O = _d(V), _d(O)
+    F = _d(F, np.int32)
+    W = np.empty(O.shape[0], np.float64)
+    rc = lib().oracle_winding_number_hier(_ptr(V), V.shape[0], _ptr(F), F.shape[0], _ptr(O),
+                                          O.shape[0], _ptr(W), nthreads)
+    if rc:
+        raise ValueError("oracle_winding_number_hier failed")
+    return W
+
+
+def solid_angle(a, b, c, p) -> float:
+    a, b, c, p = (_d(x) for x in (a, b, c, p))
+    return lib().oracle_solid_angle(_ptr(a), _ptr(b), _ptr(c), _ptr(p))
+
+
+class Octree:
+    """igl::octree outputs in CSR form: pi_off (ncells+1), pi_idx, CH, CN, W."""
+
+    def __init__(self, pi_off, pi_idx, CH, CN, W):
+        self.pi_off, self.pi_idx, self.CH, self.CN, self.W = pi_off, pi_idx, CH, CN, W
+
+    @property
+    def ncells(self):
+        return self.CH.shape[0]
+
+    def point_indices(self):
+        return [self.pi_idx[self.pi_off[c]:self.pi_off[c + 1]].tolist() for c in range(self.ncells)]
+
+
+def octree(P) -> Octree:
+    P = _d(P).reshape(-1, 3)
+    L = lib()
+    h = L.oracle_octree_build(_ptr(P), P.shape[0])
+    try:
+        nc, ni = C.c_int64(), C.c_int64()
+        L.oracle_octree_sizes(h, C.byref(nc), C.byref(ni))
+        nc, ni = nc.value, ni.value
+        pi_off = np.empty(nc + 1, np.int64)
+        pi_idx = np.empty(max(ni, 1), np.int32)[:ni]
+        CH = np.empty((nc, 8), np.int32)
+        CN = np.empty((nc, 3), np.float64)
+        W = np.empty(nc, np.float64)
+        L.oracle_octree_export(h, _ptr(pi_off), _ptr(pi_idx), _ptr(CH), _ptr(CN), _ptr(W))
+    finally:
+        L.oracle_octree_free(h)
+    return Octree(pi_off, pi_idx, CH, CN, W)
+
+
+def num_terms(order: int) -> int:
+    return {0: 3, 1: 12, 2: 39}[order]
+
+
+def cloud_precompute(P, N, A, tree: Octree, order: int = 2, nthreads: int = 0):
+    P, N, A = _d(P), _d(N), _d(A).reshape(-1)
+    nc = tree.ncells
+    CM = np.empty((nc, 3), np.float64)
+    R = np.empty(nc, np.float64)
+    EC = np.empty((nc, num_terms(order)), np.float64)
+    rc = lib().oracle_cloud_precompute(_ptr(P), _ptr(N), _ptr(A), _ptr(tree.pi_off),
+                                       _ptr(tree.pi_idx), _ptr(tree.CH), nc, order, _ptr(CM),
+                                       _ptr(R), _ptr(EC), nthreads)
+    if rc:
+        raise ValueError("oracle_cloud_precompute failed")
+    return CM, R, EC
+
+
+def cloud_eval(P, N, A, tree: Octree, CM, R, EC, Q, beta: float = 2.0, nthreads: int = 0):
+    P, N, A, Q = _d(P), _d(N), _d(A).reshape(-1), _d(Q)
+    CM, R, EC = _d(CM), _d(R), _d(EC)
+    order = {3: 0, 12: 1, 39: 2}[EC.shape[1]]
+    W = np.empty(Q.shape[0], np.float64)
+    rc = lib().oracle_cloud_eval(_ptr(P), _ptr(N), _ptr(A), P.shape[0], _ptr(tree.pi_off),
+                                 _ptr(tree.pi_idx), _ptr(tree.CH), tree.ncells, _ptr(CM), _ptr(R),
+                                 _ptr(EC), order, _ptr(Q), Q.shape[0], float(beta), _ptr(W),
+                                 nthreads)
+    if rc:
+        raise ValueError("oracle_cloud_eval failed")
+    return W
+
+
+def cloud_fwn(P, N, A, Q, order: int = 2, beta: float = 2.0, nthreads: int = 0):
+    """One-shot point-cloud FWN: octree -> precompute -> eval (fast_winding_number.cpp:320-344)."""
+    t = octree(P)
+    CM, R, EC = cloud_precompute(P, N, A, t, order, nthreads)
+    return cloud_eval(P, N, A, t, CM, R, EC, Q, beta, nthreads)
+
+
+class SoupPort:
+    """CPU restatement of the HDK soup FWN (oracle/soup_port.cpp)."""
+
+    def __init__(self, V, F, order: int = 2):
+        self._V = _d(V)
+        self._F = _d(F, np.int32)
+        self._h = lib().oracle_soup_build(_ptr(self._V), self._V.shape[0], _ptr(self._F),
+                                          self._F.shape[0], order)
+
+    def eval(self, Q, accuracy_scale: float = 2.0, nthreads: int = 0) -> np.ndarray:
+        Q = _d(Q)
+        W = np.empty(Q.shape[0], np.float64)
+        lib().oracle_soup_eval(self._h, float(accuracy_scale), _ptr(Q), Q.shape[0], _ptr(W),
+                               nthreads)
+        return W
+
+    @property
+    def nodes(self) -> int:
+        return lib().oracle_soup_nodes(self._h)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().oracle_soup_free(self._h)
+            self._h = None
+
+
+_ref = None
+
+
+def ref_soup_available() -> bool:
+    return os.path.exists(REF_SOUP_PATH)
+
+
+def ref_lib():
+    global _ref
+    if _ref is None:
+        L = C.CDLL(REF_SOUP_PATH)
+        p = C.c_void_p
+        L.ref_soup_build.argtypes = [p, C.c_int64, p, C.c_int64, C.c_int]
+        L.ref_soup_build.restype = p
+        L.ref_soup_eval.argtypes = [p, C.c_float, p, C.c_int64, p]
+        L.ref_soup_free.argtypes = [p]
+        _ref = L
+    return _ref
+
+
+class RefSoup:
+    """The reference's own UT_SolidAngle soup FWN (only where the reference tree exists)."""
+
+    def __init__(self, V, F, order: int = 2):
+        self._V = _d(V)
+        self._F = _d(F, np.int32)
+        self._h = ref_lib().ref_soup_build(_ptr(self._V), self._V.shape[0], _ptr(self._F),
+                                           self._F.shape[0], order)
+
+    def eval(self, Q, accuracy_scale: float = 2.0) -> np.ndarray:
+        Q = _d(Q)
+        W = np.empty(Q.shape[0], np.float64)
+        ref_lib().ref_soup_eval(self._h, float(accuracy_scale), _ptr(Q), Q.shape[0], _ptr(W))
+        return W
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            ref_lib().ref_soup_free(self._h)
+            self._h = None

@@ -1,0 +1,119 @@
+"""CPU tests of the oracle itself: pinned against the reference's own golden
+vectors and known answers (tests/include/igl/fast_winding_number.cpp:17-53,
+tests/include/igl/signed_distance.cpp:4-42) and against analytic cases."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+
+def test_one_point_cloud_golden():
+    # tests/include/igl/fast_winding_number.cpp:17-53, tolerance 1e-15 (:52)
+    P = np.array([[0.1, 0.2, 0.3]])
+    N = np.array([[4.0, 5.0, 6.0]])
+    N /= np.linalg.norm(N[0])
+    A = np.array([0.7])
+    Q = np.array([[0, 0, 0], [4, -3, 2], [-1, 1, 3], [0, 5, -2]], float)
+    W = O.cloud_fwn(P, N, A, Q, order=2, beta=2.0)
+    expected = np.array([0.38779369004261133, -0.00041235296362485, -0.00362978253577090,
+                         -0.00041235296362485])
+    assert np.abs(W - expected).max() <= 1e-15
+
+
+TET_V = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], float)
+TET_F = np.array([[0, 1, 3], [0, 2, 1], [0, 3, 2], [1, 2, 3]], np.int32)
+
+
+def test_single_tet_exact():
+    # tests/include/igl/signed_distance.cpp:4-42: (.5,.5,.5) is outside the unit tet.
+    W = O.winding_number(TET_V, TET_F, [[0.5, 0.5, 0.5], [0.1, 0.1, 0.1]])
+    assert abs(W[0]) < 1e-15 and abs(W[1] - 1) < 1e-15
+
+
+def test_single_triangle_analytic():
+    # A unit right triangle seen from far along its normal: Omega ~ area / d^2.
+    a, b, c = [0, 0, 0], [1, 0, 0], [0, 1, 0]
+    for d in (10.0, 100.0, 1000.0):
+        w = O.solid_angle(a, b, c, [1 / 3, 1 / 3, d])
+        # solid angle of a small planar patch: A cos / d^2, sign: normal +z, point above
+        approx = -(0.5 / d ** 2) / (4 * np.pi)
+        assert abs(w - approx) / abs(approx) < 3.0 / d
+
+
+@pytest.mark.skipif(not O.ref_soup_available(), reason="reference tree not present")
+def test_reference_soup_single_tet_sign():
+    r = O.RefSoup(TET_V, TET_F)
+    W = r.eval(np.array([[0.5, 0.5, 0.5], [0.1, 0.1, 0.1]]))
+    assert abs(W[0]) < 1e-6 and abs(W[1] - 1) < 1e-6
+
+
+def _brute_octree(P):
+    """Independent pure-Python statement of octree.cpp:5-170 (recursive)."""
+    P = np.asarray(P, float)
+    n = P.shape[0]
+    pi, ch, cn, w = [list(range(n))], [[-1] * 8], [], []
+    mn, mx = P.min(0), P.max(0)
+    cn.append(((mn + mx) / 2.0).tolist())
+    w.append(float((mx - mn).max()))
+    m = [1]
+
+    def helper(index, depth):
+        if len(pi[index]) > 1 and depth < 30000:
+            ch[index] = [m[0] + i for i in range(8)]
+            h = w[index] / 2
+            c = cn[index]
+            for i in range(8):
+                ch.append([-1] * 8)
+                pi.append([])
+                hh = h / 2
+                cn.append([c[0] + (hh if i % 2 else -hh), c[1] + (hh if i in (2, 3, 6, 7) else -hh),
+                           c[2] + (hh if i > 3 else -hh)])
+                w.append(h)
+            for p in pi[index]:
+                o = int(P[p, 0] >= c[0]) + 2 * int(P[p, 1] >= c[1]) + 4 * int(P[p, 2] >= c[2])
+                pi[m[0] + o].append(p)
+            first = m[0]
+            m[0] += 8
+            for i in range(8):
+                helper(first + i, depth + 1)
+
+    helper(0, 0)
+    return pi, np.array(ch), np.array(cn), np.array(w)
+
+
+@pytest.mark.parametrize("seed,n", [(0, 1), (1, 2), (2, 9), (3, 40), (4, 150)])
+def test_octree_matches_recursive_statement(seed, n):
+    rng = np.random.default_rng(seed)
+    P = rng.random((n, 3))
+    t = O.octree(P)
+    pi, ch, cn, w = _brute_octree(P)
+    assert t.point_indices() == pi
+    assert np.array_equal(t.CH, ch)
+    assert np.array_equal(t.CN, cn)
+    assert np.array_equal(t.W, w)
+
+
+def test_octree_duplicate_points_reach_max_depth():
+    # Two identical points never separate: the split recurses to MAX_DEPTH =
+    # 30000 (octree.cpp:16, :98), emitting 8 cells per level.
+    P = np.array([[0.25, 0.5, 0.75], [0.25, 0.5, 0.75], [0.9, 0.1, 0.3]])
+    t = O.octree(P)
+    internal = (t.CH[:, 0] != -1).sum()
+    assert t.ncells == 1 + 8 * internal
+    assert internal == 30000  # the root (3 points) and the pair at depths 1..29999
+    sizes = np.diff(t.pi_off)
+    assert sizes.max() == 3 and (sizes == 2).sum() == 30000  # depths 1..30000
+
+
+def test_cloud_direct_matches_bh_far():
+    rng = np.random.default_rng(7)
+    P = rng.random((300, 3))
+    Nn = rng.normal(size=(300, 3))
+    Nn /= np.linalg.norm(Nn, axis=1, keepdims=True)
+    A = rng.random(300) * 0.01
+    Q = rng.random((50, 3)) * 8 + 5  # far from the cloud
+    t = O.octree(P)
+    CM, R, EC = O.cloud_precompute(P, Nn, A, t, 2)
+    Wbh = O.cloud_eval(P, Nn, A, t, CM, R, EC, Q, 2.0)
+    Wd = O.cloud_eval(P, Nn, A, t, CM, R, EC, Q, 0.0)
+    assert np.abs(Wbh - Wd).max() < 1e-3 * np.abs(Wd).max()  # order-3 truncation
