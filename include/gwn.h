@@ -110,6 +110,17 @@ int gwn_soup_eval(const gwn_soup* soup, float accuracy_scale, const void* Q, int
 int gwn_soup_stats_get(const gwn_soup* soup, gwn_soup_stats* out);
 void gwn_soup_free(gwn_soup* soup);
 
+/* Copies the built tree to host memory (for inspection and testing):
+ * nodes: num_nodes records of 24 doubles in pre-order,
+ *   {P[3], maxPDist2, N[3], Nxx, Nyy, Nzz, Nxy+Nyx, Nyz+Nzy, Nzx+Nxz,
+ *    Nxxx, Nyyy, Nzzz, 2(Nxyz+Nyzx+Nzxy), 2Nxxy+Nyxx, 2Nxxz+Nzxx,
+ *    2Nyyz+Nzyy, 2Nyyx+Nxyy, 2Nzzx+Nxzz, 2Nzzy+Nyzz, link}
+ *   where link (an int64 stored in the last slot's bytes) is >= 0 for an
+ *   internal node (index one past its subtree) and ~slot for a leaf;
+ * tri_index: num_triangles input-triangle ids, one per leaf slot.
+ * Either pointer may be NULL. */
+int gwn_soup_export(const gwn_soup* soup, double* nodes, int32_t* tri_index);
+
 /* ------------------------------------------------------------------------
  * Octree over a point cloud, bit-exact with igl::octree.
  * Replaces igl::octree(P,point_indices,CH,CN,W)  include/igl/octree.h:44-50

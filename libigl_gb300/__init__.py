@@ -143,3 +143,266 @@ def winding_number(V, F, O, precision="mixed", out_dtype=None):
                                  N.GWN_F64 if wdt == np.float64 else N.GWN_F32,
                                  _prec(precision), mem, stream))
     return W
+
+
+# ---------------------------------------------------------- triangle soup --
+class _SoupStats(C.Structure):
+    _fields_ = [("num_triangles", C.c_int64), ("num_nodes", C.c_int64),
+                ("device_bytes", C.c_int64), ("order", C.c_int32), ("max_depth", C.c_int32)]
+
+
+class FastWindingNumberBVH:
+    """Device-resident soup tree + moments (igl::FastWindingNumberBVH,
+    include/igl/fast_winding_number.h:140-147).  Built by
+    ``fast_winding_number_soup_precompute``; owns device copies of V and F."""
+
+    def __init__(self, V, F, order: int = 2):
+        L = N.load()
+        Va = _Arg(V, np.float64)
+        Fa = _Arg(F, np.int32, allowed=(np.int32,))
+        mem = _same_mem(Va, Fa)
+        if len(Va.shape) != 2 or Va.shape[1] != 3 or len(Fa.shape) != 2 or Fa.shape[1] != 3:
+            raise ValueError("V must be #V x 3 and F #F x 3")
+        h = C.c_void_p()
+        stream = _stream_ptr() if mem == N.GWN_DEVICE else None
+        N.check(L.gwn_soup_build(Va.ptr, Va.shape[0], Fa.ptr, Fa.shape[0], int(order), mem, stream,
+                                 C.byref(h)))
+        self._h = h
+        self.order = order
+
+    def eval(self, Q, accuracy_scale: float = 2.0, precision="mixed", out_dtype=None):
+        """W(p) = computeSolidAngle(p, accuracy_scale) / 4pi for every row of Q."""
+        L = N.load()
+        Qa = _Arg(Q)
+        if len(Qa.shape) != 2 or Qa.shape[1] != 3:
+            raise ValueError("Q must be #Q x 3")
+        wdt = np.dtype(out_dtype) if out_dtype is not None else Qa.np_dtype
+        W = _empty_like_mem(Qa.mem, (Qa.shape[0],), wdt, like=Qa)
+        stream = _stream_ptr() if Qa.mem == N.GWN_DEVICE else None
+        N.check(L.gwn_soup_eval(self._h, C.c_float(accuracy_scale), Qa.ptr, Qa.code, Qa.shape[0],
+                                _ptr_of(W), N.GWN_F64 if wdt == np.float64 else N.GWN_F32,
+                                _prec(precision), Qa.mem, stream))
+        return W
+
+    def eval_ptr(self, q_ptr, q_dtype: int, nq: int, w_ptr, w_dtype: int, accuracy_scale=2.0,
+                 precision="mixed", stream=None):
+        """Raw device-pointer evaluation (no allocation on the Python side)."""
+        N.check(N.load().gwn_soup_eval(self._h, C.c_float(accuracy_scale), C.c_void_p(q_ptr),
+                                       q_dtype, nq, C.c_void_p(w_ptr), w_dtype, _prec(precision),
+                                       N.GWN_DEVICE, C.c_void_p(stream)))
+
+    def export(self):
+        """(nodes (num_nodes x 24 float64, pre-order), links (int64), tri_index (int32))."""
+        st = self.stats
+        nodes = np.empty((st["num_nodes"], 24), np.float64)
+        tri = np.empty(st["num_triangles"], np.int32)
+        N.check(N.load().gwn_soup_export(self._h, nodes.ctypes.data_as(C.c_void_p),
+                                         tri.ctypes.data_as(C.c_void_p)))
+        links = nodes[:, 23].copy().view(np.int64)
+        return nodes, links, tri
+
+    @property
+    def stats(self) -> dict:
+        st = _SoupStats()
+        N.check(N.load().gwn_soup_stats_get(self._h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in _SoupStats._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            N.load().gwn_soup_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def fast_winding_number_soup_precompute(V, F, order: int = 2) -> FastWindingNumberBVH:
+    """igl::fast_winding_number(V,F,order,fwn_bvh) (fast_winding_number.h:176-181)."""
+    return FastWindingNumberBVH(V, F, order)
+
+
+def fast_winding_number_soup(V, F, Q, order: int = 2, accuracy_scale: float = 2.0,
+                             precision="mixed"):
+    """One-shot soup FWN, igl::fast_winding_number(V,F,Q,W) (fast_winding_number.h:157-163):
+    order 2, accuracy_scale 2."""
+    bvh = FastWindingNumberBVH(V, F, order)
+    try:
+        return bvh.eval(Q, accuracy_scale, precision)
+    finally:
+        bvh.close()
+
+
+# ---------------------------------------------------------------- octree --
+class Octree:
+    """igl::octree output (include/igl/octree.h:44-50), device-resident.
+
+    ``export()`` returns (pi_offsets, pi_indices, CH, CN, W): point_indices in
+    CSR form plus the child table, centres and widths, bit-exact with the
+    reference."""
+
+    def __init__(self, P):
+        L = N.load()
+        Pa = _Arg(P, np.float64)
+        if len(Pa.shape) != 2 or Pa.shape[1] != 3:
+            raise ValueError("P must be #P x 3")
+        h = C.c_void_p()
+        stream = _stream_ptr() if Pa.mem == N.GWN_DEVICE else None
+        N.check(L.gwn_octree_build(Pa.ptr, Pa.shape[0], Pa.mem, stream, C.byref(h)))
+        self._h = h
+        self.num_points = Pa.shape[0]
+
+    def sizes(self):
+        nc, ni, md = C.c_int64(), C.c_int64(), C.c_int32()
+        N.check(N.load().gwn_octree_sizes(self._h, C.byref(nc), C.byref(ni), C.byref(md)))
+        return nc.value, ni.value, md.value
+
+    def export(self):
+        nc, ni, _ = self.sizes()
+        off = np.empty(nc + 1, np.int64)
+        idx = np.empty(max(ni, 1), np.int32)
+        CH = np.empty((nc, 8), np.int32)
+        CN = np.empty((nc, 3), np.float64)
+        W = np.empty(nc, np.float64)
+        P = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+        N.check(N.load().gwn_octree_export(self._h, P(off), P(idx), P(CH), P(CN), P(W),
+                                           N.GWN_HOST, None))
+        return off, idx[:ni], CH, CN, W
+
+    def point_indices(self):
+        off, idx, *_ = self.export()
+        return [idx[off[c]:off[c + 1]].tolist() for c in range(off.shape[0] - 1)]
+
+    def close(self):
+        if getattr(self, "_h", None):
+            N.load().gwn_octree_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def octree(P):
+    """igl::octree(P, point_indices, CH, CN, W) -> (pi_offsets, pi_indices, CH, CN, W)."""
+    t = Octree(P)
+    try:
+        return t.export()
+    finally:
+        t.close()
+
+
+# ------------------------------------------------------------ point cloud --
+class CloudExpansion:
+    """Device-resident octree + order-k expansion of a point cloud
+    (igl::fast_winding_number precompute, fast_winding_number.h:35-53)."""
+
+    def __init__(self, P, Nrm, A, order: int = 2, tree: Octree | None = None):
+        L = N.load()
+        own = tree is None
+        if own:
+            tree = Octree(P)
+        Na = _Arg(Nrm, np.float64)
+        Aa = _Arg(np.asarray(A).reshape(-1) if not _is_torch_cuda(A) else A.reshape(-1),
+                  np.float64)
+        h = C.c_void_p()
+        stream = _stream_ptr() if Na.mem == N.GWN_DEVICE else None
+        N.check(L.gwn_cloud_build(tree._h, None, Na.ptr, Aa.ptr, int(order), Na.mem, stream,
+                                  C.byref(h)))
+        self._h = h
+        self.order = order
+        self.num_terms = {0: 3, 1: 12, 2: 39}[order]
+        self.tree = tree
+        self.ncells = tree.sizes()[0]
+
+    def export(self):
+        """(CM, R, EC) with one row per octree cell (rows >= #cells of the
+        reference's 8*#cells-row outputs are not produced)."""
+        nc = self.ncells
+        CM = np.empty((nc, 3))
+        R = np.empty(nc)
+        EC = np.empty((nc, self.num_terms))
+        P = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+        N.check(N.load().gwn_cloud_export(self._h, P(CM), P(R), P(EC), N.GWN_HOST, None))
+        return CM, R, EC
+
+    def eval(self, Q, beta: float = 2.0, precision="mixed", out_dtype=None):
+        L = N.load()
+        Qa = _Arg(Q)
+        if len(Qa.shape) != 2 or Qa.shape[1] != 3:
+            raise ValueError("Q must be #Q x 3")
+        wdt = np.dtype(out_dtype) if out_dtype is not None else Qa.np_dtype
+        W = _empty_like_mem(Qa.mem, (Qa.shape[0],), wdt, like=Qa)
+        stream = _stream_ptr() if Qa.mem == N.GWN_DEVICE else None
+        N.check(L.gwn_cloud_eval(self._h, C.c_double(beta), Qa.ptr, Qa.code, Qa.shape[0],
+                                 _ptr_of(W), N.GWN_F64 if wdt == np.float64 else N.GWN_F32,
+                                 _prec(precision), Qa.mem, stream))
+        return W
+
+    def close(self):
+        if getattr(self, "_h", None):
+            N.load().gwn_cloud_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def fast_winding_number_cloud_precompute(P, Nrm, A, pi_offsets, pi_indices, CH, order: int = 2):
+    """igl::fast_winding_number(P,N,A,point_indices,CH,expansion_order,CM,R,EC)
+    over caller-held octree arrays (host memory).  Returns (CM, R, EC) with
+    #cells rows."""
+    P, Nrm, A = _f64(P), _f64(Nrm), _f64(np.asarray(A).reshape(-1))
+    off = np.ascontiguousarray(pi_offsets, np.int64)
+    idx = np.ascontiguousarray(pi_indices, np.int32)
+    CH = np.ascontiguousarray(CH, np.int32)
+    nc = CH.shape[0]
+    nt = {0: 3, 1: 12, 2: 39}[order]
+    CM, R, EC = np.empty((nc, 3)), np.empty(nc), np.empty((nc, nt))
+    p = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    N.check(N.load().gwn_cloud_precompute_arrays(p(P), p(Nrm), p(A), P.shape[0], p(off), p(idx),
+                                                 p(CH), nc, int(order), p(CM), p(R), p(EC)))
+    return CM, R, EC
+
+
+def fast_winding_number_cloud(P, Nrm, A, pi_offsets, pi_indices, CH, CM, R, EC, Q,
+                              beta: float = 2.0, precision="mixed"):
+    """igl::fast_winding_number(P,N,A,point_indices,CH,CM,R,EC,Q,beta,WN) over
+    caller-held arrays (host memory); CM/R/EC may carry the reference's
+    8*#cells rows, only the first #cells are read."""
+    P, Nrm, A, Q = _f64(P), _f64(Nrm), _f64(np.asarray(A).reshape(-1)), _f64(Q)
+    off = np.ascontiguousarray(pi_offsets, np.int64)
+    idx = np.ascontiguousarray(pi_indices, np.int32)
+    CH = np.ascontiguousarray(CH, np.int32)
+    nc = CH.shape[0]
+    CM, R, EC = _f64(CM)[:nc], _f64(np.asarray(R).reshape(-1))[:nc], _f64(EC)[:nc]
+    order = {3: 0, 12: 1, 39: 2}[EC.shape[1]]
+    W = np.empty(Q.shape[0])
+    p = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    N.check(N.load().gwn_cloud_eval_arrays(p(P), p(Nrm), p(A), P.shape[0], p(off), p(idx), p(CH),
+                                           nc, p(CM), p(R), p(EC), order, p(Q), Q.shape[0],
+                                           float(beta), p(W), _prec(precision)))
+    return W
+
+
+def fast_winding_number_cloud_oneshot(P, Nrm, A, Q, order: int = 2, beta: float = 2.0,
+                                      precision="mixed"):
+    """igl::fast_winding_number(P,N,A,Q,order,beta,WN) (fast_winding_number.h:104-131):
+    octree -> precompute -> evaluate, all on the device."""
+    ce = CloudExpansion(P, Nrm, A, order)
+    try:
+        return ce.eval(Q, beta, precision)
+    finally:
+        ce.close()
+        ce.tree.close()

@@ -2,12 +2,16 @@
 // string, device status words, host/device staging of arguments).
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <mutex>
 #include <string>
 #include <vector>
 
 #include "gwn_common.cuh"
 #include "gwn_internal.cuh"
+#include "soup.cuh"
+#include "octree.cuh"
+#include "cloud.cuh"
 
 namespace gwn {
 
@@ -118,6 +122,24 @@ struct StagedBytes {
 
 using namespace gwn;
 
+struct gwn_soup {
+  gwn_soup_impl impl;
+};
+struct gwn_octree {
+  gwn_octree_impl impl;
+};
+struct gwn_cloud {
+  gwn_cloud_impl impl;
+};
+
+namespace {
+void check_device_of(int dev) {
+  int cur = 0;
+  GWN_CUDA(cudaGetDevice(&cur));
+  GWN_REQUIRE(cur == dev, "handle was built on another CUDA device than the current one");
+}
+}  // namespace
+
 extern "C" {
 
 const char* gwn_last_error(void) { return g_last_error.c_str(); }
@@ -164,6 +186,297 @@ int gwn_winding_number(const double* V, int64_t nV, int dim, const int32_t* F, i
                                  cudaMemcpyDeviceToHost, st));
       GWN_CUDA(cudaStreamSynchronize(st));
     }
+  });
+}
+
+int gwn_soup_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, int order,
+                   int mem, void* stream, gwn_soup** out) {
+  return guarded("gwn_soup_build", [&] {
+    GWN_REQUIRE(out != nullptr, "out must be non-null");
+    *out = nullptr;
+    GWN_REQUIRE(nV >= 0 && nF >= 0, "sizes must be non-negative");
+    GWN_REQUIRE(nF == 0 || (V && F), "V and F must be non-null");
+    check_mem(mem);
+    ensure_device();
+    cudaStream_t st = as_stream(stream);
+    Staged<double> dV(V, (size_t)nV * 3, mem, st);
+    Staged<int32_t> dF(F, (size_t)nF * 3, mem, st);
+    gwn_soup* s = new gwn_soup();
+    try {
+      GWN_CUDA(cudaGetDevice(&s->impl.device));
+      soup_build(s->impl, dV.dev, nV, dF.dev, nF, order, mem == GWN_HOST, st);
+      GWN_CUDA(cudaStreamSynchronize(st));
+    } catch (...) {
+      delete s;
+      throw;
+    }
+    *out = s;
+  });
+}
+
+int gwn_soup_eval(const gwn_soup* soup, float accuracy_scale, const void* Q, int q_dtype,
+                  int64_t nQ, void* W, int w_dtype, int precision, int mem, void* stream) {
+  return guarded("gwn_soup_eval", [&] {
+    GWN_REQUIRE(soup != nullptr, "soup handle is null");
+    GWN_REQUIRE(nQ >= 0, "nQ must be non-negative");
+    GWN_REQUIRE(nQ == 0 || (Q && W), "Q and W must be non-null");
+    GWN_REQUIRE(nQ < (int64_t(1) << 31), "at most 2^31-1 queries per call");
+    GWN_REQUIRE(std::isfinite(accuracy_scale), "accuracy_scale must be finite");
+    check_dtype(q_dtype, "Q");
+    check_dtype(w_dtype, "W");
+    check_precision(precision);
+    check_mem(mem);
+    ensure_device();
+    cudaStream_t st = as_stream(stream);
+    StagedBytes dQ(Q, (size_t)nQ * 3 * dtype_size(q_dtype), mem, st);
+    StagedBytes dW(W, (size_t)nQ * dtype_size(w_dtype), mem, st, false);
+    soup_eval(soup->impl, accuracy_scale, dQ.dev, q_dtype, nQ, dW.dev, w_dtype, precision, st);
+    if (mem == GWN_HOST) {
+      if (nQ)
+        GWN_CUDA(cudaMemcpyAsync(W, dW.dev, (size_t)nQ * dtype_size(w_dtype),
+                                 cudaMemcpyDeviceToHost, st));
+      GWN_CUDA(cudaStreamSynchronize(st));
+    }
+  });
+}
+
+int gwn_soup_stats_get(const gwn_soup* soup, gwn_soup_stats* out) {
+  return guarded("gwn_soup_stats_get", [&] {
+    GWN_REQUIRE(soup && out, "null argument");
+    out->num_triangles = soup->impl.n;
+    out->num_nodes = soup->impl.nnodes;
+    out->device_bytes = (int64_t)soup->impl.bytes;
+    out->order = soup->impl.order;
+    out->max_depth = soup->impl.max_depth;
+  });
+}
+
+void gwn_soup_free(gwn_soup* soup) { delete soup; }
+
+int gwn_soup_export(const gwn_soup* soup, double* nodes, int32_t* tri_index) {
+  return guarded("gwn_soup_export", [&] {
+    GWN_REQUIRE(soup != nullptr, "soup handle is null");
+    static_assert(sizeof(SoupNodeD) == 24 * sizeof(double), "node record layout");
+    const gwn_soup_impl& s = soup->impl;
+    if (nodes && s.nnodes)
+      GWN_CUDA(cudaMemcpy(nodes, s.nd.get(), s.nd.bytes(), cudaMemcpyDeviceToHost));
+    if (tri_index && s.n)
+      GWN_CUDA(cudaMemcpy(tri_index, s.tri_index.get(), s.tri_index.bytes(),
+                          cudaMemcpyDeviceToHost));
+  });
+}
+
+
+// ------------------------------------------------------------------ octree --
+int gwn_octree_build(const double* P, int64_t nP, int mem, void* stream, gwn_octree** out) {
+  return guarded("gwn_octree_build", [&] {
+    GWN_REQUIRE(out != nullptr, "out must be non-null");
+    *out = nullptr;
+    GWN_REQUIRE(nP >= 0, "nP must be non-negative");
+    GWN_REQUIRE(nP == 0 || P, "P must be non-null");
+    check_mem(mem);
+    ensure_device();
+    cudaStream_t st = as_stream(stream);
+    Staged<double> dP(P, (size_t)nP * 3, mem, st);
+    gwn_octree* t = new gwn_octree();
+    try {
+      GWN_CUDA(cudaGetDevice(&t->impl.device));
+      octree_build(t->impl, dP.dev, nP, mem == GWN_HOST, st);
+      GWN_CUDA(cudaStreamSynchronize(st));
+    } catch (...) {
+      delete t;
+      throw;
+    }
+    *out = t;
+  });
+}
+
+int gwn_octree_sizes(const gwn_octree* tree, int64_t* num_cells, int64_t* num_indices,
+                     int32_t* max_depth) {
+  return guarded("gwn_octree_sizes", [&] {
+    GWN_REQUIRE(tree != nullptr, "octree handle is null");
+    if (num_cells) *num_cells = tree->impl.ncells;
+    if (num_indices) *num_indices = tree->impl.nindices;
+    if (max_depth) *max_depth = tree->impl.max_depth;
+  });
+}
+
+int gwn_octree_export(const gwn_octree* tree, int64_t* pi_offsets, int32_t* pi_indices,
+                      int32_t* CH, double* CN, double* W, int mem, void* stream) {
+  return guarded("gwn_octree_export", [&] {
+    GWN_REQUIRE(tree != nullptr, "octree handle is null");
+    check_mem(mem);
+    check_device_of(tree->impl.device);
+    const gwn_octree_impl& t = tree->impl;
+    cudaStream_t st = as_stream(stream);
+    const size_t nc = (size_t)t.ncells;
+    const cudaMemcpyKind kind = mem == GWN_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    if (pi_offsets || pi_indices) {
+      DevBuf<int64_t> off(nc + 1, st);
+      DevBuf<int32_t> idx((size_t)std::max<int64_t>(t.nindices, 1), st);
+      octree_export_csr(t, off.get(), pi_indices ? idx.get() : nullptr, st);
+      if (pi_offsets) GWN_CUDA(cudaMemcpyAsync(pi_offsets, off.get(), (nc + 1) * 8, kind, st));
+      if (pi_indices && t.nindices)
+        GWN_CUDA(cudaMemcpyAsync(pi_indices, idx.get(), (size_t)t.nindices * 4, kind, st));
+      GWN_CUDA(cudaStreamSynchronize(st));
+    }
+    if (CH) GWN_CUDA(cudaMemcpyAsync(CH, t.ch.get(), nc * 8 * 4, kind, st));
+    if (CN) GWN_CUDA(cudaMemcpyAsync(CN, t.cn.get(), nc * 3 * 8, kind, st));
+    if (W) GWN_CUDA(cudaMemcpyAsync(W, t.w.get(), nc * 8, kind, st));
+    if (mem == GWN_HOST) GWN_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
+void gwn_octree_free(gwn_octree* tree) { delete tree; }
+
+// ------------------------------------------------------------------- cloud --
+int gwn_cloud_build(const gwn_octree* tree, const double* P, const double* N, const double* A,
+                    int order, int mem, void* stream, gwn_cloud** out) {
+  return guarded("gwn_cloud_build", [&] {
+    GWN_REQUIRE(out != nullptr, "out must be non-null");
+    *out = nullptr;
+    GWN_REQUIRE(tree != nullptr, "octree handle is null");
+    check_mem(mem);
+    check_device_of(tree->impl.device);
+    const int64_t n = tree->impl.n;
+    GWN_REQUIRE(n == 0 || (N && A), "N and A must be non-null");
+    (void)P;  // the octree handle holds its own copy of the points
+    cudaStream_t st = as_stream(stream);
+    Staged<double> dN(N, (size_t)n * 3, mem, st);
+    Staged<double> dA(A, (size_t)n, mem, st);
+    gwn_cloud* c = new gwn_cloud();
+    try {
+      c->impl.device = tree->impl.device;
+      cloud_build(c->impl, tree->impl, dN.dev, dA.dev, order, st);
+      GWN_CUDA(cudaStreamSynchronize(st));
+    } catch (...) {
+      delete c;
+      throw;
+    }
+    *out = c;
+  });
+}
+
+int gwn_cloud_export(const gwn_cloud* cloud, double* CM, double* R, double* EC, int mem,
+                     void* stream) {
+  return guarded("gwn_cloud_export", [&] {
+    GWN_REQUIRE(cloud != nullptr, "cloud handle is null");
+    check_mem(mem);
+    check_device_of(cloud->impl.device);
+    const gwn_cloud_impl& c = cloud->impl;
+    cudaStream_t st = as_stream(stream);
+    const cudaMemcpyKind kind = mem == GWN_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    const size_t nc = (size_t)c.ncells;
+    if (CM) GWN_CUDA(cudaMemcpyAsync(CM, c.CM.get(), nc * 24, kind, st));
+    if (R) GWN_CUDA(cudaMemcpyAsync(R, c.R.get(), nc * 8, kind, st));
+    if (EC) GWN_CUDA(cudaMemcpyAsync(EC, c.EC.get(), nc * c.num_terms * 8, kind, st));
+    if (mem == GWN_HOST) GWN_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
+int gwn_cloud_eval(const gwn_cloud* cloud, double beta, const void* Q, int q_dtype, int64_t nQ,
+                   void* W, int w_dtype, int precision, int mem, void* stream) {
+  return guarded("gwn_cloud_eval", [&] {
+    GWN_REQUIRE(cloud != nullptr, "cloud handle is null");
+    GWN_REQUIRE(nQ >= 0 && nQ < (int64_t(1) << 31), "0 <= nQ < 2^31");
+    GWN_REQUIRE(nQ == 0 || (Q && W), "Q and W must be non-null");
+    check_dtype(q_dtype, "Q");
+    check_dtype(w_dtype, "W");
+    check_precision(precision);
+    check_mem(mem);
+    check_device_of(cloud->impl.device);
+    cudaStream_t st = as_stream(stream);
+    StagedBytes dQ(Q, (size_t)nQ * 3 * dtype_size(q_dtype), mem, st);
+    StagedBytes dW(W, (size_t)nQ * dtype_size(w_dtype), mem, st, false);
+    cloud_eval(cloud->impl, beta, dQ.dev, q_dtype, nQ, dW.dev, w_dtype, precision, st);
+    if (mem == GWN_HOST) {
+      if (nQ)
+        GWN_CUDA(cudaMemcpyAsync(W, dW.dev, (size_t)nQ * dtype_size(w_dtype),
+                                 cudaMemcpyDeviceToHost, st));
+      GWN_CUDA(cudaStreamSynchronize(st));
+    }
+  });
+}
+
+void gwn_cloud_free(gwn_cloud* cloud) { delete cloud; }
+
+static void check_csr(const int64_t* pi_offsets, const int32_t* CH, int64_t ncells, int64_t nP) {
+  GWN_REQUIRE(ncells >= 1, "the octree needs at least the root cell");
+  GWN_REQUIRE(pi_offsets[0] == 0, "pi_offsets[0] must be 0");
+  for (int64_t c = 0; c < ncells; ++c) {
+    GWN_REQUIRE(pi_offsets[c + 1] >= pi_offsets[c], "pi_offsets must be non-decreasing");
+    if (CH[c * 8] != -1)
+      for (int k = 0; k < 8; ++k)
+        GWN_REQUIRE(CH[c * 8 + k] > 0 && CH[c * 8 + k] < ncells, "CH child id out of range");
+  }
+  (void)nP;
+}
+
+int gwn_cloud_precompute_arrays(const double* P, const double* N, const double* A, int64_t nP,
+                                const int64_t* pi_offsets, const int32_t* pi_indices,
+                                const int32_t* CH, int64_t ncells, int order, double* CM,
+                                double* R, double* EC) {
+  return guarded("gwn_cloud_precompute_arrays", [&] {
+    GWN_REQUIRE(nP >= 0 && ncells >= 1, "nP >= 0 and ncells >= 1");
+    GWN_REQUIRE(pi_offsets && CH && CM && R && EC, "null argument");
+    GWN_REQUIRE(order >= 0 && order <= 2, "expansion order must be 0, 1 or 2");
+    check_csr(pi_offsets, CH, ncells, nP);
+    const int64_t nidx = pi_offsets[ncells];
+    for (int64_t j = 0; j < nidx; ++j)
+      GWN_REQUIRE(pi_indices[j] >= 0 && pi_indices[j] < nP, "point index out of range");
+    ensure_device();
+    cudaStream_t st = nullptr;
+    Staged<double> dP(P, (size_t)nP * 3, GWN_HOST, st), dN(N, (size_t)nP * 3, GWN_HOST, st),
+        dA(A, (size_t)nP, GWN_HOST, st);
+    Staged<int64_t> doff(pi_offsets, (size_t)ncells + 1, GWN_HOST, st);
+    Staged<int32_t> didx(pi_indices, (size_t)nidx, GWN_HOST, st);
+    Staged<int32_t> dch(CH, (size_t)ncells * 8, GWN_HOST, st);
+    gwn_cloud_impl c;
+    cloud_build_arrays(c, dP.dev, dN.dev, dA.dev, nP, doff.dev, didx.dev, dch.dev, ncells, order,
+                       true, nullptr, nullptr, nullptr, st);
+    const int nt = c.num_terms;
+    GWN_CUDA(cudaMemcpyAsync(CM, c.CM.get(), (size_t)ncells * 24, cudaMemcpyDeviceToHost, st));
+    GWN_CUDA(cudaMemcpyAsync(R, c.R.get(), (size_t)ncells * 8, cudaMemcpyDeviceToHost, st));
+    GWN_CUDA(cudaMemcpyAsync(EC, c.EC.get(), (size_t)ncells * nt * 8, cudaMemcpyDeviceToHost, st));
+    GWN_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
+int gwn_cloud_eval_arrays(const double* P, const double* N, const double* A, int64_t nP,
+                          const int64_t* pi_offsets, const int32_t* pi_indices,
+                          const int32_t* CH, int64_t ncells, const double* CM, const double* R,
+                          const double* EC, int order, const double* Q, int64_t nQ,
+                          double beta, double* W, int precision) {
+  return guarded("gwn_cloud_eval_arrays", [&] {
+    GWN_REQUIRE(nP >= 0 && ncells >= 1 && nQ >= 0, "sizes");
+    GWN_REQUIRE(pi_offsets && CH && CM && R && EC, "null argument");
+    GWN_REQUIRE(nQ == 0 || (Q && W), "Q and W must be non-null");
+    GWN_REQUIRE(order >= 0 && order <= 2, "expansion order must be 0, 1 or 2");
+    check_precision(precision);
+    check_csr(pi_offsets, CH, ncells, nP);
+    const int64_t nidx = pi_offsets[ncells];
+    for (int64_t j = 0; j < nidx; ++j)
+      GWN_REQUIRE(pi_indices[j] >= 0 && pi_indices[j] < nP, "point index out of range");
+    ensure_device();
+    cudaStream_t st = nullptr;
+    Staged<double> dP(P, (size_t)nP * 3, GWN_HOST, st), dN(N, (size_t)nP * 3, GWN_HOST, st),
+        dA(A, (size_t)nP, GWN_HOST, st);
+    Staged<int64_t> doff(pi_offsets, (size_t)ncells + 1, GWN_HOST, st);
+    Staged<int32_t> didx(pi_indices, (size_t)nidx, GWN_HOST, st);
+    Staged<int32_t> dch(CH, (size_t)ncells * 8, GWN_HOST, st);
+    const int nt = order == 0 ? 3 : (order == 1 ? 12 : 39);
+    Staged<double> dCM(CM, (size_t)ncells * 3, GWN_HOST, st), dR(R, (size_t)ncells, GWN_HOST, st),
+        dEC(EC, (size_t)ncells * nt, GWN_HOST, st);
+    gwn_cloud_impl c;
+    cloud_build_arrays(c, dP.dev, dN.dev, dA.dev, nP, doff.dev, didx.dev, dch.dev, ncells, order,
+                       false, pi_offsets, pi_indices, CH, st);
+    cloud_set_moments(c, dCM.dev, dR.dev, dEC.dev, st);
+    cloud_emit_arrays(c, st);
+    Staged<double> dQ(Q, (size_t)nQ * 3, GWN_HOST, st);
+    Staged<double> dW(W, (size_t)nQ, GWN_HOST, st, false);
+    cloud_eval(c, beta, dQ.dev, GWN_F64, nQ, dW.dev, GWN_F64, precision, st);
+    if (nQ) GWN_CUDA(cudaMemcpyAsync(W, dW.dev, (size_t)nQ * 8, cudaMemcpyDeviceToHost, st));
+    GWN_CUDA(cudaStreamSynchronize(st));
   });
 }
 

@@ -1,0 +1,855 @@
+// Triangle-soup fast winding number: GPU tree build, HDK moments, and a
+// warp-coherent stackless Barnes-Hut traversal.
+//
+// Reference: UT_SolidAngle (include/igl/FastWindingNumberForSoups.h) behind
+// igl::fast_winding_number(V,F,order,bvh) / (bvh,accuracy_scale,Q,W)
+// (include/igl/fast_winding_number.cpp:380-455).  The reference builds a
+// 4-wide SAH BVH on the CPU; the tree is an internal detail of the opaque
+// FastWindingNumberBVH, so this path builds its own:
+//
+//  build (all on the device)
+//   1. per triangle: FP64 bounding box and centroid; boxes with a non-finite
+//      coordinate are excluded, as UT_BVH::init does (FWNFS.h:4606-4615);
+//   2. 63-bit Morton key of the centroid, stable radix sort;
+//   3. binary radix tree over the sorted keys (internal node i splits at the
+//      highest differing key bit, ties broken by index);
+//   4. one bottom-up pass: each leaf computes the HDK per-triangle data
+//      (area-weighted normal N, centroid P, the second-moment integrals
+//      Nijk; FWNFS.h:6668-6890), and the second thread to reach an internal
+//      node merges its two children with the parallel-axis shifts of
+//      FWNFS.h:6892-7118, all accumulated in FP64;
+//   5. pre-order positions (pre(child) = pre(parent) + 1 [+ size(left)]),
+//      then the nodes are written in pre-order as 96-byte FP32 records and
+//      192-byte FP64 records with a skip link (= end of subtree) or, for
+//      leaves, the triangle slot.
+//
+//  evaluate
+//   * queries are sorted by a 30-bit Morton key so that a warp's 32 queries
+//     are close together; the warp walks the pre-order node array as one:
+//     every lane evaluates the current node (a broadcast load) if it is
+//     still interested in it (node >= its resume index); the warp moves to
+//     node+1 when any lane opens the node, otherwise to the smallest resume
+//     index of the warp.  No stack, no per-lane divergence in the walk;
+//   * per node: open iff |q - P|^2 <= maxPDist2 * beta^2 (FWNFS.h:7176-7193);
+//     the root is always opened; otherwise the order-0/1/2 far field of
+//     FWNFS.h:7195-7251 is added (a non-finite value forces opening);
+//     opened leaves add the exact triangle solid angle (FWNFS.h:6070-6110);
+//   * mixed precision: FP32 records and arithmetic; the open test is redone
+//     in FP64 whenever the FP32 margin is inside a proven error band, so the
+//     mixed walk makes exactly the plain FP64 walk's decisions; exact
+//     triangle terms within 1e-3 * bbox diagonal of the query are computed in
+//     FP64 from the original vertices; results within 1e-3 of 0.5 are
+//     recomputed by the plain FP64 walk.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "bh_common.cuh"
+#include "gwn_common.cuh"
+#include "soup.cuh"
+#include "sort.cuh"
+
+namespace gwn {
+
+namespace {
+
+constexpr double kNearFrac = 1e-3;
+constexpr double kBand = 1e-3;
+constexpr float kInv4PiF = 0.079577471545947667884f;
+constexpr double kInv4Pi = 0.079577471545947667884;
+
+// Per-node FP64 build data (moments about the node's own average point P).
+struct BuildM {
+  double P[3], area, areaP[3], N[3], lo[3], hi[3];
+  double Nii[3], Nxy, Nyx, Nyz, Nzy, Nzx, Nxz;
+  double Niii[3], perm, c2[6];  // c2: 2Nxxy+Nyxx, 2Nxxz+Nzxx, 2Nyyz+Nzyy, 2Nyyx+Nxyy, 2Nzzx+Nxzz, 2Nzzy+Nyzz
+};
+
+// ------------------------------------------------------------- leaf data --
+// HDK per-triangle data, FWNFS.h:6668-6890, in FP64.
+__device__ void compute_integrals(const double* a, const double* b, const double* c,
+                                  const double* P, double* ii, double* ij, double* ik, int i) {
+  double oab[3], oac[3], ocb[3];
+  for (int d = 0; d < 3; ++d) {
+    oab[d] = b[d] - a[d];
+    oac[d] = c[d] - a[d];
+    ocb[d] = b[d] - c[d];
+  }
+  const double t = oab[i] / oac[i];
+  const int j = (i == 2) ? 0 : (i + 1);
+  const int k = (j == 2) ? 0 : (j + 1);
+  const double jdiff = t * oac[j] - oab[j];
+  const double kdiff = t * oac[k] - oab[k];
+  double ca0 = jdiff * oab[k] - kdiff * oab[j], ca1 = kdiff * oab[i], ca2 = jdiff * oab[i];
+  double cc0 = jdiff * ocb[k] - kdiff * ocb[j], cc1 = kdiff * ocb[i], cc2 = jdiff * ocb[i];
+  const double asa = sqrt(ca0 * ca0 + ca1 * ca1 + ca2 * ca2);
+  const double asc = sqrt(cc0 * cc0 + cc1 * cc1 + cc2 * cc2);
+  const double Pai = a[i] - P[i], Pci = c[i] - P[i];
+  const double ia = asa * (0.5 * Pai * Pai + (2.0 / 3.0) * Pai * oab[i] + 0.25 * oab[i] * oab[i]);
+  const double ic = asc * (0.5 * Pci * Pci + (2.0 / 3.0) * Pci * ocb[i] + 0.25 * ocb[i] * ocb[i]);
+  *ii = ia + ic;
+  for (int pass = 0; pass < 2; ++pass) {
+    double* out = pass == 0 ? ij : ik;
+    const int jk = pass == 0 ? j : k;
+    const double diff = pass == 0 ? jdiff : kdiff;
+    if (!out) continue;
+    const double obmid = b[jk] + 0.5 * diff;
+    const double oabmid = obmid - a[jk];
+    const double ocbmid = obmid - c[jk];
+    const double Paj = a[jk] - P[jk], Pcj = c[jk] - P[jk];
+    const double ija = asa * (0.5 * Pai * Paj + (1.0 / 3.0) * Pai * oabmid +
+                              (1.0 / 3.0) * Paj * oab[i] + 0.25 * oab[i] * oabmid);
+    const double ijc = asc * (0.5 * Pci * Pcj + (1.0 / 3.0) * Pci * ocbmid +
+                              (1.0 / 3.0) * Pcj * ocb[i] + 0.25 * ocb[i] * ocbmid);
+    *out = ija + ijc;
+  }
+}
+
+__device__ void sort3_axis(const double* v[3], int axis, int o[3]) {
+  o[0] = 0;
+  o[1] = 1;
+  o[2] = 2;
+  int t;
+  if (v[0][axis] > v[1][axis]) { t = o[0]; o[0] = o[1]; o[1] = t; }
+  if (v[o[0]][axis] > v[2][axis]) { t = o[0]; o[0] = o[2]; o[2] = t; }
+  if (v[o[1]][axis] > v[o[2]][axis]) { t = o[1]; o[1] = o[2]; o[2] = t; }
+}
+
+__device__ void leaf_moments(const double* a, const double* b, const double* c, int order,
+                             BuildM& m) {
+  double ab[3], ac[3];
+  for (int d = 0; d < 3; ++d) {
+    ab[d] = b[d] - a[d];
+    ac[d] = c[d] - a[d];
+    m.lo[d] = fmin(a[d], fmin(b[d], c[d]));
+    m.hi[d] = fmax(a[d], fmax(b[d], c[d]));
+  }
+  m.N[0] = 0.5 * (ab[1] * ac[2] - ab[2] * ac[1]);
+  m.N[1] = 0.5 * (ab[2] * ac[0] - ab[0] * ac[2]);
+  m.N[2] = 0.5 * (ab[0] * ac[1] - ab[1] * ac[0]);
+  const double area = sqrt(m.N[0] * m.N[0] + m.N[1] * m.N[1] + m.N[2] * m.N[2]);
+  for (int d = 0; d < 3; ++d) {
+    m.P[d] = (a[d] + b[d] + c[d]) / 3;
+    m.areaP[d] = m.P[d] * area;
+    m.Nii[d] = 0;
+    m.Niii[d] = 0;
+  }
+  m.area = area;
+  m.Nxy = m.Nyx = m.Nyz = m.Nzy = m.Nzx = m.Nxz = 0;
+  m.perm = 0;
+  for (int k = 0; k < 6; ++k) m.c2[k] = 0;
+  if (order < 2 || area == 0) return;
+  double n[3] = {m.N[0] / area, m.N[1] / area, m.N[2] / area};
+  const double* v[3] = {a, b, c};
+  int ox[3], oy[3], oz[3];
+  sort3_axis(v, 0, ox);
+  sort3_axis(v, 1, oy);
+  sort3_axis(v, 2, oz);
+  const double dx = v[ox[2]][0] - v[ox[0]][0];
+  const double dy = v[oy[2]][1] - v[oy[0]][1];
+  const double dz = v[oz[2]][2] - v[oz[0]][2];
+  double xx = 0, xy = 0, yy = 0, yz = 0, zz = 0, zx = 0;
+  if (dx > 0)
+    compute_integrals(v[ox[0]], v[ox[1]], v[ox[2]], m.P, &xx, (dx >= dy && dy > 0) ? &xy : nullptr,
+                      (dx >= dz && dz > 0) ? &zx : nullptr, 0);
+  if (dy > 0)
+    compute_integrals(v[oy[0]], v[oy[1]], v[oy[2]], m.P, &yy, (dy >= dz && dz > 0) ? &yz : nullptr,
+                      (dx < dy && dx > 0) ? &xy : nullptr, 1);
+  if (dz > 0)
+    compute_integrals(v[oz[0]], v[oz[1]], v[oz[2]], m.P, &zz, (dx < dz && dx > 0) ? &zx : nullptr,
+                      (dy < dz && dy > 0) ? &yz : nullptr, 2);
+  m.Niii[0] = xx * n[0];
+  m.Niii[1] = yy * n[1];
+  m.Niii[2] = zz * n[2];
+  m.perm = 2 * (n[0] * yz + n[1] * zx + n[2] * xy);
+  m.c2[0] = 2 * (n[0] * xy) + n[1] * xx;
+  m.c2[1] = 2 * (n[0] * zx) + n[2] * xx;
+  m.c2[2] = 2 * (n[1] * yz) + n[2] * yy;
+  m.c2[3] = 2 * (n[1] * xy) + n[0] * yy;
+  m.c2[4] = 2 * (n[2] * zx) + n[0] * zz;
+  m.c2[5] = 2 * (n[2] * yz) + n[1] * zz;
+}
+
+// Merge children (FWNFS.h:6892-7118 for two children).
+__device__ void merge_moments(const BuildM& L, const BuildM& R, BuildM& m) {
+  const BuildM* ch[2] = {&L, &R};
+  m.area = L.area + R.area;
+  for (int d = 0; d < 3; ++d) {
+    m.N[d] = L.N[d] + R.N[d];
+    m.areaP[d] = L.areaP[d] + R.areaP[d];
+    m.lo[d] = fmin(L.lo[d], R.lo[d]);
+    m.hi[d] = fmax(L.hi[d], R.hi[d]);
+  }
+  for (int d = 0; d < 3; ++d)
+    m.P[d] = m.area > 0 ? m.areaP[d] / m.area : 0.5 * (m.lo[d] + m.hi[d]);
+  for (int d = 0; d < 3; ++d) {
+    m.Nii[d] = 0;
+    m.Niii[d] = 0;
+  }
+  m.Nxy = m.Nyx = m.Nyz = m.Nzy = m.Nzx = m.Nxz = 0;
+  m.perm = 0;
+  for (int k = 0; k < 6; ++k) m.c2[k] = 0;
+  for (int c = 0; c < 2; ++c) {
+    const BuildM& C = *ch[c];
+    const double dx = C.P[0] - m.P[0], dy = C.P[1] - m.P[1], dz = C.P[2] - m.P[2];
+    const double* N = C.N;
+    m.Nii[0] += C.Nii[0] + N[0] * dx;
+    m.Nii[1] += C.Nii[1] + N[1] * dy;
+    m.Nii[2] += C.Nii[2] + N[2] * dz;
+    const double Nxy = C.Nxy + N[0] * dy, Nyx = C.Nyx + N[1] * dx;
+    const double Nyz = C.Nyz + N[1] * dz, Nzy = C.Nzy + N[2] * dy;
+    const double Nzx = C.Nzx + N[2] * dx, Nxz = C.Nxz + N[0] * dz;
+    m.Nxy += Nxy;
+    m.Nyx += Nyx;
+    m.Nyz += Nyz;
+    m.Nzy += Nzy;
+    m.Nzx += Nzx;
+    m.Nxz += Nxz;
+    m.Niii[0] += C.Niii[0] + 2 * dx * C.Nii[0] + dx * dx * N[0];
+    m.Niii[1] += C.Niii[1] + 2 * dy * C.Nii[1] + dy * dy * N[1];
+    m.Niii[2] += C.Niii[2] + 2 * dz * C.Nii[2] + dz * dz * N[2];
+    m.perm += C.perm + (dx * (Nyz + Nzy) + dy * (Nzx + Nxz) + dz * (Nxy + Nyx));
+    m.c2[0] += C.c2[0] + 2 * (dy * C.Nii[0] + dx * C.Nxy + N[0] * dx * dy) + 2 * C.Nyx * dx +
+               N[1] * dx * dx;
+    m.c2[1] += C.c2[1] + 2 * (dz * C.Nii[0] + dx * C.Nxz + N[0] * dx * dz) + 2 * C.Nzx * dx +
+               N[2] * dx * dx;
+    m.c2[2] += C.c2[2] + 2 * (dz * C.Nii[1] + dy * C.Nyz + N[1] * dy * dz) + 2 * C.Nzy * dy +
+               N[2] * dy * dy;
+    m.c2[3] += C.c2[3] + 2 * (dx * C.Nii[1] + dy * C.Nyx + N[1] * dy * dx) + 2 * C.Nxy * dy +
+               N[0] * dy * dy;
+    m.c2[4] += C.c2[4] + 2 * (dx * C.Nii[2] + dz * C.Nzx + N[2] * dz * dx) + 2 * C.Nxz * dz +
+               N[0] * dz * dz;
+    m.c2[5] += C.c2[5] + 2 * (dy * C.Nii[2] + dz * C.Nzy + N[2] * dz * dy) + 2 * C.Nyz * dz +
+               N[1] * dz * dz;
+  }
+}
+
+// ------------------------------------------------------------ build kernels --
+__global__ void tri_keys_kernel(const double* __restrict__ V, int64_t nV,
+                                const int32_t* __restrict__ F, int64_t nF,
+                                unsigned long long* __restrict__ cmm, int phase,
+                                unsigned long long* __restrict__ keys, int32_t* __restrict__ vals,
+                                unsigned* __restrict__ valid_count, unsigned* __restrict__ status) {
+  const int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  bool ok = f < nF;
+  double cen[3] = {0, 0, 0};
+  if (ok) {
+    for (int c = 0; c < 3; ++c) {
+      const int32_t idx = F[f * 3 + c];
+      if (idx < 0 || idx >= nV) {
+        atomicOr(status, kStatusBadInput);
+        ok = false;
+        break;
+      }
+      for (int d = 0; d < 3; ++d) {
+        const double v = V[(int64_t)idx * 3 + d];
+        if (!isfinite(v)) ok = false;
+        cen[d] += v;
+      }
+    }
+    for (int d = 0; d < 3; ++d) cen[d] /= 3.0;
+  }
+  if (phase == 0) {
+    // centroid bounding box of the kept triangles
+    for (int d = 0; d < 3; ++d) {
+      double lo = ok ? cen[d] : INFINITY, hi = ok ? cen[d] : -INFINITY;
+      for (int o = 16; o > 0; o >>= 1) {
+        lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+      }
+      if ((threadIdx.x & 31) == 0 && lo <= hi) {
+        atomicMin(&cmm[d], ordered_bits(lo));
+        atomicMax(&cmm[3 + d], ordered_bits(hi));
+      }
+    }
+    return;
+  }
+  if (f >= nF) return;
+  unsigned long long key = ~0ull;  // excluded triangles sort last
+  if (ok) {
+    key = 0;
+    for (int d = 0; d < 3; ++d) {
+      const double lo = from_ordered_bits(cmm[d]), hi = from_ordered_bits(cmm[3 + d]);
+      const double ext = hi - lo;
+      double t = ext > 0 ? (cen[d] - lo) / ext : 0.0;
+      t = fmin(fmax(t, 0.0), 1.0);
+      const unsigned long long q = (unsigned long long)fmin(t * 2097152.0, 2097151.0);
+      key |= spread21(q) << (2 - d);
+    }
+    atomicAdd(valid_count, 1u);
+  }
+  keys[f] = key;
+  vals[f] = (int32_t)f;
+}
+
+__device__ __forceinline__ int delta_key(const unsigned long long* keys, int n, int i, int j) {
+  if (j < 0 || j >= n) return -1;
+  const unsigned long long a = keys[i], b = keys[j];
+  if (a == b) return 64 + __clz((unsigned)(i ^ j));
+  return __clzll((long long)(a ^ b));
+}
+
+// Binary radix tree over n sorted keys: internal nodes 0..n-2, leaf j is node n-1+j.
+__global__ void radix_tree_kernel(const unsigned long long* __restrict__ keys, int n,
+                                  int32_t* __restrict__ left, int32_t* __restrict__ right,
+                                  int32_t* __restrict__ parent) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n - 1) return;
+  const int d = (delta_key(keys, n, i, i + 1) - delta_key(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+  const int dmin = delta_key(keys, n, i, i - d);
+  int lmax = 2;
+  while (delta_key(keys, n, i, i + lmax * d) > dmin) lmax <<= 1;
+  int l = 0;
+  for (int t = lmax >> 1; t >= 1; t >>= 1)
+    if (delta_key(keys, n, i, i + (l + t) * d) > dmin) l += t;
+  const int j = i + l * d;
+  const int dnode = delta_key(keys, n, i, j);
+  int s = 0;
+  int t = l;
+  do {
+    t = (t + 1) >> 1;
+    if (delta_key(keys, n, i, i + (s + t) * d) > dnode) s += t;
+  } while (t > 1);
+  const int gamma = i + s * d + min(d, 0);
+  const int lo = min(i, j), hi = max(i, j);
+  const int lc = (lo == gamma) ? (n - 1 + gamma) : gamma;
+  const int rc = (hi == gamma + 1) ? (n - 1 + gamma + 1) : (gamma + 1);
+  left[i] = lc;
+  right[i] = rc;
+  parent[lc] = i;
+  parent[rc] = i;
+}
+
+__global__ void bottom_up_kernel(const double* __restrict__ V, const int32_t* __restrict__ F,
+                                 const int32_t* __restrict__ sorted_tri, int n, int order,
+                                 const int32_t* __restrict__ left,
+                                 const int32_t* __restrict__ right,
+                                 const int32_t* __restrict__ parent, BuildM* __restrict__ M,
+                                 int32_t* __restrict__ size, unsigned* __restrict__ flags,
+                                 int32_t* __restrict__ depth_max) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const int node = n - 1 + j;
+  {
+    const int32_t f = sorted_tri[j];
+    double a[3], b[3], c[3];
+    for (int d = 0; d < 3; ++d) {
+      a[d] = V[(int64_t)F[(int64_t)f * 3 + 0] * 3 + d];
+      b[d] = V[(int64_t)F[(int64_t)f * 3 + 1] * 3 + d];
+      c[d] = V[(int64_t)F[(int64_t)f * 3 + 2] * 3 + d];
+    }
+    BuildM m;
+    leaf_moments(a, b, c, order, m);
+    M[node] = m;
+    size[node] = 1;
+  }
+  if (n == 1) return;
+  int cur = node;
+  int levels = 0;
+  while (true) {
+    const int p = parent[cur];
+    __threadfence();
+    if (atomicAdd(&flags[p], 1u) == 0) return;  // first child to arrive stops here
+    __threadfence();
+    const int lc = left[p], rc = right[p];
+    BuildM m;
+    merge_moments(M[lc], M[rc], m);
+    M[p] = m;
+    size[p] = 1 + size[lc] + size[rc];
+    ++levels;
+    if (p == 0) {
+      atomicMax(depth_max, levels);
+      return;
+    }
+    cur = p;
+  }
+}
+
+// pre-order position of every node: walk up, adding 1 per level plus the
+// left sibling's subtree size whenever the path enters a right child.
+__global__ void preorder_kernel(const int32_t* __restrict__ left,
+                                const int32_t* __restrict__ parent,
+                                const int32_t* __restrict__ size, int nnodes, int root,
+                                int32_t* __restrict__ pre, int32_t* __restrict__ depth) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= nnodes) return;
+  int p = 0, dep = 0, cur = x;
+  while (cur != root) {
+    const int par = parent[cur];
+    const int lc = left[par];
+    p += 1 + (lc == cur ? 0 : size[lc]);
+    ++dep;
+    cur = par;
+  }
+  pre[x] = p;
+  depth[x] = dep;
+}
+
+__global__ void emit_kernel(const BuildM* __restrict__ M, const int32_t* __restrict__ pre,
+                            const int32_t* __restrict__ size, int n,
+                            const double* __restrict__ V, const int32_t* __restrict__ F,
+                            const int32_t* __restrict__ sorted_tri, SoupNodeF* __restrict__ nf,
+                            SoupNodeD* __restrict__ nd, float4* __restrict__ tf,
+                            double* __restrict__ td) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nnodes = 2 * n - 1;
+  if (x >= nnodes) return;
+  const BuildM& m = M[x];
+  const int p = pre[x];
+  const bool leaf = x >= n - 1;
+  double mp[3];
+  for (int d = 0; d < 3; ++d) mp[d] = fmax(m.P[d] - m.lo[d], m.hi[d] - m.P[d]);
+  const double maxP2 = mp[0] * mp[0] + mp[1] * mp[1] + mp[2] * mp[2];
+  const int slot = leaf ? (x - (n - 1)) : -1;
+  const long long link = leaf ? (long long)~slot : (long long)(p + size[x]);
+  SoupNodeD D;
+  D.P[0] = m.P[0];
+  D.P[1] = m.P[1];
+  D.P[2] = m.P[2];
+  D.maxP2 = maxP2;
+  for (int d = 0; d < 3; ++d) {
+    D.N[d] = m.N[d];
+    D.Nii[d] = m.Nii[d];
+    D.Niii[d] = m.Niii[d];
+  }
+  D.Nxy_yx = m.Nxy + m.Nyx;
+  D.Nyz_zy = m.Nyz + m.Nzy;
+  D.Nzx_xz = m.Nzx + m.Nxz;
+  D.perm = m.perm;
+  for (int k = 0; k < 6; ++k) D.c2[k] = m.c2[k];
+  D.link = link;
+  nd[p] = D;
+  SoupNodeF Fr;
+  Fr.a = make_float4((float)D.P[0], (float)D.P[1], (float)D.P[2], (float)maxP2);
+  Fr.b = make_float4((float)D.N[0], (float)D.N[1], (float)D.N[2], (float)D.Nii[0]);
+  Fr.c = make_float4((float)D.Nii[1], (float)D.Nii[2], (float)D.Nxy_yx, (float)D.Nyz_zy);
+  Fr.d = make_float4((float)D.Nzx_xz, (float)D.Niii[0], (float)D.Niii[1], (float)D.Niii[2]);
+  Fr.e = make_float4((float)D.perm, (float)D.c2[0], (float)D.c2[1], (float)D.c2[2]);
+  Fr.f = make_float4((float)D.c2[3], (float)D.c2[4], (float)D.c2[5], __int_as_float((int)link));
+  nf[p] = Fr;
+  if (leaf) {
+    const int32_t f = sorted_tri[slot];
+    double v[9];
+    for (int c = 0; c < 3; ++c)
+      for (int d = 0; d < 3; ++d) v[c * 3 + d] = V[(int64_t)F[(int64_t)f * 3 + c] * 3 + d];
+    for (int k = 0; k < 9; ++k) td[(int64_t)slot * 9 + k] = v[k];
+    tf[(int64_t)slot * 3 + 0] = make_float4((float)v[0], (float)v[1], (float)v[2], (float)v[3]);
+    tf[(int64_t)slot * 3 + 1] = make_float4((float)v[4], (float)v[5], (float)v[6], (float)v[7]);
+    tf[(int64_t)slot * 3 + 2] = make_float4((float)v[8], 0.f, 0.f, 0.f);
+  }
+}
+
+// --------------------------------------------------------------- evaluate --
+// Far field of one node about its average point, FWNFS.h:7195-7251, with
+// (dx,dy,dz) = q - P and r2 = |q - P|^2.  T is float or double.
+template <typename T>
+struct Far {
+  T N[3], Nii[3], Nxy_yx, Nyz_zy, Nzx_xz, Niii[3], perm, c2[6];
+};
+
+template <typename T>
+__device__ __forceinline__ T far_field(const Far<T>& m, T dx, T dy, T dz, T r2, int order) {
+  const T m2 = T(1) / r2;
+  const T m1 = sqrt(m2);
+  const T qx = dx * m1, qy = dy * m1, qz = dz * m1;
+  T omega = -m2 * (qx * m.N[0] + qy * m.N[1] + qz * m.N[2]);
+  if (order >= 1) {
+    const T q2x = qx * qx, q2y = qy * qy, q2z = qz * qz;
+    const T m3 = m2 * m1;
+    omega += m3 * (m.Nii[0] + m.Nii[1] + m.Nii[2] -
+                   T(3) * (q2x * m.Nii[0] + q2y * m.Nii[1] + q2z * m.Nii[2] + qx * qy * m.Nxy_yx +
+                           qx * qz * m.Nzx_xz + qy * qz * m.Nyz_zy));
+    if (order >= 2) {
+      const T q3x = q2x * qx, q3y = q2y * qy, q3z = q2z * qz;
+      const T m4 = m2 * m2;
+      const T t0x = m.c2[3] + m.c2[4], t0y = m.c2[5] + m.c2[0], t0z = m.c2[1] + m.c2[2];
+      const T t1x = qy * m.c2[0] + qz * m.c2[1];
+      const T t1y = qz * m.c2[2] + qx * m.c2[3];
+      const T t1z = qx * m.c2[4] + qy * m.c2[5];
+      omega += m4 * (T(1.5) * (qx * (T(3) * m.Niii[0] + t0x) + qy * (T(3) * m.Niii[1] + t0y) +
+                               qz * (T(3) * m.Niii[2] + t0z)) -
+                     T(7.5) * (q3x * m.Niii[0] + q3y * m.Niii[1] + q3z * m.Niii[2] +
+                               qx * qy * qz * m.perm + q2x * t1x + q2y * t1y + q2z * t1z));
+    }
+  }
+  return omega;
+}
+
+// Exact triangle solid angle, FWNFS.h:6070-6110 (normalised corner vectors).
+template <typename T>
+__device__ __forceinline__ T tri_solid_angle(T ax, T ay, T az, T bx, T by, T bz, T cx, T cy,
+                                             T cz) {
+  const T la = sqrt(ax * ax + ay * ay + az * az);
+  const T lb = sqrt(bx * bx + by * by + bz * bz);
+  const T lc = sqrt(cx * cx + cy * cy + cz * cz);
+  if (la == T(0) || lb == T(0) || lc == T(0)) return T(0);
+  ax /= la; ay /= la; az /= la;
+  bx /= lb; by /= lb; bz /= lb;
+  cx /= lc; cy /= lc; cz /= lc;
+  const T ux = bx - ax, uy = by - ay, uz = bz - az;
+  const T vx = cx - ax, vy = cy - ay, vz = cz - az;
+  const T num = ax * (uy * vz - uz * vy) + ay * (uz * vx - ux * vz) + az * (ux * vy - uy * vx);
+  if (num == T(0)) return T(0);
+  const T den = T(1) + (ax * bx + ay * by + az * bz) + (ax * cx + ay * cy + az * cz) +
+                (bx * cx + by * cy + bz * cz);
+  return T(2) * atan2(num, den);
+}
+
+__device__ __forceinline__ Far<float> load_far(const SoupNodeF* r) {
+  const float4 b = __ldg(&r->b), c = __ldg(&r->c), d = __ldg(&r->d), e = __ldg(&r->e),
+               f = __ldg(&r->f);
+  Far<float> m;
+  m.N[0] = b.x; m.N[1] = b.y; m.N[2] = b.z;
+  m.Nii[0] = b.w; m.Nii[1] = c.x; m.Nii[2] = c.y;
+  m.Nxy_yx = c.z; m.Nyz_zy = c.w; m.Nzx_xz = d.x;
+  m.Niii[0] = d.y; m.Niii[1] = d.z; m.Niii[2] = d.w;
+  m.perm = e.x; m.c2[0] = e.y; m.c2[1] = e.z; m.c2[2] = e.w;
+  m.c2[3] = f.x; m.c2[4] = f.y; m.c2[5] = f.z;
+  return m;
+}
+
+__device__ __forceinline__ Far<double> load_far(const SoupNodeD* r) {
+  Far<double> m;
+  for (int d = 0; d < 3; ++d) {
+    m.N[d] = r->N[d];
+    m.Nii[d] = r->Nii[d];
+    m.Niii[d] = r->Niii[d];
+  }
+  m.Nxy_yx = r->Nxy_yx;
+  m.Nyz_zy = r->Nyz_zy;
+  m.Nzx_xz = r->Nzx_xz;
+  m.perm = r->perm;
+  for (int k = 0; k < 6; ++k) m.c2[k] = r->c2[k];
+  return m;
+}
+
+template <typename QT>
+__device__ __forceinline__ void read_query(const QT* Q, const int32_t* perm, const int32_t* list,
+                                           int64_t i, int64_t& qi, double& x, double& y,
+                                           double& z) {
+  qi = list ? (int64_t)list[i] : (perm ? (int64_t)perm[i] : i);
+  x = (double)Q[qi * 3 + 0];
+  y = (double)Q[qi * 3 + 1];
+  z = (double)Q[qi * 3 + 2];
+}
+
+struct EvalParams {
+  const SoupNodeF* nf;
+  const SoupNodeD* nd;
+  const float4* tf;
+  const double* td;
+  int nnodes;
+  int order;
+  float beta2f;
+  double beta2d;
+  float eps;       // near-field distance (1e-3 * bbox diagonal)
+  float cmax;      // max |coordinate| of any node centre
+  unsigned* status;
+};
+
+// Mixed-precision warp-coherent walk.  One query per lane.
+template <typename QT, typename WT>
+__global__ void __launch_bounds__(128) soup_eval_mixed_kernel(EvalParams prm, const QT* __restrict__ Q,
+                                                              const int32_t* __restrict__ perm,
+                                                              int64_t nQ, WT* __restrict__ W,
+                                                              int32_t* __restrict__ refine_list,
+                                                              unsigned* __restrict__ refine_count) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool valid = i < nQ;
+  int64_t qi = 0;
+  double qx = 0, qy = 0, qz = 0;
+  if (valid) read_query(Q, perm, (const int32_t*)nullptr, i, qi, qx, qy, qz);
+  const float fx = (float)qx, fy = (float)qy, fz = (float)qz;
+  const float S = fmaxf(fabsf(fx), fmaxf(fabsf(fy), fabsf(fz))) + prm.cmax;
+  const float sigma = guard_sigma(S);
+  float acc = 0.f;
+  double acc64 = 0.0;
+  int resume = valid ? 0 : 0x7fffffff;
+  int node = 0;
+  const unsigned full = 0xffffffffu;
+  while (node < prm.nnodes) {
+    const SoupNodeF* r = prm.nf + node;
+    const float4 a = __ldg(&r->a);
+    const int link = __float_as_int(__ldg(&r->f).w);
+    bool open = false;
+    if (node >= resume) {
+      const bool leaf = link < 0;
+      if (node == 0 && !leaf) {
+        open = true;
+      } else {
+        const float dx = fx - a.x, dy = fy - a.y, dz = fz - a.z;
+        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        const float thr = a.w * prm.beta2f;
+        bool near = r2 <= thr;
+        if (in_guard_band(r2, thr, sigma)) {
+          const SoupNodeD* rd = prm.nd + node;
+          near = open_test64(qx, qy, qz, rd->P[0], rd->P[1], rd->P[2], rd->maxP2, prm.beta2d);
+        }
+        if (!near) {
+          const float om = far_field<float>(load_far(r), dx, dy, dz, r2, prm.order);
+          if (isfinite(om)) {
+            acc += om;
+            resume = leaf ? node + 1 : link;
+          } else {
+            near = true;
+          }
+        }
+        if (near) {
+          if (leaf) {
+            const int slot = ~link;
+            const float rad = sqrtf(a.w) + prm.eps;
+            if (r2 <= rad * rad * 1.0001f) {
+              const double* t = prm.td + (int64_t)slot * 9;
+              acc64 += tri_solid_angle<double>(t[0] - qx, t[1] - qy, t[2] - qz, t[3] - qx,
+                                               t[4] - qy, t[5] - qz, t[6] - qx, t[7] - qy,
+                                               t[8] - qz);
+            } else {
+              const float4 t0 = __ldg(&prm.tf[(int64_t)slot * 3]);
+              const float4 t1 = __ldg(&prm.tf[(int64_t)slot * 3 + 1]);
+              const float4 t2 = __ldg(&prm.tf[(int64_t)slot * 3 + 2]);
+              acc += tri_solid_angle<float>(t0.x - fx, t0.y - fy, t0.z - fz, t0.w - fx, t1.x - fy,
+                                            t1.y - fz, t1.z - fx, t1.w - fy, t2.x - fz);
+            }
+            resume = node + 1;
+          } else {
+            open = true;
+          }
+        }
+      }
+    }
+    if (__any_sync(full, open))
+      node = node + 1;
+    else
+      node = __reduce_min_sync(full, resume);
+  }
+  if (!valid) return;
+  const double w = acc64 != 0.0 ? ((double)acc + acc64) * kInv4Pi : (double)(acc * kInv4PiF);
+  W[qi] = (WT)w;
+  if (fabs(w - 0.5) <= kBand) {
+    const unsigned s = atomicAdd(refine_count, 1u);
+    refine_list[s] = (int32_t)qi;
+  }
+}
+
+// Plain FP64 walk (also used, over a list, to re-evaluate threshold queries).
+template <typename QT, typename WT>
+__global__ void __launch_bounds__(128) soup_eval_fp64_kernel(EvalParams prm, const QT* __restrict__ Q,
+                                                             const int32_t* __restrict__ perm,
+                                                             const int32_t* __restrict__ list,
+                                                             const unsigned* __restrict__ list_count,
+                                                             int64_t nQ, WT* __restrict__ W) {
+  const int64_t n = list ? (int64_t)*list_count : nQ;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (list && blockIdx.x * (int64_t)blockDim.x >= n) return;  // whole warp idle
+  const bool valid = i < n;
+  int64_t qi = 0;
+  double qx = 0, qy = 0, qz = 0;
+  if (valid) read_query(Q, perm, list, i, qi, qx, qy, qz);
+  double acc = 0.0;
+  int resume = valid ? 0 : 0x7fffffff;
+  int node = 0;
+  const unsigned full = 0xffffffffu;
+  while (node < prm.nnodes) {
+    const SoupNodeD* r = prm.nd + node;
+    bool open = false;
+    if (node >= resume) {
+      const long long link = r->link;
+      const bool leaf = link < 0;
+      if (node == 0 && !leaf) {
+        open = true;
+      } else {
+        bool near = open_test64(qx, qy, qz, r->P[0], r->P[1], r->P[2], r->maxP2, prm.beta2d);
+        const double dx = qx - r->P[0], dy = qy - r->P[1], dz = qz - r->P[2];
+        const double r2 = dx * dx + dy * dy + dz * dz;
+        if (!near) {
+          const double om = far_field<double>(load_far(r), dx, dy, dz, r2, prm.order);
+          if (isfinite(om)) {
+            acc += om;
+            resume = leaf ? node + 1 : (int)link;
+          } else {
+            near = true;
+          }
+        }
+        if (near) {
+          if (leaf) {
+            const double* t = prm.td + (int64_t)(~link) * 9;
+            acc += tri_solid_angle<double>(t[0] - qx, t[1] - qy, t[2] - qz, t[3] - qx, t[4] - qy,
+                                           t[5] - qz, t[6] - qx, t[7] - qy, t[8] - qz);
+            resume = node + 1;
+          } else {
+            open = true;
+          }
+        }
+      }
+    }
+    if (__any_sync(full, open))
+      node = node + 1;
+    else
+      node = __reduce_min_sync(full, resume);
+  }
+  if (valid) W[qi] = (WT)(acc * kInv4Pi);
+}
+
+template <typename WT>
+__global__ void fill_zero_kernel(WT* w, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) w[i] = WT(0);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ build --
+void soup_build(gwn_soup_impl& s, const double* V, int64_t nV, const int32_t* F, int64_t nF,
+                int order, bool host_mode, cudaStream_t st) {
+  GWN_REQUIRE(order >= 0 && order <= 2, "order must be 0, 1 or 2");
+  GWN_REQUIRE(nF < (int64_t(1) << 30), "at most 2^30 triangles");
+  s.order = order;
+  s.n_input = nF;
+  DeviceStatus status(st, host_mode);
+  DevBuf<unsigned long long> cmm(6, st);
+  init_minmax(cmm.get(), 3, st);
+  DevBuf<unsigned long long> keys((size_t)std::max<int64_t>(nF, 1), st),
+      keys_tmp((size_t)std::max<int64_t>(nF, 1), st);
+  DevBuf<int32_t> vals((size_t)std::max<int64_t>(nF, 1), st),
+      vals_tmp((size_t)std::max<int64_t>(nF, 1), st);
+  DevBuf<unsigned> counters(2, st);
+  counters.zero(st);
+  const unsigned gridF = (unsigned)std::max<int64_t>(1, (nF + 255) / 256);
+  if (nF > 0) {
+    tri_keys_kernel<<<gridF, 256, 0, st>>>(V, nV, F, nF, cmm.get(), 0, keys.get(), vals.get(),
+                                           counters.get(), status.ptr());
+    tri_keys_kernel<<<gridF, 256, 0, st>>>(V, nV, F, nF, cmm.get(), 1, keys.get(), vals.get(),
+                                           counters.get(), status.ptr());
+    GWN_CUDA(cudaGetLastError());
+    radix_sort_pairs<unsigned long long>(keys.get(), vals.get(), keys_tmp.get(), vals_tmp.get(), nF,
+                                         0, 64, st);
+  }
+  unsigned nvalid = 0;
+  unsigned long long cmm_h[6];
+  GWN_CUDA(cudaMemcpyAsync(&nvalid, counters.get(), sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+  GWN_CUDA(cudaMemcpyAsync(cmm_h, cmm.get(), sizeof(cmm_h), cudaMemcpyDeviceToHost, st));
+  GWN_CUDA(cudaStreamSynchronize(st));
+  if (host_mode) status.check(st, "soup_build");
+  const int n = (int)nvalid;
+  s.n = n;
+  double lo[3], hi[3], diag2 = 0, cmax = 0;
+  for (int d = 0; d < 3; ++d) {
+    lo[d] = from_ordered_bits(cmm_h[d]);
+    hi[d] = from_ordered_bits(cmm_h[3 + d]);
+    if (n == 0) lo[d] = hi[d] = 0;
+    s.lo[d] = lo[d];
+    s.hi[d] = hi[d];
+  }
+  if (n == 0) {
+    s.nnodes = 0;
+    return;
+  }
+  const int nnodes = 2 * n - 1;
+  s.nnodes = nnodes;
+  DevBuf<int32_t> left((size_t)std::max(n - 1, 1), st), right((size_t)std::max(n - 1, 1), st);
+  DevBuf<int32_t> parent((size_t)nnodes, st), size((size_t)nnodes, st), pre((size_t)nnodes, st),
+      depth((size_t)nnodes, st);
+  DevBuf<unsigned> flags((size_t)std::max(n - 1, 1), st);
+  flags.zero(st);
+  DevBuf<BuildM> M((size_t)nnodes, st);
+  DevBuf<int32_t> dmax(1, st);
+  dmax.zero(st);
+  if (n > 1) {
+    radix_tree_kernel<<<(n - 1 + 255) / 256, 256, 0, st>>>(keys.get(), n, left.get(), right.get(),
+                                                           parent.get());
+    GWN_CUDA(cudaGetLastError());
+  }
+  bottom_up_kernel<<<(n + 127) / 128, 128, 0, st>>>(V, F, vals.get(), n, order, left.get(),
+                                                    right.get(), parent.get(), M.get(), size.get(),
+                                                    flags.get(), dmax.get());
+  GWN_CUDA(cudaGetLastError());
+  preorder_kernel<<<(nnodes + 255) / 256, 256, 0, st>>>(left.get(), parent.get(), size.get(),
+                                                        nnodes, 0, pre.get(),
+                                                        depth.get());
+  GWN_CUDA(cudaGetLastError());
+  s.tri_index.alloc((size_t)n);
+  GWN_CUDA(cudaMemcpyAsync(s.tri_index.get(), vals.get(), (size_t)n * sizeof(int32_t),
+                           cudaMemcpyDeviceToDevice, st));
+  s.nf.alloc((size_t)nnodes);
+  s.nd.alloc((size_t)nnodes);
+  s.tf.alloc((size_t)n * 3);
+  s.td.alloc((size_t)n * 9);
+  emit_kernel<<<(nnodes + 255) / 256, 256, 0, st>>>(M.get(), pre.get(), size.get(), n, V, F,
+                                                    vals.get(), s.nf.get(), s.nd.get(), s.tf.get(),
+                                                    s.td.get());
+  GWN_CUDA(cudaGetLastError());
+  int dm = 0;
+  BuildM root;
+  GWN_CUDA(cudaMemcpyAsync(&dm, dmax.get(), sizeof(int), cudaMemcpyDeviceToHost, st));
+  GWN_CUDA(cudaMemcpyAsync(&root, M.get(), sizeof(BuildM), cudaMemcpyDeviceToHost, st));
+  GWN_CUDA(cudaStreamSynchronize(st));
+  s.max_depth = dm;
+  // The root box bounds every kept vertex; node average points lie inside it.
+  for (int d = 0; d < 3; ++d) {
+    s.lo[d] = root.lo[d];
+    s.hi[d] = root.hi[d];
+    const double e = root.hi[d] - root.lo[d];
+    diag2 += e * e;
+    cmax = fmax(cmax, fmax(fabs(root.lo[d]), fabs(root.hi[d])));
+  }
+  s.eps = kNearFrac * sqrt(diag2);
+  s.cmax = cmax;
+  s.bytes = s.nf.bytes() + s.nd.bytes() + s.tf.bytes() + s.td.bytes() + s.tri_index.bytes();
+}
+
+// ------------------------------------------------------------------- eval --
+template <typename QT, typename WT>
+static void soup_eval_t(const gwn_soup_impl& s, float beta, const void* Qv, int64_t nQ, void* Wv,
+                        int precision, cudaStream_t st) {
+  const QT* Q = static_cast<const QT*>(Qv);
+  WT* W = static_cast<WT*>(Wv);
+  if (nQ == 0) return;
+  if (s.nnodes == 0) {
+    fill_zero_kernel<WT><<<(unsigned)((nQ + 255) / 256), 256, 0, st>>>(W, nQ);
+    GWN_CUDA(cudaGetLastError());
+    return;
+  }
+  EvalParams prm;
+  prm.nf = s.nf.get();
+  prm.nd = s.nd.get();
+  prm.tf = s.tf.get();
+  prm.td = s.td.get();
+  prm.nnodes = (int)s.nnodes;
+  prm.order = s.order;
+  prm.beta2f = beta * beta;
+  prm.beta2d = (double)beta * (double)beta;
+  prm.eps = (float)s.eps;
+  prm.cmax = (float)s.cmax;
+  prm.status = nullptr;
+  QueryOrder qo;
+  order_queries(Qv, sizeof(QT) == 8 ? GWN_F64 : GWN_F32, nQ, s.lo, s.hi, qo, st);
+  const int32_t* perm = qo.active ? qo.perm.get() : nullptr;
+  const unsigned grid = (unsigned)((nQ + 127) / 128);
+  if (precision == GWN_MIXED) {
+    DevBuf<int32_t> list((size_t)nQ, st);
+    DevBuf<unsigned> count(1, st);
+    count.zero(st);
+    soup_eval_mixed_kernel<QT, WT><<<grid, 128, 0, st>>>(prm, Q, perm, nQ, W, list.get(),
+                                                         count.get());
+    GWN_CUDA(cudaGetLastError());
+    soup_eval_fp64_kernel<QT, WT><<<grid, 128, 0, st>>>(prm, Q, nullptr, list.get(), count.get(),
+                                                        nQ, W);
+    GWN_CUDA(cudaGetLastError());
+  } else {
+    soup_eval_fp64_kernel<QT, WT><<<grid, 128, 0, st>>>(prm, Q, perm, nullptr, nullptr, nQ, W);
+    GWN_CUDA(cudaGetLastError());
+  }
+}
+
+void soup_eval(const gwn_soup_impl& s, float beta, const void* Q, int q_dtype, int64_t nQ, void* W,
+               int w_dtype, int precision, cudaStream_t st) {
+  const bool qd = q_dtype == GWN_F64, wd = w_dtype == GWN_F64;
+  if (qd && wd) soup_eval_t<double, double>(s, beta, Q, nQ, W, precision, st);
+  else if (qd) soup_eval_t<double, float>(s, beta, Q, nQ, W, precision, st);
+  else if (wd) soup_eval_t<float, double>(s, beta, Q, nQ, W, precision, st);
+  else soup_eval_t<float, float>(s, beta, Q, nQ, W, precision, st);
+}
+
+}  // namespace gwn

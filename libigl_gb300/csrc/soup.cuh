@@ -1,0 +1,56 @@
+// Device layout of a built triangle soup (the state behind gwn_soup).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "gwn_common.cuh"
+
+namespace gwn {
+
+// 96-byte FP32 node record, read by the mixed-precision walk.
+//   a: P (average point) xyz, maxPDist2
+//   b: N xyz, Nxx          c: Nyy, Nzz, Nxy+Nyx, Nyz+Nzy
+//   d: Nzx+Nxz, Nxxx, Nyyy, Nzzz
+//   e: 2(Nxyz+Nyzx+Nzxy), 2Nxxy+Nyxx, 2Nxxz+Nzxx, 2Nyyz+Nzyy
+//   f: 2Nyyx+Nxyy, 2Nzzx+Nxzz, 2Nzzy+Nyzz, link (int bits)
+// link >= 0: internal node, index one past its subtree (pre-order);
+// link < 0: leaf, triangle slot ~link.
+struct __align__(16) SoupNodeF {
+  float4 a, b, c, d, e, f;
+};
+
+// 192-byte FP64 node record (plain FP64 walk, FP64 re-checks).
+struct __align__(16) SoupNodeD {
+  double P[3], maxP2;
+  double N[3], Nii[3];
+  double Nxy_yx, Nyz_zy, Nzx_xz;
+  double Niii[3], perm, c2[6];
+  long long link;
+};
+
+struct gwn_soup_impl {
+  int device = 0;
+  int order = 2;
+  int64_t n_input = 0;   // triangles passed in
+  int64_t n = 0;         // triangles kept (finite, valid)
+  int64_t nnodes = 0;    // 2n-1
+  int max_depth = 0;
+  double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};  // bbox of kept vertices
+  double eps = 0;        // near-field distance: 1e-3 * bbox diagonal
+  double cmax = 0;       // max |coordinate| inside the bbox
+  DevMem<SoupNodeF> nf;
+  DevMem<SoupNodeD> nd;
+  DevMem<float4> tf;     // 3 float4 per slot: a.xyz b.x | b.yz c.xy | c.z
+  DevMem<double> td;     // 9 doubles per slot
+  DevMem<int32_t> tri_index;  // input triangle id per slot
+  size_t bytes = 0;
+};
+
+void soup_build(gwn_soup_impl& s, const double* V, int64_t nV, const int32_t* F, int64_t nF,
+                int order, bool host_mode, cudaStream_t st);
+void soup_eval(const gwn_soup_impl& s, float beta, const void* Q, int q_dtype, int64_t nQ,
+               void* W, int w_dtype, int precision, cudaStream_t st);
+
+}  // namespace gwn

@@ -76,6 +76,12 @@ def lib():
             L.oracle_soup_free.argtypes = [p]
             L.oracle_soup_nodes.argtypes = [p]
             L.oracle_soup_nodes.restype = i64
+        if hasattr(L, "oracle_soup_tree_eval"):
+            L.oracle_soup_tree_moments.argtypes = [p, p, p, i64, p, p]
+            L.oracle_soup_tree_moments_flat.argtypes = [p, p, p, i64, p, p]
+            L.oracle_soup_tree_eval.argtypes = [p, p, p, i64, p, C.c_int, C.c_float, p, i64, p,
+                                                C.c_int]
+            L.oracle_soup_leaf.argtypes = [p, p, p, p]
         if hasattr(L, "oracle_winding_number_hier"):
             L.oracle_winding_number_hier.argtypes = [p, i64, p, i64, p, i64, p, C.c_int]
             L.oracle_winding_number_hier.restype = C.c_int
@@ -262,3 +268,29 @@ class RefSoup:
         if getattr(self, "_h", None):
             ref_lib().ref_soup_free(self._h)
             self._h = None
+
+
+def soup_tree_moments(V, F, nodes, tri_index, flat: bool = False) -> np.ndarray:
+    """Every node's HDK moments recomputed on the CPU from its triangles:
+    two-child post() merges over the given tree, or (flat=True) the
+    grouping-independent exact shifts."""
+    V, F = _d(V), _d(F, np.int32)
+    nodes = _d(nodes)
+    tri_index = _d(tri_index, np.int32)
+    out = np.zeros_like(nodes)
+    fn = lib().oracle_soup_tree_moments_flat if flat else lib().oracle_soup_tree_moments
+    fn(_ptr(V), _ptr(F), _ptr(nodes), nodes.shape[0], _ptr(tri_index), _ptr(out))
+    return out
+
+
+def soup_tree_eval(V, F, nodes, tri_index, Q, accuracy_scale: float = 2.0, order: int = 2,
+                   nthreads: int = 0) -> np.ndarray:
+    """FP64 computeSolidAngle/(4 pi) walked over a given pre-order tree."""
+    V, F, Q = _d(V), _d(F, np.int32), _d(Q)
+    nodes = _d(nodes)
+    tri_index = _d(tri_index, np.int32)
+    W = np.empty(Q.shape[0], np.float64)
+    lib().oracle_soup_tree_eval(_ptr(V), _ptr(F), _ptr(nodes), nodes.shape[0], _ptr(tri_index),
+                                order, float(accuracy_scale), _ptr(Q), Q.shape[0], _ptr(W),
+                                nthreads)
+    return W
