@@ -172,6 +172,18 @@ int gwn_cloud_eval_arrays(const double* P, const double* N, const double* A, int
                           const double* EC, int order, const double* Q, int64_t nQ,
                           double beta, double* W, int precision);
 
+/* ------------------------------------------------------------------------
+ * Per-phase timing (no counterpart in the reference; for benchmarks and
+ * profiling).  After gwn_profile_enable(1), every call on this thread records
+ * CUDA events around its phases on its stream (e.g. "order_queries", "walk",
+ * "refine"); gwn_profile_read waits for the last call's events and returns
+ * the phase names ';'-separated and their durations in milliseconds.
+ * ---------------------------------------------------------------------- */
+int gwn_profile_enable(int on);
+int gwn_profile_read(char* names, int names_cap, float* ms, int max_phases, int* num_phases);
+/* Number of kernels this library has launched in this process (all threads). */
+unsigned long long gwn_launch_count(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -406,3 +406,34 @@ def fast_winding_number_cloud_oneshot(P, Nrm, A, Q, order: int = 2, beta: float 
     finally:
         ce.close()
         ce.tree.close()
+
+
+# ------------------------------------------------------------- profiling --
+def profile_enable(on: bool = True) -> None:
+    """Record CUDA events around each phase of this thread's calls."""
+    N.check(N.load().gwn_profile_enable(int(on)))
+
+
+def profile_read() -> dict:
+    """{phase name: milliseconds} of the last profiled call (waits for it)."""
+    names = C.create_string_buffer(4096)
+    ms = (C.c_float * 64)()
+    n = C.c_int(0)
+    N.check(N.load().gwn_profile_read(names, 4096, ms, 64, C.byref(n)))
+    keys = names.value.decode().split(";") if names.value else []
+    out = {}
+    for k, v in zip(keys, list(ms)[: n.value]):
+        out[k] = out.get(k, 0.0) + float(v)
+    return out
+
+
+def launch_count() -> int:
+    """Kernels launched by libgwn in this process so far."""
+    return int(N.load().gwn_launch_count())
+
+
+def launch_count_of(fn) -> int:
+    """Kernels libgwn launches while running fn() (same thread, nothing concurrent)."""
+    a = launch_count()
+    fn()
+    return launch_count() - a

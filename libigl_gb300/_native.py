@@ -49,6 +49,9 @@ SIGNATURES = {
     "gwn_cloud_eval": ([_p, _d, _p, _i, _i64, _p, _i, _i, _i, _p], _i),
     "gwn_cloud_free": ([_p], None),
     "gwn_cloud_precompute_arrays": ([_p, _p, _p, _i64, _p, _p, _p, _i64, _i, _p, _p, _p], _i),
+    "gwn_profile_enable": ([_i], _i),
+    "gwn_launch_count": ([], C.c_ulonglong),
+    "gwn_profile_read": ([_p, _i, _p, _i, _p], _i),
     "gwn_cloud_eval_arrays": ([_p, _p, _p, _i64, _p, _p, _p, _i64, _p, _p, _p, _i, _p, _i64, _d,
                                _p, _i], _i),
 }

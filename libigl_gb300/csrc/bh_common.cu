@@ -48,10 +48,10 @@ void order_queries(const void* Q, int q_dtype, int64_t nQ, const double lo[3], c
   out.perm.alloc((size_t)nQ, st);
   const unsigned grid = (unsigned)((nQ + 255) / 256);
   if (q_dtype == GWN_F64)
-    query_keys_kernel<double><<<grid, 256, 0, st>>>(static_cast<const double*>(Q), nQ, l, inv,
+    launch_kernel(query_keys_kernel<double>, grid, 256, 0, st, static_cast<const double*>(Q), nQ, l, inv,
                                                    keys.get(), out.perm.get());
   else
-    query_keys_kernel<float><<<grid, 256, 0, st>>>(static_cast<const float*>(Q), nQ, l, inv,
+    launch_kernel(query_keys_kernel<float>, grid, 256, 0, st, static_cast<const float*>(Q), nQ, l, inv,
                                                   keys.get(), out.perm.get());
   GWN_CUDA(cudaGetLastError());
   radix_sort_pairs<uint32_t>(keys.get(), out.perm.get(), keys_tmp.get(), tmp.get(), nQ, 0, 30, st);

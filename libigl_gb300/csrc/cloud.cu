@@ -565,7 +565,7 @@ void precompute(gwn_cloud_impl& c, const CsrView& v, int64_t ncells, const doubl
   c.EC.alloc((size_t)std::max<int64_t>(ncells, 1) * c.num_terms);
   if (ncells == 0) return;
   DevBuf<unsigned> nch((size_t)ncells, st), cbase((size_t)ncells, st);
-  chunk_count_kernel<<<blocks(ncells), 256, 0, st>>>(v.count, ncells, nch.get());
+  launch_kernel(chunk_count_kernel, blocks(ncells), 256, 0, st, v.count, ncells, nch.get());
   exclusive_scan_u32(nch.get(), cbase.get(), ncells, st);
   unsigned last_n = 0, last_b = 0;
   GWN_CUDA(cudaMemcpyAsync(&last_n, nch.get() + ncells - 1, 4, cudaMemcpyDeviceToHost, st));
@@ -573,26 +573,26 @@ void precompute(gwn_cloud_impl& c, const CsrView& v, int64_t ncells, const doubl
   GWN_CUDA(cudaStreamSynchronize(st));
   const int64_t nchunks = (int64_t)last_n + last_b;
   DevBuf<int32_t> chunk_cell((size_t)std::max<int64_t>(nchunks, 1), st);
-  chunk_fill_kernel<<<blocks(ncells), 256, 0, st>>>(nch.get(), cbase.get(), ncells, chunk_cell.get());
+  launch_kernel(chunk_fill_kernel, blocks(ncells), 256, 0, st, nch.get(), cbase.get(), ncells, chunk_cell.get());
   DevBuf<double> part((size_t)std::max<int64_t>(nchunks, 1) * 37, st);
   if (nchunks)
-    pass1_kernel<<<blocks(nchunks * 32), 256, 0, st>>>(v, chunk_cell.get(), cbase.get(), nchunks, P,
+    launch_kernel(pass1_kernel, blocks(nchunks * 32), 256, 0, st, v, chunk_cell.get(), cbase.get(), nchunks, P,
                                                       N, A, part.get());
-  combine1_kernel<<<blocks(ncells), 256, 0, st>>>(v.count, ncells, nch.get(), cbase.get(),
+  launch_kernel(combine1_kernel, blocks(ncells), 256, 0, st, v.count, ncells, nch.get(), cbase.get(),
                                                   part.get(), c.num_terms, c.CM.get(), c.EC.get());
   GWN_CUDA(cudaGetLastError());
   if (nchunks) {
     if (c.num_terms == 39)
-      pass2_kernel<39><<<blocks(nchunks * 32), 256, 0, st>>>(v, chunk_cell.get(), cbase.get(),
+      launch_kernel(pass2_kernel<39>, blocks(nchunks * 32), 256, 0, st, v, chunk_cell.get(), cbase.get(),
                                                             nchunks, P, N, A, c.CM.get(), part.get());
     else if (c.num_terms == 12)
-      pass2_kernel<12><<<blocks(nchunks * 32), 256, 0, st>>>(v, chunk_cell.get(), cbase.get(),
+      launch_kernel(pass2_kernel<12>, blocks(nchunks * 32), 256, 0, st, v, chunk_cell.get(), cbase.get(),
                                                             nchunks, P, N, A, c.CM.get(), part.get());
     else
-      pass2_kernel<3><<<blocks(nchunks * 32), 256, 0, st>>>(v, chunk_cell.get(), cbase.get(),
+      launch_kernel(pass2_kernel<3>, blocks(nchunks * 32), 256, 0, st, v, chunk_cell.get(), cbase.get(),
                                                            nchunks, P, N, A, c.CM.get(), part.get());
   }
-  combine2_kernel<<<blocks(ncells), 256, 0, st>>>(v.count, ncells, nch.get(), cbase.get(),
+  launch_kernel(combine2_kernel, blocks(ncells), 256, 0, st, v.count, ncells, nch.get(), cbase.get(),
                                                   part.get(), c.num_terms, c.R.get(), c.EC.get());
   GWN_CUDA(cudaGetLastError());
 }
@@ -632,7 +632,7 @@ __global__ void bbox3_kernel(const double* __restrict__ P, int64_t n,
 void points_bbox(const double* P, int64_t n, double lo[3], double hi[3], cudaStream_t st) {
   DevBuf<unsigned long long> mm(6, st);
   init_minmax(mm.get(), 3, st);
-  if (n) bbox3_kernel<<<std::min<unsigned>(blocks(n), 1024u), 256, 0, st>>>(P, n, mm.get());
+  if (n) launch_kernel(bbox3_kernel, std::min<unsigned>(blocks(n), 1024u), 256, 0, st, P, n, mm.get());
   unsigned long long h[6];
   GWN_CUDA(cudaMemcpyAsync(h, mm.get(), sizeof(h), cudaMemcpyDeviceToHost, st));
   GWN_CUDA(cudaStreamSynchronize(st));
@@ -670,14 +670,14 @@ void cloud_build(gwn_cloud_impl& c, const gwn_octree_impl& t, const double* N, c
   c.AN.alloc((size_t)std::max<int64_t>(n, 1) * 3);
   if (n) {
     GWN_CUDA(cudaMemcpyAsync(c.P.get(), t.P.get(), (size_t)n * 3 * 8, cudaMemcpyDeviceToDevice, st));
-    an_kernel<<<blocks(n), 256, 0, st>>>(N, A, n, c.AN.get());
+    launch_kernel(an_kernel, blocks(n), 256, 0, st, N, A, n, c.AN.get());
   }
   CsrView v{t.start.get(), t.count.get(), t.perm.get()};
   precompute(c, v, ncells, c.P.get(), N, A, st);
   // traversal order of non-empty cells
   DevBuf<unsigned long long> key((size_t)ncells, st), key_tmp((size_t)ncells, st);
   DevBuf<int32_t> val((size_t)ncells, st), val_tmp((size_t)ncells, st);
-  nonempty_keys_kernel<<<blocks(ncells), 256, 0, st>>>(t.start.get(), t.count.get(), t.depth.get(),
+  launch_kernel(nonempty_keys_kernel, blocks(ncells), 256, 0, st, t.start.get(), t.count.get(), t.depth.get(),
                                                        ncells, key.get(), val.get());
   radix_sort_pairs<unsigned long long>(key.get(), val.get(), key_tmp.get(), val_tmp.get(), ncells, 0,
                                        48, st);
@@ -685,7 +685,7 @@ void cloud_build(gwn_cloud_impl& c, const gwn_octree_impl& t, const double* N, c
   {
     DevBuf<unsigned long long> cnt(1, st);
     cnt.zero(st);
-    count_nonempty_kernel<<<blocks(ncells), 256, 0, st>>>(t.count.get(), ncells, cnt.get());
+    launch_kernel(count_nonempty_kernel, blocks(ncells), 256, 0, st, t.count.get(), ncells, cnt.get());
     unsigned long long h = 0;
     GWN_CUDA(cudaMemcpyAsync(&h, cnt.get(), 8, cudaMemcpyDeviceToHost, st));
     GWN_CUDA(cudaStreamSynchronize(st));
@@ -696,10 +696,10 @@ void cloud_build(gwn_cloud_impl& c, const gwn_octree_impl& t, const double* N, c
   c.nd.alloc((size_t)std::max<int64_t>(nnodes, 1));
   LayoutIn in{val.get(), nullptr, nullptr, key.get(), nnodes, t.start.get(), t.count.get(), t.ch.get(),
               t.depth.get(), c.CM.get(), c.R.get(), c.EC.get(), c.num_terms};
-  if (nnodes) emit_nodes_kernel<<<blocks(nnodes), 256, 0, st>>>(in, c.nf.get(), c.nd.get());
+  if (nnodes) launch_kernel(emit_nodes_kernel, blocks(nnodes), 256, 0, st, in, c.nf.get(), c.nd.get());
   c.pf.alloc((size_t)std::max<int64_t>(n, 1) * 2);
   c.pd.alloc((size_t)std::max<int64_t>(n, 1) * 6);
-  if (n) emit_points_kernel<<<blocks(n), 256, 0, st>>>(t.perm.get(), n, c.P.get(), c.AN.get(),
+  if (n) launch_kernel(emit_points_kernel, blocks(n), 256, 0, st, t.perm.get(), n, c.P.get(), c.AN.get(),
                                                       c.pf.get(), c.pd.get());
   GWN_CUDA(cudaGetLastError());
   finish_extent(c, st);
@@ -729,10 +729,10 @@ void cloud_build_arrays(gwn_cloud_impl& c, const double* P, const double* N, con
   c.AN.alloc((size_t)std::max<int64_t>(nP, 1) * 3);
   if (nP) {
     GWN_CUDA(cudaMemcpyAsync(c.P.get(), P, (size_t)nP * 24, cudaMemcpyDeviceToDevice, st));
-    an_kernel<<<blocks(nP), 256, 0, st>>>(N, A, nP, c.AN.get());
+    launch_kernel(an_kernel, blocks(nP), 256, 0, st, N, A, nP, c.AN.get());
   }
   DevBuf<int32_t> cnt((size_t)ncells, st);
-  csr_count_kernel<<<blocks(ncells), 256, 0, st>>>(pi_off_d, ncells, cnt.get());
+  launch_kernel(csr_count_kernel, blocks(ncells), 256, 0, st, pi_off_d, ncells, cnt.get());
   if (compute_moments) {
     CsrView v{pi_off_d, cnt.get(), pi_idx_d};
     precompute(c, v, ncells, c.P.get(), N, A, st);
@@ -791,7 +791,7 @@ void cloud_build_arrays(gwn_cloud_impl& c, const double* P, const double* N, con
   c.pf.alloc((size_t)std::max<int64_t>(nslots, 1) * 2);
   c.pd.alloc((size_t)std::max<int64_t>(nslots, 1) * 6);
   if (nslots)
-    emit_points_kernel<<<blocks(nslots), 256, 0, st>>>(slot_d.get(), nslots, c.P.get(), c.AN.get(),
+    launch_kernel(emit_points_kernel, blocks(nslots), 256, 0, st, slot_d.get(), nslots, c.P.get(), c.AN.get(),
                                                         c.pf.get(), c.pd.get());
   // node records need CM/R/EC: emitted by cloud_emit_arrays once moments exist
   c.layout_order = std::move(order_d);
@@ -808,7 +808,7 @@ void cloud_emit_arrays(gwn_cloud_impl& c, cudaStream_t st) {
   LayoutIn in{c.layout_order.get(), c.layout_first.get(), c.layout_skip.get(), nullptr, c.nnodes,
               c.layout_start.get(), c.layout_count.get(), c.layout_ch, nullptr, c.CM.get(),
               c.R.get(), c.EC.get(), c.num_terms};
-  if (c.nnodes) emit_nodes_kernel<<<blocks(c.nnodes), 256, 0, st>>>(in, c.nf.get(), c.nd.get());
+  if (c.nnodes) launch_kernel(emit_nodes_kernel, blocks(c.nnodes), 256, 0, st, in, c.nf.get(), c.nd.get());
   GWN_CUDA(cudaGetLastError());
 }
 
@@ -830,16 +830,16 @@ static void cloud_eval_t(const gwn_cloud_impl& c, double beta, const void* Qv, i
   WT* W = static_cast<WT*>(Wv);
   if (nQ == 0) return;
   if (c.n == 0 || c.nnodes == 0) {
-    fill_zero<WT><<<blocks(nQ), 256, 0, st>>>(W, nQ);
+    launch_kernel(fill_zero<WT>, blocks(nQ), 256, 0, st, W, nQ);
     GWN_CUDA(cudaGetLastError());
     return;
   }
   if (!(beta > 0)) {
     if (precision == GWN_MIXED)
-      cloud_direct_kernel<QT, WT, true><<<blocks(nQ), 256, 0, st>>>(c.pf.get(), c.pd.get(), c.n,
+      launch_kernel(cloud_direct_kernel<QT, WT, true>, blocks(nQ), 256, 0, st, c.pf.get(), c.pd.get(), c.n,
                                                                    (float)c.eps, Q, nQ, W);
     else
-      cloud_direct_kernel<QT, WT, false><<<blocks(nQ), 256, 0, st>>>(c.pf.get(), c.pd.get(), c.n,
+      launch_kernel(cloud_direct_kernel<QT, WT, false>, blocks(nQ), 256, 0, st, c.pf.get(), c.pd.get(), c.n,
                                                                     (float)c.eps, Q, nQ, W);
     GWN_CUDA(cudaGetLastError());
     return;
@@ -856,19 +856,31 @@ static void cloud_eval_t(const gwn_cloud_impl& c, double beta, const void* Qv, i
   prm.eps = (float)c.eps;
   prm.cmax = (float)c.cmax;
   QueryOrder qo;
-  order_queries(Qv, sizeof(QT) == 8 ? GWN_F64 : GWN_F32, nQ, c.lo, c.hi, qo, st);
+  {
+    PhaseTimer ph("order_queries", st);
+    order_queries(Qv, sizeof(QT) == 8 ? GWN_F64 : GWN_F32, nQ, c.lo, c.hi, qo, st);
+  }
   const int32_t* perm = qo.active ? qo.perm.get() : nullptr;
   const unsigned grid = blocks(nQ, 128);
   if (precision == GWN_MIXED) {
     DevBuf<int32_t> list((size_t)nQ, st);
     DevBuf<unsigned> count(1, st);
     count.zero(st);
-    cloud_eval_mixed_kernel<QT, WT><<<grid, 128, 0, st>>>(prm, Q, perm, nQ, W, list.get(), count.get());
+    {
+      PhaseTimer ph("walk", st);
+      launch_kernel(cloud_eval_mixed_kernel<QT, WT>, grid, 128, 0, st, prm, Q, perm, nQ, W, list.get(),
+                                                            count.get());
+    }
     GWN_CUDA(cudaGetLastError());
-    cloud_eval_fp64_kernel<QT, WT><<<grid, 128, 0, st>>>(prm, Q, nullptr, list.get(), count.get(), nQ, W);
+    {
+      PhaseTimer ph("refine", st);
+      launch_kernel(cloud_eval_fp64_kernel<QT, WT>, grid, 128, 0, st, prm, Q, nullptr, list.get(),
+                                                           count.get(), nQ, W);
+    }
     GWN_CUDA(cudaGetLastError());
   } else {
-    cloud_eval_fp64_kernel<QT, WT><<<grid, 128, 0, st>>>(prm, Q, perm, nullptr, nullptr, nQ, W);
+    PhaseTimer ph("walk", st);
+    launch_kernel(cloud_eval_fp64_kernel<QT, WT>, grid, 128, 0, st, prm, Q, perm, nullptr, nullptr, nQ, W);
     GWN_CUDA(cudaGetLastError());
   }
 }

@@ -485,12 +485,12 @@ void launch_exact3(const ExactArgs& a, cudaStream_t st) {
   DeviceStatus status(st, a.host_mode);
   DevBuf<unsigned long long> mm(6, st);
   init_minmax(mm.get(), 3, st);
-  bbox_kernel<<<std::max(1, std::min(num_sms() * 4, (int)((a.nV + 255) / 256))), 256, 0, st>>>(
+  launch_kernel(bbox_kernel, std::max(1, std::min(num_sms() * 4, (int)((a.nV + 255) / 256))), 256, 0, st, 
       a.V, a.nV, 3, mm.get());
   DevBuf<TriF> tris((size_t)std::max<int64_t>(nPad, 1), st);
   DevBuf<double> tris64((size_t)std::max<int64_t>(nPad, 1) * 9, st);
   if (nPad > 0) {
-    pack_tris_kernel<<<(unsigned)((nPad + 255) / 256), 256, 0, st>>>(
+    launch_kernel(pack_tris_kernel, (unsigned)((nPad + 255) / 256), 256, 0, st, 
         a.V, a.nV, a.F, a.nF, nPad, mm.get(), tris.get(), tris64.get(), status.ptr());
   }
   const unsigned grid = (unsigned)((a.nQ + kThreads - 1) / kThreads);
@@ -498,7 +498,7 @@ void launch_exact3(const ExactArgs& a, cudaStream_t st) {
   WT* W = static_cast<WT*>(a.W);
   if (a.precision == GWN_MIXED) {
     DevBuf<float4> meta((size_t)std::max(ntiles, 1), st);
-    if (ntiles > 0) tile_meta_kernel<<<ntiles, kTile, 0, st>>>(tris.get(), ntiles, mm.get(), meta.get());
+    if (ntiles > 0) launch_kernel(tile_meta_kernel, ntiles, kTile, 0, st, tris.get(), ntiles, mm.get(), meta.get());
     DevBuf<int32_t> list((size_t)std::max<int64_t>(a.nQ, 1), st);
     DevBuf<unsigned> count(1, st);
     count.zero(st);
@@ -506,12 +506,18 @@ void launch_exact3(const ExactArgs& a, cudaStream_t st) {
       const size_t smem = sizeof(Smem3);
       GWN_CUDA(cudaFuncSetAttribute(exact3_mixed_kernel<QT, WT>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      exact3_mixed_kernel<QT, WT><<<grid, kThreads, smem, st>>>(
-          tris.get(), tris64.get(), meta.get(), ntiles, Q, a.nQ, W, list.get(), count.get(),
-          status.ptr());
+      {
+        PhaseTimer ph("nbody", st);
+        launch_kernel(exact3_mixed_kernel<QT, WT>, grid, kThreads, smem, st, 
+            tris.get(), tris64.get(), meta.get(), ntiles, Q, a.nQ, W, list.get(), count.get(),
+            status.ptr());
+      }
       GWN_CUDA(cudaGetLastError());
-      exact3_refine_kernel<QT, WT><<<num_sms() * 4, kThreads, 0, st>>>(
-          tris64.get(), a.nF, Q, W, list.get(), count.get());
+      {
+        PhaseTimer ph("refine", st);
+        launch_kernel(exact3_refine_kernel<QT, WT>, num_sms() * 4, kThreads, 0, st, 
+            tris64.get(), a.nF, Q, W, list.get(), count.get());
+      }
       GWN_CUDA(cudaGetLastError());
     }
     status.check(st, "winding_number (mixed)");
@@ -522,7 +528,8 @@ void launch_exact3(const ExactArgs& a, cudaStream_t st) {
       const size_t smem = sizeof(Smem64);
       GWN_CUDA(cudaFuncSetAttribute(exact3_fp64_kernel<QT, WT>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      exact3_fp64_kernel<QT, WT><<<grid, kThreads, smem, st>>>(tris64.get(), ntiles64, Q,
+      PhaseTimer ph("nbody", st);
+      launch_kernel(exact3_fp64_kernel<QT, WT>, grid, kThreads, smem, st, tris64.get(), ntiles64, Q,
                                                                 a.nQ, W, status.ptr());
       GWN_CUDA(cudaGetLastError());
     }
@@ -534,7 +541,7 @@ template <typename QT, typename WT>
 void launch_exact2(const ExactArgs& a, cudaStream_t st) {
   DeviceStatus status(st, a.host_mode);
   if (a.nQ > 0) {
-    exact2_kernel<QT, WT><<<(unsigned)((a.nQ + 127) / 128), 128, 0, st>>>(
+    launch_kernel(exact2_kernel<QT, WT>, (unsigned)((a.nQ + 127) / 128), 128, 0, st, 
         a.V, a.nV, a.F, a.nF, static_cast<const QT*>(a.Q), a.nQ, static_cast<WT*>(a.W),
         status.ptr());
     GWN_CUDA(cudaGetLastError());

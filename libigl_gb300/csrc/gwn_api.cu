@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstring>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -23,6 +24,49 @@ std::vector<int> g_sms;               // per device
 }  // namespace
 
 void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+namespace {
+std::atomic<unsigned long long> g_launches{0};
+}
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+namespace {
+struct PhaseRec {
+  std::string name;
+  cudaEvent_t start = nullptr, stop = nullptr;
+};
+thread_local bool g_profile = false;
+thread_local std::vector<PhaseRec> g_phases;
+void clear_phases() {
+  for (auto& p : g_phases) {
+    if (p.start) cudaEventDestroy(p.start);
+    if (p.stop) cudaEventDestroy(p.stop);
+  }
+  g_phases.clear();
+}
+}  // namespace
+
+void profile_begin_call() {
+  if (g_profile) clear_phases();
+}
+
+PhaseTimer::PhaseTimer(const char* name, cudaStream_t st) {
+  if (!g_profile) return;
+  g_phases.emplace_back();
+  PhaseRec& r = g_phases.back();
+  r.name = name;
+  cudaEventCreate(&r.start);
+  cudaEventCreate(&r.stop);
+  cudaEventRecord(r.start, st);
+  rec = new std::pair<size_t, cudaStream_t>(g_phases.size() - 1, st);
+}
+
+PhaseTimer::~PhaseTimer() {
+  if (!rec) return;
+  auto* p = static_cast<std::pair<size_t, cudaStream_t>*>(rec);
+  if (p->first < g_phases.size()) cudaEventRecord(g_phases[p->first].stop, p->second);
+  delete p;
+}
 
 void ensure_device() {
   int n = 0;
@@ -82,7 +126,7 @@ __global__ void init_minmax_kernel(unsigned long long* mm, int dim) {
 }
 
 void init_minmax(unsigned long long* mm, int dim, cudaStream_t s) {
-  init_minmax_kernel<<<1, 32, 0, s>>>(mm, dim);
+  launch_kernel(init_minmax_kernel, 1, 32, 0, s, mm, dim);
   GWN_CUDA(cudaGetLastError());
 }
 
@@ -162,6 +206,7 @@ int gwn_winding_number(const double* V, int64_t nV, int dim, const int32_t* F, i
                        const void* O, int o_dtype, int64_t nO, void* W, int w_dtype,
                        int precision, int mem, void* stream) {
   return guarded("gwn_winding_number", [&] {
+    profile_begin_call();
     GWN_REQUIRE(dim == 2 || dim == 3, "dim must be 2 (edges) or 3 (triangles)");
     GWN_REQUIRE(nV >= 0 && nF >= 0 && nO >= 0, "sizes must be non-negative");
     GWN_REQUIRE(nF == 0 || (V && F), "V and F must be non-null");
@@ -217,6 +262,7 @@ int gwn_soup_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, in
 int gwn_soup_eval(const gwn_soup* soup, float accuracy_scale, const void* Q, int q_dtype,
                   int64_t nQ, void* W, int w_dtype, int precision, int mem, void* stream) {
   return guarded("gwn_soup_eval", [&] {
+    profile_begin_call();
     GWN_REQUIRE(soup != nullptr, "soup handle is null");
     GWN_REQUIRE(nQ >= 0, "nQ must be non-negative");
     GWN_REQUIRE(nQ == 0 || (Q && W), "Q and W must be non-null");
@@ -377,6 +423,7 @@ int gwn_cloud_export(const gwn_cloud* cloud, double* CM, double* R, double* EC, 
 int gwn_cloud_eval(const gwn_cloud* cloud, double beta, const void* Q, int q_dtype, int64_t nQ,
                    void* W, int w_dtype, int precision, int mem, void* stream) {
   return guarded("gwn_cloud_eval", [&] {
+    profile_begin_call();
     GWN_REQUIRE(cloud != nullptr, "cloud handle is null");
     GWN_REQUIRE(nQ >= 0 && nQ < (int64_t(1) << 31), "0 <= nQ < 2^31");
     GWN_REQUIRE(nQ == 0 || (Q && W), "Q and W must be non-null");
@@ -479,5 +526,39 @@ int gwn_cloud_eval_arrays(const double* P, const double* N, const double* A, int
     GWN_CUDA(cudaStreamSynchronize(st));
   });
 }
+
+
+// ---------------------------------------------------------------- profile --
+int gwn_profile_enable(int on) {
+  return guarded("gwn_profile_enable", [&] {
+    g_profile = on != 0;
+    if (!g_profile) clear_phases();
+  });
+}
+
+int gwn_profile_read(char* names, int names_cap, float* ms, int max_phases, int* num_phases) {
+  return guarded("gwn_profile_read", [&] {
+    std::string all;
+    int n = 0;
+    for (auto& p : g_phases) {
+      float t = 0.f;
+      GWN_CUDA(cudaEventSynchronize(p.stop));
+      GWN_CUDA(cudaEventElapsedTime(&t, p.start, p.stop));
+      if (n < max_phases && ms) ms[n] = t;
+      if (!all.empty()) all += ";";
+      all += p.name;
+      ++n;
+    }
+    if (names && names_cap > 0) {
+      const size_t k = std::min<size_t>((size_t)names_cap - 1, all.size());
+      memcpy(names, all.data(), k);
+      names[k] = 0;
+    }
+    if (num_phases) *num_phases = n;
+  });
+}
+
+
+unsigned long long gwn_launch_count(void) { return g_launches.load(); }
 
 }  // extern "C"

@@ -9,6 +9,7 @@
 #include <stdexcept>
 #include <string>
 #include <utility>
+#include <atomic>
 
 #include "../../include/gwn.h"
 
@@ -174,6 +175,28 @@ struct DeviceStatus {
   // failure.  Device mode: no-op (the sticky word keeps the report).
   void check(cudaStream_t s, const char* where) const;
 };
+
+// Optional per-phase timing of the calling thread's ABI calls (CUDA events
+// recorded on the launch stream).  Off unless gwn_profile_enable(1).
+struct PhaseTimer {
+  PhaseTimer(const char* name, cudaStream_t st);
+  ~PhaseTimer();
+  void* rec = nullptr;
+};
+void profile_begin_call();
+
+// Every kernel of the library is launched through launch_kernel: the launch
+// is checked and counted (gwn_launch_count()).
+void count_launch();
+#ifdef __CUDACC__
+template <typename... KArgs, typename... Args>
+inline void launch_kernel(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                          cudaStream_t st, Args&&... args) {
+  kernel<<<grid, block, smem, st>>>(std::forward<Args>(args)...);
+  GWN_CUDA(cudaGetLastError());
+  count_launch();
+}
+#endif
 
 // Initialise 2*dim ordered-bit slots for atomicMin (first dim) / atomicMax.
 void init_minmax(unsigned long long* mm, int dim, cudaStream_t s);

@@ -367,16 +367,23 @@ __global__ void final_layout_kernel(int64_t ncells, const double* __restrict__ c
   for (int j = 0; j < 8; ++j) ch[id * 8 + j] = internal ? (int32_t)(1 + 8 * (int64_t)rank[x] + j) : -1;
 }
 
-// Gather each cell's point range into the CSR index array (warp per cell).
+// Gather each cell's point range into the CSR index array (warp per cell),
+// with a (cell id, point id) sort key: a cell's range in perm is ordered by
+// octant path, the reference's lists are ascending (octree.cpp:117-122).
 __global__ void csr_gather_kernel(const int64_t* __restrict__ off, const int64_t* __restrict__ start,
                                   const int32_t* __restrict__ count, const int32_t* __restrict__ perm,
-                                  int64_t ncells, int32_t* __restrict__ idx) {
+                                  int64_t ncells, int32_t* __restrict__ idx,
+                                  unsigned long long* __restrict__ key) {
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= ncells) return;
   const int64_t o = off[warp], s = start[warp];
   const int32_t c = count[warp];
-  for (int32_t j = lane; j < c; j += 32) idx[o + j] = perm[s + j];
+  for (int32_t j = lane; j < c; j += 32) {
+    const int32_t p = perm[s + j];
+    idx[o + j] = p;
+    key[o + j] = ((unsigned long long)warp << 30) | (unsigned long long)p;
+  }
 }
 
 // 64-bit exclusive scan of per-cell counts (block-partials, recursive).
@@ -428,12 +435,12 @@ __global__ void scan64_tiles(const int32_t* __restrict__ cnt, int64_t n,
 void exclusive_scan_counts64(const int32_t* cnt, int64_t n, int64_t* off, cudaStream_t st) {
   const int64_t nb = (n + 4095) / 4096;
   if (nb <= 1) {
-    scan64_tiles<<<1, 1024, 0, st>>>(cnt, n, nullptr, off);
+    launch_kernel(scan64_tiles, 1, 1024, 0, st, cnt, n, nullptr, off);
     GWN_CUDA(cudaGetLastError());
     return;
   }
   DevBuf<int64_t> part((size_t)nb, st), part_off((size_t)nb + 1, st);
-  scan64_partials<<<(unsigned)nb, 1024, 0, st>>>(cnt, n, part.get());
+  launch_kernel(scan64_partials, (unsigned)nb, 1024, 0, st, cnt, n, part.get());
   // partials are few (<= 2^20 for 2^32 cells); scan them on the host
   std::vector<int64_t> h((size_t)nb), ho((size_t)nb + 1);
   GWN_CUDA(cudaMemcpyAsync(h.data(), part.get(), (size_t)nb * sizeof(int64_t),
@@ -443,7 +450,7 @@ void exclusive_scan_counts64(const int32_t* cnt, int64_t n, int64_t* off, cudaSt
   for (int64_t i = 0; i < nb; ++i) ho[(size_t)i + 1] = ho[(size_t)i] + h[(size_t)i];
   GWN_CUDA(cudaMemcpyAsync(part_off.get(), ho.data(), ((size_t)nb + 1) * sizeof(int64_t),
                            cudaMemcpyHostToDevice, st));
-  scan64_tiles<<<(unsigned)nb, 1024, 0, st>>>(cnt, n, part_off.get(), off);
+  launch_kernel(scan64_tiles, (unsigned)nb, 1024, 0, st, cnt, n, part_off.get(), off);
   GWN_CUDA(cudaGetLastError());
   GWN_CUDA(cudaStreamSynchronize(st));  // ho must outlive the copy
 }
@@ -471,16 +478,16 @@ void octree_build(gwn_octree_impl& t, const double* P, int64_t n, bool host_mode
   DevBuf<unsigned long long> mm(6, st);
   init_minmax(mm.get(), 3, st);
   if (n > 0) {
-    point_bbox_kernel<<<std::min<unsigned>(blocks(n), 1024u), 256, 0, st>>>(dP, n, mm.get());
+    launch_kernel(point_bbox_kernel, std::min<unsigned>(blocks(n), 1024u), 256, 0, st, dP, n, mm.get());
     GWN_CUDA(cudaGetLastError());
   }
-  root_kernel<<<1, 1, 0, st>>>(mm.get(), n, cells.c.get(), cells.w.get(), cells.start.get(),
+  launch_kernel(root_kernel, 1, 1, 0, st, mm.get(), n, cells.c.get(), cells.w.get(), cells.start.get(),
                                cells.count.get(), cells.depth.get(), cells.parent.get(),
                                cells.oct.get());
   GWN_CUDA(cudaGetLastError());
   cells.size = 1;
   DevBuf<int32_t> perm((size_t)std::max<int64_t>(n, 1), st);
-  iota_kernel<<<blocks(n), 256, 0, st>>>(perm.get(), n);
+  launch_kernel(iota_kernel, blocks(n), 256, 0, st, perm.get(), n);
 
   // level state
   int64_t M = n >= 2 ? n : 0;  // active entries
@@ -489,10 +496,10 @@ void octree_build(gwn_octree_impl& t, const double* P, int64_t n, bool host_mode
   DevBuf<int32_t> seg_cell(1, st), seg_first(1, st);
   DevBuf<int64_t> seg_pstart(1, st);
   if (K) {
-    iota_kernel<<<blocks(M), 256, 0, st>>>(act_pt.get(), M);
-    fill_i32_kernel<<<blocks(M), 256, 0, st>>>(act_seg.get(), M, 0);
-    fill_i32_kernel<<<1, 32, 0, st>>>(seg_cell.get(), 1, 0);
-    fill_i32_kernel<<<1, 32, 0, st>>>(seg_first.get(), 1, 0);
+    launch_kernel(iota_kernel, blocks(M), 256, 0, st, act_pt.get(), M);
+    launch_kernel(fill_i32_kernel, blocks(M), 256, 0, st, act_seg.get(), M, 0);
+    launch_kernel(fill_i32_kernel, 1, 32, 0, st, seg_cell.get(), 1, 0);
+    launch_kernel(fill_i32_kernel, 1, 32, 0, st, seg_first.get(), 1, 0);
     GWN_CUDA(cudaMemsetAsync(seg_pstart.get(), 0, sizeof(int64_t), st));
   }
   bool had_chain = false;
@@ -506,17 +513,17 @@ void octree_build(gwn_octree_impl& t, const double* P, int64_t n, bool host_mode
     seg_mask.zero(st);
     seg_diff.zero(st);
     child_count.zero(st);
-    octant_kernel<<<blocks(M), 256, 0, st>>>(dP, act_pt.get(), act_seg.get(), M, seg_cell.get(),
+    launch_kernel(octant_kernel, blocks(M), 256, 0, st, dP, act_pt.get(), act_seg.get(), M, seg_cell.get(),
                                              seg_first.get(), cells.c.get(), key.get(),
                                              seg_mask.get(), seg_diff.get());
     GWN_CUDA(cudaGetLastError());
     radix_sort_pairs<uint32_t>(key.get(), act_pt.get(), key_tmp.get(), pt_tmp.get(), M, 0,
                                bits_for((uint64_t)K8 - 1), st);
-    child_count_kernel<<<blocks(M), 256, 0, st>>>(key.get(), M, child_count.get());
+    launch_kernel(child_count_kernel, blocks(M), 256, 0, st, key.get(), M, child_count.get());
     cells.reserve(cells.size + K8, st);
     const int64_t base = cells.size;
     DevBuf<unsigned> child_state((size_t)K8, st);
-    emit_children_kernel<<<blocks(K8), 256, 0, st>>>(
+    launch_kernel(emit_children_kernel, blocks(K8), 256, 0, st, 
         K, seg_cell.get(), seg_pstart.get(), seg_mask.get(), seg_diff.get(), child_count.get(), base,
         cells.c.get(), cells.w.get(), cells.start.get(), cells.count.get(), cells.depth.get(),
         cells.parent.get(), cells.oct.get(), child_state.get());
@@ -526,15 +533,15 @@ void octree_build(gwn_octree_impl& t, const double* P, int64_t n, bool host_mode
     // compacted entry positions
     DevBuf<unsigned> child_newseg((size_t)K8, st), child_chainslot((size_t)K8, st),
         child_firstpos((size_t)K8, st), tmp((size_t)K8, st);
-    state_flag_kernel<<<blocks(K8), 256, 0, st>>>(child_state.get(), K8, 1u, tmp.get());
+    launch_kernel(state_flag_kernel, blocks(K8), 256, 0, st, child_state.get(), K8, 1u, tmp.get());
     exclusive_scan_u32(tmp.get(), child_newseg.get(), K8, st);
-    state_flag_kernel<<<blocks(K8), 256, 0, st>>>(child_state.get(), K8, 2u, tmp.get());
+    launch_kernel(state_flag_kernel, blocks(K8), 256, 0, st, child_state.get(), K8, 2u, tmp.get());
     exclusive_scan_u32(tmp.get(), child_chainslot.get(), K8, st);
-    active_count_kernel<<<blocks(K8), 256, 0, st>>>(child_state.get(), child_count.get(), K8,
+    launch_kernel(active_count_kernel, blocks(K8), 256, 0, st, child_state.get(), child_count.get(), K8,
                                                     tmp.get());
     exclusive_scan_u32(tmp.get(), child_firstpos.get(), K8, st);
     DevBuf<unsigned> eflag((size_t)M, st), epos((size_t)M, st);
-    entry_flag_kernel<<<blocks(M), 256, 0, st>>>(key.get(), M, child_state.get(), eflag.get());
+    launch_kernel(entry_flag_kernel, blocks(M), 256, 0, st, key.get(), M, child_state.get(), eflag.get());
     exclusive_scan_u32(eflag.get(), epos.get(), M, st);
     // totals
     unsigned last_state = 0, last_newseg = 0, last_chain = 0, last_eflag = 0, last_epos = 0;
@@ -549,7 +556,7 @@ void octree_build(gwn_octree_impl& t, const double* P, int64_t n, bool host_mode
     const int64_t nM = (int64_t)last_epos + last_eflag;
     DevBuf<int32_t> next_pt((size_t)std::max<int64_t>(nM, 1), st),
         next_seg((size_t)std::max<int64_t>(nM, 1), st);
-    advance_kernel<<<blocks(M), 256, 0, st>>>(act_pt.get(), key.get(), M, seg_first.get(),
+    launch_kernel(advance_kernel, blocks(M), 256, 0, st, act_pt.get(), key.get(), M, seg_first.get(),
                                               seg_pstart.get(), child_state.get(),
                                               child_newseg.get(), epos.get(), perm.get(),
                                               next_pt.get(), next_seg.get());
@@ -557,7 +564,7 @@ void octree_build(gwn_octree_impl& t, const double* P, int64_t n, bool host_mode
     DevBuf<int32_t> nseg_cell((size_t)std::max(nK, 1), st), nseg_first((size_t)std::max(nK, 1), st);
     DevBuf<int64_t> nseg_pstart((size_t)std::max(nK, 1), st);
     DevBuf<int32_t> chain_cell((size_t)std::max(nChains, 1), st);
-    next_segments_kernel<<<blocks(K8), 256, 0, st>>>(
+    launch_kernel(next_segments_kernel, blocks(K8), 256, 0, st, 
         K8, child_state.get(), child_newseg.get(), child_chainslot.get(), child_firstpos.get(), base,
         cells.start.get(), cells.count.get(), nseg_cell.get(), nseg_first.get(), nseg_pstart.get(),
         chain_cell.get());
@@ -577,7 +584,7 @@ void octree_build(gwn_octree_impl& t, const double* P, int64_t n, bool host_mode
       cells.reserve(cells.size + per * nChains, st);
       DevBuf<int64_t> chain_base((size_t)nChains, st);
       chain_base.upload(cb.data(), (size_t)nChains, st);
-      chain_kernel<<<blocks(nChains, 64), 64, 0, st>>>(
+      launch_kernel(chain_kernel, blocks(nChains, 64), 64, 0, st, 
           dP, perm.get(), chain_cell.get(), nChains, chain_base.get(), cells.c.get(), cells.w.get(),
           cells.start.get(), cells.count.get(), cells.depth.get(), cells.parent.get(),
           cells.oct.get());
@@ -599,7 +606,7 @@ void octree_build(gwn_octree_impl& t, const double* P, int64_t n, bool host_mode
   DevBuf<unsigned long long> ikey((size_t)ncells, st), ikey_tmp((size_t)ncells, st);
   DevBuf<int32_t> ival((size_t)ncells, st), ival_tmp((size_t)ncells, st);
   DevBuf<unsigned> is_internal((size_t)ncells, st);
-  internal_keys_kernel<<<blocks(ncells), 256, 0, st>>>(cells.start.get(), cells.count.get(),
+  launch_kernel(internal_keys_kernel, blocks(ncells), 256, 0, st, cells.start.get(), cells.count.get(),
                                                        cells.depth.get(), ncells, ikey.get(),
                                                        ival.get(), is_internal.get());
   GWN_CUDA(cudaGetLastError());
@@ -608,7 +615,7 @@ void octree_build(gwn_octree_impl& t, const double* P, int64_t n, bool host_mode
   const int64_t ninternal = (ncells - 1) / 8;
   DevBuf<int32_t> rank((size_t)ncells, st);
   if (ninternal > 0)
-    rank_kernel<<<blocks(ninternal), 256, 0, st>>>(ival.get(), ninternal, rank.get());
+    launch_kernel(rank_kernel, blocks(ninternal), 256, 0, st, ival.get(), ninternal, rank.get());
   t.ncells = ncells;
   t.cn.alloc((size_t)ncells * 3);
   t.w.alloc((size_t)ncells);
@@ -616,7 +623,7 @@ void octree_build(gwn_octree_impl& t, const double* P, int64_t n, bool host_mode
   t.start.alloc((size_t)ncells);
   t.count.alloc((size_t)ncells);
   t.depth.alloc((size_t)ncells);
-  final_layout_kernel<<<blocks(ncells), 256, 0, st>>>(
+  launch_kernel(final_layout_kernel, blocks(ncells), 256, 0, st, 
       ncells, cells.c.get(), cells.w.get(), cells.start.get(), cells.count.get(), cells.depth.get(),
       cells.parent.get(), cells.oct.get(), rank.get(), t.cn.get(), t.w.get(), t.ch.get(),
       t.start.get(), t.count.get(), t.depth.get());
@@ -637,10 +644,18 @@ void octree_export_csr(const gwn_octree_impl& t, int64_t* pi_offsets, int32_t* p
                        cudaStream_t st) {
   exclusive_scan_counts64(t.count.get(), t.ncells, pi_offsets, st);
   if (pi_indices && t.nindices > 0) {
+    GWN_REQUIRE(t.nindices < (int64_t(1) << 32), "point lists exceed 2^32 entries");
     const int64_t threads = t.ncells * 32;
-    csr_gather_kernel<<<blocks(threads), 256, 0, st>>>(pi_offsets, t.start.get(), t.count.get(),
-                                                       t.perm.get(), t.ncells, pi_indices);
+    DevBuf<unsigned long long> key((size_t)t.nindices, st), key_tmp((size_t)t.nindices, st);
+    DevBuf<int32_t> tmp((size_t)t.nindices, st);
+    launch_kernel(csr_gather_kernel, blocks(threads), 256, 0, st, pi_offsets, t.start.get(), t.count.get(),
+                                                       t.perm.get(), t.ncells, pi_indices,
+                                                       key.get());
     GWN_CUDA(cudaGetLastError());
+    // entries are already grouped by cell; sort by the full key to order
+    // every cell's points ascending
+    radix_sort_pairs<unsigned long long>(key.get(), pi_indices, key_tmp.get(), tmp.get(),
+                                         t.nindices, 0, 30 + bits_for((uint64_t)t.ncells), st);
   }
 }
 

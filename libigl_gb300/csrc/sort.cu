@@ -163,15 +163,15 @@ void exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, cudaStream
   if (n <= 0) return;
   const int64_t nt = (n + kScanTile - 1) / kScanTile;
   if (nt == 1) {
-    scan_tiles_kernel<<<1, kScanThreads, 0, st>>>(in, out, n, nullptr);
+    launch_kernel(scan_tiles_kernel, 1, kScanThreads, 0, st, in, out, n, nullptr);
     GWN_CUDA(cudaGetLastError());
     return;
   }
   DevBuf<uint32_t> partials((size_t)nt, st);
-  scan_partials_kernel<<<(unsigned)nt, kScanThreads, 0, st>>>(in, n, partials.get());
+  launch_kernel(scan_partials_kernel, (unsigned)nt, kScanThreads, 0, st, in, n, partials.get());
   GWN_CUDA(cudaGetLastError());
   exclusive_scan_u32(partials.get(), partials.get(), nt, st);
-  scan_tiles_kernel<<<(unsigned)nt, kScanThreads, 0, st>>>(in, out, n, partials.get());
+  launch_kernel(scan_tiles_kernel, (unsigned)nt, kScanThreads, 0, st, in, out, n, partials.get());
   GWN_CUDA(cudaGetLastError());
 }
 
@@ -187,10 +187,10 @@ void radix_sort_pairs(K* keys, int32_t* vals, K* keys_tmp, int32_t* vals_tmp, in
   K* kb = keys_tmp;
   int32_t* vb = vals_tmp;
   for (int shift = begin_bit; shift < end_bit; shift += 8) {
-    rs_hist_kernel<K><<<ntiles, kRsThreads, 0, st>>>(ka, n, shift, counts.get(), ntiles);
+    launch_kernel(rs_hist_kernel<K>, ntiles, kRsThreads, 0, st, ka, n, shift, counts.get(), ntiles);
     GWN_CUDA(cudaGetLastError());
     exclusive_scan_u32(counts.get(), counts.get(), (int64_t)ntiles * 256, st);
-    rs_scatter_kernel<K><<<ntiles, kRsThreads, 0, st>>>(ka, va, kb, vb, n, shift, counts.get(),
+    launch_kernel(rs_scatter_kernel<K>, ntiles, kRsThreads, 0, st, ka, va, kb, vb, n, shift, counts.get(),
                                                         ntiles);
     GWN_CUDA(cudaGetLastError());
     std::swap(ka, kb);

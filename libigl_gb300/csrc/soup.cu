@@ -718,9 +718,9 @@ void soup_build(gwn_soup_impl& s, const double* V, int64_t nV, const int32_t* F,
   counters.zero(st);
   const unsigned gridF = (unsigned)std::max<int64_t>(1, (nF + 255) / 256);
   if (nF > 0) {
-    tri_keys_kernel<<<gridF, 256, 0, st>>>(V, nV, F, nF, cmm.get(), 0, keys.get(), vals.get(),
+    launch_kernel(tri_keys_kernel, gridF, 256, 0, st, V, nV, F, nF, cmm.get(), 0, keys.get(), vals.get(),
                                            counters.get(), status.ptr());
-    tri_keys_kernel<<<gridF, 256, 0, st>>>(V, nV, F, nF, cmm.get(), 1, keys.get(), vals.get(),
+    launch_kernel(tri_keys_kernel, gridF, 256, 0, st, V, nV, F, nF, cmm.get(), 1, keys.get(), vals.get(),
                                            counters.get(), status.ptr());
     GWN_CUDA(cudaGetLastError());
     radix_sort_pairs<unsigned long long>(keys.get(), vals.get(), keys_tmp.get(), vals_tmp.get(), nF,
@@ -757,15 +757,15 @@ void soup_build(gwn_soup_impl& s, const double* V, int64_t nV, const int32_t* F,
   DevBuf<int32_t> dmax(1, st);
   dmax.zero(st);
   if (n > 1) {
-    radix_tree_kernel<<<(n - 1 + 255) / 256, 256, 0, st>>>(keys.get(), n, left.get(), right.get(),
+    launch_kernel(radix_tree_kernel, (n - 1 + 255) / 256, 256, 0, st, keys.get(), n, left.get(), right.get(),
                                                            parent.get());
     GWN_CUDA(cudaGetLastError());
   }
-  bottom_up_kernel<<<(n + 127) / 128, 128, 0, st>>>(V, F, vals.get(), n, order, left.get(),
+  launch_kernel(bottom_up_kernel, (n + 127) / 128, 128, 0, st, V, F, vals.get(), n, order, left.get(),
                                                     right.get(), parent.get(), M.get(), size.get(),
                                                     flags.get(), dmax.get());
   GWN_CUDA(cudaGetLastError());
-  preorder_kernel<<<(nnodes + 255) / 256, 256, 0, st>>>(left.get(), parent.get(), size.get(),
+  launch_kernel(preorder_kernel, (nnodes + 255) / 256, 256, 0, st, left.get(), parent.get(), size.get(),
                                                         nnodes, 0, pre.get(),
                                                         depth.get());
   GWN_CUDA(cudaGetLastError());
@@ -776,7 +776,7 @@ void soup_build(gwn_soup_impl& s, const double* V, int64_t nV, const int32_t* F,
   s.nd.alloc((size_t)nnodes);
   s.tf.alloc((size_t)n * 3);
   s.td.alloc((size_t)n * 9);
-  emit_kernel<<<(nnodes + 255) / 256, 256, 0, st>>>(M.get(), pre.get(), size.get(), n, V, F,
+  launch_kernel(emit_kernel, (nnodes + 255) / 256, 256, 0, st, M.get(), pre.get(), size.get(), n, V, F,
                                                     vals.get(), s.nf.get(), s.nd.get(), s.tf.get(),
                                                     s.td.get());
   GWN_CUDA(cudaGetLastError());
@@ -807,7 +807,7 @@ static void soup_eval_t(const gwn_soup_impl& s, float beta, const void* Qv, int6
   WT* W = static_cast<WT*>(Wv);
   if (nQ == 0) return;
   if (s.nnodes == 0) {
-    fill_zero_kernel<WT><<<(unsigned)((nQ + 255) / 256), 256, 0, st>>>(W, nQ);
+    launch_kernel(fill_zero_kernel<WT>, (unsigned)((nQ + 255) / 256), 256, 0, st, W, nQ);
     GWN_CUDA(cudaGetLastError());
     return;
   }
@@ -824,21 +824,31 @@ static void soup_eval_t(const gwn_soup_impl& s, float beta, const void* Qv, int6
   prm.cmax = (float)s.cmax;
   prm.status = nullptr;
   QueryOrder qo;
-  order_queries(Qv, sizeof(QT) == 8 ? GWN_F64 : GWN_F32, nQ, s.lo, s.hi, qo, st);
+  {
+    PhaseTimer ph("order_queries", st);
+    order_queries(Qv, sizeof(QT) == 8 ? GWN_F64 : GWN_F32, nQ, s.lo, s.hi, qo, st);
+  }
   const int32_t* perm = qo.active ? qo.perm.get() : nullptr;
   const unsigned grid = (unsigned)((nQ + 127) / 128);
   if (precision == GWN_MIXED) {
     DevBuf<int32_t> list((size_t)nQ, st);
     DevBuf<unsigned> count(1, st);
     count.zero(st);
-    soup_eval_mixed_kernel<QT, WT><<<grid, 128, 0, st>>>(prm, Q, perm, nQ, W, list.get(),
-                                                         count.get());
+    {
+      PhaseTimer ph("walk", st);
+      launch_kernel(soup_eval_mixed_kernel<QT, WT>, grid, 128, 0, st, prm, Q, perm, nQ, W, list.get(),
+                                                           count.get());
+    }
     GWN_CUDA(cudaGetLastError());
-    soup_eval_fp64_kernel<QT, WT><<<grid, 128, 0, st>>>(prm, Q, nullptr, list.get(), count.get(),
-                                                        nQ, W);
+    {
+      PhaseTimer ph("refine", st);
+      launch_kernel(soup_eval_fp64_kernel<QT, WT>, grid, 128, 0, st, prm, Q, nullptr, list.get(),
+                                                          count.get(), nQ, W);
+    }
     GWN_CUDA(cudaGetLastError());
   } else {
-    soup_eval_fp64_kernel<QT, WT><<<grid, 128, 0, st>>>(prm, Q, perm, nullptr, nullptr, nQ, W);
+    PhaseTimer ph("walk", st);
+    launch_kernel(soup_eval_fp64_kernel<QT, WT>, grid, 128, 0, st, prm, Q, perm, nullptr, nullptr, nQ, W);
     GWN_CUDA(cudaGetLastError());
   }
 }

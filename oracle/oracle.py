@@ -20,7 +20,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "liboracle.so")
 REF_SOUP_PATH = os.path.join(HERE, "_ref", "libref_soup.so")
 
-_SOURCES = ["gwn_oracle.cpp", "soup_port.cpp", "wn_hier.cpp"]
+_SOURCES = ["gwn_oracle.cpp", "soup_port.cpp", "soup_hdk.cpp", "wn_hier.cpp"]
 
 
 def build(force: bool = False) -> str:

@@ -147,8 +147,12 @@ def test_direct_sum_beta_nonpositive(cuda):
     CM, R, EC = O.cloud_precompute(P, Nn, A, t, 2)
     Wref = O.cloud_eval(P, Nn, A, t, CM, R, EC, Q, 0.0)
     ce = G.CloudExpansion(P, Nn, A, order=2)
-    assert np.abs(ce.eval(Q, 0.0, precision="fp64") - Wref).max() <= 1e-11
-    assert np.abs(ce.eval(Q, -1.0, precision="mixed") - Wref).max() <= TOL_MIXED
+    # the direct sum adds thousands of dipoles of magnitude up to ~10: rounding
+    # of the summation order is ~1e-16 * sum |term|
+    W64 = ce.eval(Q, 0.0, precision="fp64")
+    assert np.abs(W64 - Wref).max() <= 1e-10, np.abs(W64 - Wref).max()
+    Wm = ce.eval(Q, -1.0, precision="mixed")
+    assert np.abs(Wm - Wref).max() <= TOL_MIXED, np.abs(Wm - Wref).max()
 
 
 def test_query_on_a_point_gives_half_dipole(cuda):

@@ -117,3 +117,16 @@ def test_cloud_direct_matches_bh_far():
     Wbh = O.cloud_eval(P, Nn, A, t, CM, R, EC, Q, 2.0)
     Wd = O.cloud_eval(P, Nn, A, t, CM, R, EC, Q, 0.0)
     assert np.abs(Wbh - Wd).max() < 1e-3 * np.abs(Wd).max()  # order-3 truncation
+
+
+def test_soup_port_reproduces_reference_fixtures_bit_for_bit():
+    # The CPU restatement of the HDK soup algorithm (oracle/soup_hdk.cpp) is
+    # pinned against the reference's own UT_SolidAngle outputs committed by
+    # tests/golden/make_golden.py.
+    import os
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "soup_reference.npz"))
+    names = sorted({k.split("/")[0] for k in z.files})
+    for name in names:
+        V, F, Q, Wref = z[name + "/V"], z[name + "/F"], z[name + "/Q"], z[name + "/W_ref"]
+        W = O.SoupPort(V, F, order=2).eval(Q, 2.0)
+        assert np.array_equal(W, Wref), name
