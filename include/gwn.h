@@ -108,6 +108,13 @@ int gwn_soup_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, in
 int gwn_soup_eval(const gwn_soup* soup, float accuracy_scale, const void* Q, int q_dtype,
                   int64_t nQ, void* W, int w_dtype, int precision, int mem, void* stream);
 int gwn_soup_stats_get(const gwn_soup* soup, gwn_soup_stats* out);
+/* Work counters of one instrumented mixed-precision evaluation of nQ float64
+ * queries (a separate kernel instance; for profiling, no counterpart in the
+ * reference): counters[0..6] = warp steps, per-query node visits, far-field
+ * evaluations, FP32 exact triangles, FP64 near-field triangles, FP64 decision
+ * re-checks, threshold re-evaluations. */
+int gwn_soup_walk_stats(const gwn_soup* soup, float accuracy_scale, const double* Q, int64_t nQ,
+                        int mem, unsigned long long* counters);
 void gwn_soup_free(gwn_soup* soup);
 
 /* Copies the built tree to host memory (for inspection and testing):

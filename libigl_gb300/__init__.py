@@ -201,6 +201,16 @@ class FastWindingNumberBVH:
         links = nodes[:, 23].copy().view(np.int64)
         return nodes, links, tri
 
+    def walk_stats(self, Q, accuracy_scale: float = 2.0) -> dict:
+        """Work counters of one instrumented mixed evaluation of Q (float64)."""
+        Qa = _Arg(Q, np.float64)
+        out = (C.c_ulonglong * 7)()
+        N.check(N.load().gwn_soup_walk_stats(self._h, C.c_float(accuracy_scale), Qa.ptr,
+                                             Qa.shape[0], Qa.mem, out))
+        keys = ["warp_steps", "node_visits", "far_field", "exact_fp32", "exact_fp64_near",
+                "fp64_rechecks", "threshold_refines"]
+        return dict(zip(keys, [int(x) for x in out]))
+
     @property
     def stats(self) -> dict:
         st = _SoupStats()

@@ -40,6 +40,7 @@ SIGNATURES = {
     "gwn_soup_stats_get": ([_p, _p], _i),
     "gwn_soup_free": ([_p], None),
     "gwn_soup_export": ([_p, _p, _p], _i),
+    "gwn_soup_walk_stats": ([_p, _f, _p, _i64, _i, _p], _i),
     "gwn_octree_build": ([_p, _i64, _i, _p, _p], _i),
     "gwn_octree_sizes": ([_p, _p, _p, _p], _i),
     "gwn_octree_export": ([_p, _p, _p, _p, _p, _p, _i, _p], _i),

@@ -45,6 +45,17 @@ void order_queries(const void* Q, int q_dtype, int64_t nQ, const double lo[3],
                    const double hi[3], QueryOrder& out, cudaStream_t st);
 
 #ifdef __CUDACC__
+// Precision-exact math for the templated walks: the float versions must not
+// promote to double (FP64 is a slow pipe on this GPU).
+__device__ __forceinline__ float g_sqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double g_sqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float g_rsqrt(float x) { return rsqrtf(x); }
+__device__ __forceinline__ double g_rsqrt(double x) { return 1.0 / sqrt(x); }
+__device__ __forceinline__ float g_atan2(float y, float x) { return atan2f(y, x); }
+__device__ __forceinline__ double g_atan2(double y, double x) { return atan2(y, x); }
+__device__ __forceinline__ float g_rcp(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double g_rcp(double x) { return 1.0 / x; }
+
 // The FP64 open test shared by both precisions: open (do not approximate)
 // iff |q - c|^2 <= r2max * beta2.  Operations are pinned (no contraction) so
 // that every kernel evaluates the identical expression.

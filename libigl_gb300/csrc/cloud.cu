@@ -126,12 +126,14 @@ __global__ void combine1_kernel(const int32_t* __restrict__ count, int64_t ncell
                                 const unsigned* __restrict__ nch,
                                 const unsigned* __restrict__ chunk_base,
                                 const double* __restrict__ part, int num_terms,
-                                double* __restrict__ CM, double* __restrict__ EC) {
+                                double* __restrict__ CM, double* __restrict__ EC,
+                                double* __restrict__ area) {
   const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (c >= ncells) return;
   double s[7] = {0, 0, 0, 0, 0, 0, 0};
   for (unsigned j = 0; j < nch[c]; ++j)
     for (int k = 0; k < 7; ++k) s[k] += part[(chunk_base[c] + j) * 8 + k];
+  area[c] = s[0];
   for (int d = 0; d < 3; ++d) {
     CM[c * 3 + d] = count[c] > 0 ? s[1 + d] / s[0] : __longlong_as_double(0x7ff8000000000000LL);
     EC[c * num_terms + d] = s[4 + d];
@@ -252,7 +254,20 @@ struct LayoutIn {
   const double* R;
   const double* EC;
   int num_terms;
+  const double* area;  // per cell, for the FP64 near-field radius
+  double eps, cmax;
 };
+
+// FP64 near-field radius of a dipole (or expansion) of strength `area`: a
+// point dipole's field grows as area / r^2, so the FP32 rounding of q - p
+// (delta = 4 u cmax) costs area * delta / (4 pi r^3); below
+// r = (area * delta / (4 pi tau))^(1/3), tau = 2e-7 per term, or below the
+// 1e-3 * bbox-diagonal rule, the term is evaluated in FP64.
+__device__ __forceinline__ float near_radius2(double area, double eps, double cmax) {
+  const double delta = 4.0 * 5.9604644775390625e-08 * cmax;
+  const double r = fmax(eps, cbrt(fabs(area) * delta / (4.0 * kPi * 2e-7)));
+  return (float)(r * r * 1.0001);
+}
 
 __global__ void emit_nodes_kernel(LayoutIn in, CloudNodeF* __restrict__ nf,
                                   CloudNodeD* __restrict__ nd) {
@@ -279,7 +294,7 @@ __global__ void emit_nodes_kernel(LayoutIn in, CloudNodeF* __restrict__ nf,
   Fr.a = make_float4((float)D.cm[0], (float)D.cm[1], (float)D.cm[2], (float)D.r);
   float e[40];
   for (int k = 0; k < 39; ++k) e[k] = (float)D.ec[k];
-  e[39] = 0.f;
+  e[39] = near_radius2(in.area[c], in.eps, in.cmax);
   for (int k = 0; k < 10; ++k) Fr.e[k] = make_float4(e[4 * k], e[4 * k + 1], e[4 * k + 2], e[4 * k + 3]);
   Fr.l = D.l;
   nf[p] = Fr;
@@ -287,7 +302,8 @@ __global__ void emit_nodes_kernel(LayoutIn in, CloudNodeF* __restrict__ nf,
 
 __global__ void emit_points_kernel(const int32_t* __restrict__ slot_point, int64_t nslots,
                                    const double* __restrict__ P, const double* __restrict__ AN,
-                                   float4* __restrict__ pf, double* __restrict__ pd) {
+                                   double eps, double cmax, float4* __restrict__ pf,
+                                   double* __restrict__ pd) {
   const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (j >= nslots) return;
   const int64_t p = slot_point[j];
@@ -297,7 +313,8 @@ __global__ void emit_points_kernel(const int32_t* __restrict__ slot_point, int64
     v[3 + d] = AN[p * 3 + d];
   }
   for (int k = 0; k < 6; ++k) pd[j * 6 + k] = v[k];
-  pf[j * 2] = make_float4((float)v[0], (float)v[1], (float)v[2], 0.f);
+  const double strength = sqrt(v[3] * v[3] + v[4] * v[4] + v[5] * v[5]);
+  pf[j * 2] = make_float4((float)v[0], (float)v[1], (float)v[2], near_radius2(strength, eps, cmax));
   pf[j * 2 + 1] = make_float4((float)v[3], (float)v[4], (float)v[5], 0.f);
 }
 
@@ -398,7 +415,6 @@ __global__ void __launch_bounds__(128) cloud_eval_mixed_kernel(CloudEvalParams p
   const float fx = (float)qx, fy = (float)qy, fz = (float)qz;
   const float S = fmaxf(fabsf(fx), fmaxf(fabsf(fy), fabsf(fz))) + prm.cmax;
   const float sigma = guard_sigma(S);
-  const float eps2 = prm.eps * prm.eps;
   float acc = 0.f;
   double acc64 = 0.0;
   int resume = valid ? 0 : 0x7fffffff;
@@ -416,7 +432,7 @@ __global__ void __launch_bounds__(128) cloud_eval_mixed_kernel(CloudEvalParams p
           const float4 p = __ldg(&prm.pf[slot * 2]);
           const float lx = p.x - fx, ly = p.y - fy, lz = p.z - fz;
           const float r2 = fmaf(lz, lz, fmaf(ly, ly, lx * lx));
-          if (r2 <= eps2 * 1.0001f) {
+          if (r2 <= p.w) {
             const double* pd = prm.pd + slot * 6;
             acc64 += dipole64(pd[0] - qx, pd[1] - qy, pd[2] - qz, pd[3], pd[4], pd[5]);
           } else {
@@ -440,16 +456,25 @@ __global__ void __launch_bounds__(128) cloud_eval_mixed_kernel(CloudEvalParams p
           far = far64(qx, qy, qz, rd->cm, rd->r, prm.beta);
         }
         if (far) {
-          float ec[40];
+          const float rn2 = __ldg(&r->e[9]).w;
+          if (r2 <= rn2) {  // strong expansion close to the query: FP64
+            const CloudNodeD* rd = prm.nd + node;
+            const double lx = __dsub_rn(rd->cm[0], qx), ly = __dsub_rn(rd->cm[1], qy),
+                         lz = __dsub_rn(rd->cm[2], qz);
+            acc64 += expansion<double>(rd->ec, lx, ly, lz, sqrt(lx * lx + ly * ly + lz * lz),
+                                       prm.num_terms);
+          } else {
+            float ec[40];
 #pragma unroll
-          for (int k = 0; k < 10; ++k) {
-            const float4 e = __ldg(&r->e[k]);
-            ec[4 * k] = e.x;
-            ec[4 * k + 1] = e.y;
-            ec[4 * k + 2] = e.z;
-            ec[4 * k + 3] = e.w;
+            for (int k = 0; k < 10; ++k) {
+              const float4 e = __ldg(&r->e[k]);
+              ec[4 * k] = e.x;
+              ec[4 * k + 1] = e.y;
+              ec[4 * k + 2] = e.z;
+              ec[4 * k + 3] = e.w;
+            }
+            acc += expansion<float>(ec, dx, dy, dz, sqrtf(r2), prm.num_terms);
           }
-          acc += expansion<float>(ec, dx, dy, dz, sqrtf(r2), prm.num_terms);
           resume = l.x;
         } else {
           open = true;
@@ -536,7 +561,7 @@ __global__ void __launch_bounds__(256) cloud_direct_kernel(const float4* __restr
       const float4 p = __ldg(&pf[j * 2]);
       const float lx = p.x - fx, ly = p.y - fy, lz = p.z - fz;
       const float r2 = fmaf(lz, lz, fmaf(ly, ly, lx * lx));
-      if (r2 <= eps * eps * 1.0001f) {
+      if (r2 <= p.w) {
         const double* d = pd + j * 6;
         acc64 += dipole64(d[0] - qx, d[1] - qy, d[2] - qz, d[3], d[4], d[5]);
       } else {
@@ -563,6 +588,7 @@ void precompute(gwn_cloud_impl& c, const CsrView& v, int64_t ncells, const doubl
   c.CM.alloc((size_t)std::max<int64_t>(ncells, 1) * 3);
   c.R.alloc((size_t)std::max<int64_t>(ncells, 1));
   c.EC.alloc((size_t)std::max<int64_t>(ncells, 1) * c.num_terms);
+  c.area.alloc((size_t)std::max<int64_t>(ncells, 1));
   if (ncells == 0) return;
   DevBuf<unsigned> nch((size_t)ncells, st), cbase((size_t)ncells, st);
   launch_kernel(chunk_count_kernel, blocks(ncells), 256, 0, st, v.count, ncells, nch.get());
@@ -579,7 +605,8 @@ void precompute(gwn_cloud_impl& c, const CsrView& v, int64_t ncells, const doubl
     launch_kernel(pass1_kernel, blocks(nchunks * 32), 256, 0, st, v, chunk_cell.get(), cbase.get(), nchunks, P,
                                                       N, A, part.get());
   launch_kernel(combine1_kernel, blocks(ncells), 256, 0, st, v.count, ncells, nch.get(), cbase.get(),
-                                                  part.get(), c.num_terms, c.CM.get(), c.EC.get());
+                                                  part.get(), c.num_terms, c.CM.get(), c.EC.get(),
+                                                  c.area.get());
   GWN_CUDA(cudaGetLastError());
   if (nchunks) {
     if (c.num_terms == 39)
@@ -652,8 +679,7 @@ void finish_extent(gwn_cloud_impl& c, cudaStream_t st) {
   }
   c.eps = kNearFrac * std::sqrt(diag2);
   c.cmax = cmax;
-  c.bytes = c.CM.bytes() + c.R.bytes() + c.EC.bytes() + c.nf.bytes() + c.nd.bytes() + c.pf.bytes() +
-            c.pd.bytes() + c.P.bytes() + c.AN.bytes();
+  c.bytes = c.CM.bytes() + c.R.bytes() + c.EC.bytes() + c.area.bytes() + c.P.bytes() + c.AN.bytes();
 }
 
 }  // namespace
@@ -694,15 +720,17 @@ void cloud_build(gwn_cloud_impl& c, const gwn_octree_impl& t, const double* N, c
   c.nnodes = nnodes;
   c.nf.alloc((size_t)std::max<int64_t>(nnodes, 1));
   c.nd.alloc((size_t)std::max<int64_t>(nnodes, 1));
+  finish_extent(c, st);
   LayoutIn in{val.get(), nullptr, nullptr, key.get(), nnodes, t.start.get(), t.count.get(), t.ch.get(),
-              t.depth.get(), c.CM.get(), c.R.get(), c.EC.get(), c.num_terms};
+              t.depth.get(), c.CM.get(), c.R.get(), c.EC.get(), c.num_terms, c.area.get(), c.eps,
+              c.cmax};
   if (nnodes) launch_kernel(emit_nodes_kernel, blocks(nnodes), 256, 0, st, in, c.nf.get(), c.nd.get());
   c.pf.alloc((size_t)std::max<int64_t>(n, 1) * 2);
   c.pd.alloc((size_t)std::max<int64_t>(n, 1) * 6);
-  if (n) launch_kernel(emit_points_kernel, blocks(n), 256, 0, st, t.perm.get(), n, c.P.get(), c.AN.get(),
-                                                      c.pf.get(), c.pd.get());
-  GWN_CUDA(cudaGetLastError());
-  finish_extent(c, st);
+  if (n)
+    launch_kernel(emit_points_kernel, blocks(n), 256, 0, st, t.perm.get(), n, c.P.get(), c.AN.get(),
+                  c.eps, c.cmax, c.pf.get(), c.pd.get());
+  c.bytes += c.nf.bytes() + c.nd.bytes() + c.pf.bytes() + c.pd.bytes();
 }
 
 
@@ -733,11 +761,15 @@ void cloud_build_arrays(gwn_cloud_impl& c, const double* P, const double* N, con
   }
   DevBuf<int32_t> cnt((size_t)ncells, st);
   launch_kernel(csr_count_kernel, blocks(ncells), 256, 0, st, pi_off_d, ncells, cnt.get());
-  if (compute_moments) {
+  // the moments are computed even when the caller supplies CM/R/EC: the
+  // per-cell areas set the FP64 near-field radii of the walk
+  (void)compute_moments;
+  {
     CsrView v{pi_off_d, cnt.get(), pi_idx_d};
     precompute(c, v, ncells, c.P.get(), N, A, st);
   }
   if (!pi_off_h) return;
+  finish_extent(c, st);
   // depth-first pre-order of the non-empty cells (children in octant order,
   // as the reference's recursion visits them) with subtree ends and leaf slots
   std::vector<int32_t> order_h, first_h;
@@ -791,8 +823,8 @@ void cloud_build_arrays(gwn_cloud_impl& c, const double* P, const double* N, con
   c.pf.alloc((size_t)std::max<int64_t>(nslots, 1) * 2);
   c.pd.alloc((size_t)std::max<int64_t>(nslots, 1) * 6);
   if (nslots)
-    launch_kernel(emit_points_kernel, blocks(nslots), 256, 0, st, slot_d.get(), nslots, c.P.get(), c.AN.get(),
-                                                        c.pf.get(), c.pd.get());
+    launch_kernel(emit_points_kernel, blocks(nslots), 256, 0, st, slot_d.get(), nslots, c.P.get(),
+                  c.AN.get(), c.eps, c.cmax, c.pf.get(), c.pd.get());
   // node records need CM/R/EC: emitted by cloud_emit_arrays once moments exist
   c.layout_order = std::move(order_d);
   c.layout_first = std::move(first_d);
@@ -801,13 +833,12 @@ void cloud_build_arrays(gwn_cloud_impl& c, const double* P, const double* N, con
   c.layout_count = std::move(cnt);
   c.layout_ch = CH_d;
   GWN_CUDA(cudaStreamSynchronize(st));  // host vectors outlive their uploads
-  finish_extent(c, st);
 }
 
 void cloud_emit_arrays(gwn_cloud_impl& c, cudaStream_t st) {
   LayoutIn in{c.layout_order.get(), c.layout_first.get(), c.layout_skip.get(), nullptr, c.nnodes,
               c.layout_start.get(), c.layout_count.get(), c.layout_ch, nullptr, c.CM.get(),
-              c.R.get(), c.EC.get(), c.num_terms};
+              c.R.get(), c.EC.get(), c.num_terms, c.area.get(), c.eps, c.cmax};
   if (c.nnodes) launch_kernel(emit_nodes_kernel, blocks(c.nnodes), 256, 0, st, in, c.nf.get(), c.nd.get());
   GWN_CUDA(cudaGetLastError());
 }

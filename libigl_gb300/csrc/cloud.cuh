@@ -10,7 +10,7 @@
 namespace gwn {
 
 // 192-byte FP32 traversal record.
-//   a: CM xyz, R        e[0..9]: EC[0..38] (39 floats + pad)
+//   a: CM xyz, R        e[0..9]: EC[0..38], then the squared FP64 near-field radius
 //   l: skip (one past subtree), first point slot, point count, leaf flag
 struct __align__(16) CloudNodeF {
   float4 a;
@@ -37,6 +37,7 @@ struct gwn_cloud_impl {
   double eps = 0, cmax = 0;
   // per igl cell id (export)
   DevMem<double> CM, R, EC;
+  DevMem<double> area;  // sum of A per cell (FP64 near-field radii)
   // traversal (pre-order of non-empty cells)
   DevMem<CloudNodeF> nf;
   DevMem<CloudNodeD> nd;

@@ -286,6 +286,19 @@ int gwn_soup_eval(const gwn_soup* soup, float accuracy_scale, const void* Q, int
   });
 }
 
+int gwn_soup_walk_stats(const gwn_soup* soup, float accuracy_scale, const double* Q, int64_t nQ,
+                        int mem, unsigned long long* counters) {
+  return guarded("gwn_soup_walk_stats", [&] {
+    GWN_REQUIRE(soup && counters, "null argument");
+    GWN_REQUIRE(nQ >= 0 && nQ < (int64_t(1) << 31), "0 <= nQ < 2^31");
+    check_mem(mem);
+    check_device_of(soup->impl.device);
+    cudaStream_t st = nullptr;
+    Staged<double> dQ(Q, (size_t)nQ * 3, mem, st);
+    soup_walk_stats(soup->impl, accuracy_scale, dQ.dev, nQ, counters, st);
+  });
+}
+
 int gwn_soup_stats_get(const gwn_soup* soup, gwn_soup_stats* out) {
   return guarded("gwn_soup_stats_get", [&] {
     GWN_REQUIRE(soup && out, "null argument");

@@ -451,8 +451,16 @@ struct Far {
 
 template <typename T>
 __device__ __forceinline__ T far_field(const Far<T>& m, T dx, T dy, T dz, T r2, int order) {
-  const T m2 = T(1) / r2;
-  const T m1 = sqrt(m2);
+  // m1 = 1/|q-P|, m2 = m1^2 (FP64: 1/r2 then sqrt, as the reference;
+  // FP32: one reciprocal square root)
+  T m1, m2;
+  if (sizeof(T) == 4) {
+    m1 = g_rsqrt(r2);
+    m2 = m1 * m1;
+  } else {
+    m2 = T(1) / r2;
+    m1 = g_sqrt(m2);
+  }
   const T qx = dx * m1, qy = dy * m1, qz = dz * m1;
   T omega = -m2 * (qx * m.N[0] + qy * m.N[1] + qz * m.N[2]);
   if (order >= 1) {
@@ -481,20 +489,28 @@ __device__ __forceinline__ T far_field(const Far<T>& m, T dx, T dy, T dz, T r2, 
 template <typename T>
 __device__ __forceinline__ T tri_solid_angle(T ax, T ay, T az, T bx, T by, T bz, T cx, T cy,
                                              T cz) {
-  const T la = sqrt(ax * ax + ay * ay + az * az);
-  const T lb = sqrt(bx * bx + by * by + bz * bz);
-  const T lc = sqrt(cx * cx + cy * cy + cz * cz);
-  if (la == T(0) || lb == T(0) || lc == T(0)) return T(0);
-  ax /= la; ay /= la; az /= la;
-  bx /= lb; by /= lb; bz /= lb;
-  cx /= lc; cy /= lc; cz /= lc;
+  const T la2 = ax * ax + ay * ay + az * az;
+  const T lb2 = bx * bx + by * by + bz * bz;
+  const T lc2 = cx * cx + cy * cy + cz * cz;
+  if (la2 == T(0) || lb2 == T(0) || lc2 == T(0)) return T(0);
+  if (sizeof(T) == 4) {  // normalise with reciprocal square roots
+    const T ia = g_rsqrt(la2), ib = g_rsqrt(lb2), ic = g_rsqrt(lc2);
+    ax *= ia; ay *= ia; az *= ia;
+    bx *= ib; by *= ib; bz *= ib;
+    cx *= ic; cy *= ic; cz *= ic;
+  } else {  // FP64: length then divide, as FWNFS.h:6085-6095
+    const T la = g_sqrt(la2), lb = g_sqrt(lb2), lc = g_sqrt(lc2);
+    ax /= la; ay /= la; az /= la;
+    bx /= lb; by /= lb; bz /= lb;
+    cx /= lc; cy /= lc; cz /= lc;
+  }
   const T ux = bx - ax, uy = by - ay, uz = bz - az;
   const T vx = cx - ax, vy = cy - ay, vz = cz - az;
   const T num = ax * (uy * vz - uz * vy) + ay * (uz * vx - ux * vz) + az * (ux * vy - uy * vx);
   if (num == T(0)) return T(0);
   const T den = T(1) + (ax * bx + ay * by + az * bz) + (ax * cx + ay * cy + az * cz) +
                 (bx * cx + by * cy + bz * cz);
-  return T(2) * atan2(num, den);
+  return T(2) * g_atan2(num, den);
 }
 
 __device__ __forceinline__ Far<float> load_far(const SoupNodeF* r) {
@@ -549,13 +565,18 @@ struct EvalParams {
   unsigned* status;
 };
 
-// Mixed-precision warp-coherent walk.  One query per lane.
-template <typename QT, typename WT>
+// Mixed-precision warp-coherent walk.  One query per lane.  kStats builds
+// an instrumented copy that counts its work into `stats` (see
+// gwn_soup_walk_stats); the timed kernel is the kStats = false instance.
+template <typename QT, typename WT, bool kStats = false>
 __global__ void __launch_bounds__(128) soup_eval_mixed_kernel(EvalParams prm, const QT* __restrict__ Q,
                                                               const int32_t* __restrict__ perm,
                                                               int64_t nQ, WT* __restrict__ W,
                                                               int32_t* __restrict__ refine_list,
-                                                              unsigned* __restrict__ refine_count) {
+                                                              unsigned* __restrict__ refine_count,
+                                                              unsigned long long* __restrict__ stats = nullptr) {
+  unsigned long long st_steps = 0, st_visits = 0, st_far = 0, st_exact32 = 0, st_exact64 = 0,
+                     st_recheck = 0;
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const bool valid = i < nQ;
   int64_t qi = 0;
@@ -574,7 +595,9 @@ __global__ void __launch_bounds__(128) soup_eval_mixed_kernel(EvalParams prm, co
     const float4 a = __ldg(&r->a);
     const int link = __float_as_int(__ldg(&r->f).w);
     bool open = false;
+    if (kStats) ++st_steps;
     if (node >= resume) {
+      if (kStats) ++st_visits;
       const bool leaf = link < 0;
       if (node == 0 && !leaf) {
         open = true;
@@ -586,8 +609,10 @@ __global__ void __launch_bounds__(128) soup_eval_mixed_kernel(EvalParams prm, co
         if (in_guard_band(r2, thr, sigma)) {
           const SoupNodeD* rd = prm.nd + node;
           near = open_test64(qx, qy, qz, rd->P[0], rd->P[1], rd->P[2], rd->maxP2, prm.beta2d);
+          if (kStats) ++st_recheck;
         }
         if (!near) {
+          if (kStats) ++st_far;
           const float om = far_field<float>(load_far(r), dx, dy, dz, r2, prm.order);
           if (isfinite(om)) {
             acc += om;
@@ -601,11 +626,13 @@ __global__ void __launch_bounds__(128) soup_eval_mixed_kernel(EvalParams prm, co
             const int slot = ~link;
             const float rad = sqrtf(a.w) + prm.eps;
             if (r2 <= rad * rad * 1.0001f) {
+              if (kStats) ++st_exact64;
               const double* t = prm.td + (int64_t)slot * 9;
               acc64 += tri_solid_angle<double>(t[0] - qx, t[1] - qy, t[2] - qz, t[3] - qx,
                                                t[4] - qy, t[5] - qz, t[6] - qx, t[7] - qy,
                                                t[8] - qz);
             } else {
+              if (kStats) ++st_exact32;
               const float4 t0 = __ldg(&prm.tf[(int64_t)slot * 3]);
               const float4 t1 = __ldg(&prm.tf[(int64_t)slot * 3 + 1]);
               const float4 t2 = __ldg(&prm.tf[(int64_t)slot * 3 + 2]);
@@ -623,6 +650,14 @@ __global__ void __launch_bounds__(128) soup_eval_mixed_kernel(EvalParams prm, co
       node = node + 1;
     else
       node = __reduce_min_sync(full, resume);
+  }
+  if (kStats) {
+    if ((threadIdx.x & 31) == 0) atomicAdd(&stats[0], st_steps);
+    atomicAdd(&stats[1], st_visits);
+    atomicAdd(&stats[2], st_far);
+    atomicAdd(&stats[3], st_exact32);
+    atomicAdd(&stats[4], st_exact64);
+    atomicAdd(&stats[5], st_recheck);
   }
   if (!valid) return;
   const double w = acc64 != 0.0 ? ((double)acc + acc64) * kInv4Pi : (double)(acc * kInv4PiF);
@@ -837,7 +872,7 @@ static void soup_eval_t(const gwn_soup_impl& s, float beta, const void* Qv, int6
     {
       PhaseTimer ph("walk", st);
       launch_kernel(soup_eval_mixed_kernel<QT, WT>, grid, 128, 0, st, prm, Q, perm, nQ, W, list.get(),
-                                                           count.get());
+                                                           count.get(), (unsigned long long*)nullptr);
     }
     GWN_CUDA(cudaGetLastError());
     {
@@ -851,6 +886,40 @@ static void soup_eval_t(const gwn_soup_impl& s, float beta, const void* Qv, int6
     launch_kernel(soup_eval_fp64_kernel<QT, WT>, grid, 128, 0, st, prm, Q, perm, nullptr, nullptr, nQ, W);
     GWN_CUDA(cudaGetLastError());
   }
+}
+
+void soup_walk_stats(const gwn_soup_impl& s, float beta, const double* Q, int64_t nQ,
+                     unsigned long long* out7, cudaStream_t st) {
+  for (int k = 0; k < 7; ++k) out7[k] = 0;
+  if (nQ == 0 || s.nnodes == 0) return;
+  EvalParams prm;
+  prm.nf = s.nf.get();
+  prm.nd = s.nd.get();
+  prm.tf = s.tf.get();
+  prm.td = s.td.get();
+  prm.nnodes = (int)s.nnodes;
+  prm.order = s.order;
+  prm.beta2f = beta * beta;
+  prm.beta2d = (double)beta * (double)beta;
+  prm.eps = (float)s.eps;
+  prm.cmax = (float)s.cmax;
+  prm.status = nullptr;
+  QueryOrder qo;
+  order_queries(Q, GWN_F64, nQ, s.lo, s.hi, qo, st);
+  DevBuf<double> W((size_t)nQ, st);
+  DevBuf<int32_t> list((size_t)nQ, st);
+  DevBuf<unsigned> count(1, st);
+  DevBuf<unsigned long long> stats(7, st);
+  count.zero(st);
+  stats.zero(st);
+  launch_kernel(soup_eval_mixed_kernel<double, double, true>, (unsigned)((nQ + 127) / 128), 128, 0,
+                st, prm, Q, qo.active ? qo.perm.get() : nullptr, nQ, W.get(), list.get(),
+                count.get(), stats.get());
+  unsigned c = 0;
+  GWN_CUDA(cudaMemcpyAsync(out7, stats.get(), 6 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+  GWN_CUDA(cudaMemcpyAsync(&c, count.get(), sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+  GWN_CUDA(cudaStreamSynchronize(st));
+  out7[6] = c;
 }
 
 void soup_eval(const gwn_soup_impl& s, float beta, const void* Q, int q_dtype, int64_t nQ, void* W,

@@ -50,6 +50,11 @@ struct gwn_soup_impl {
 
 void soup_build(gwn_soup_impl& s, const double* V, int64_t nV, const int32_t* F, int64_t nF,
                 int order, bool host_mode, cudaStream_t st);
+// Instrumented mixed walk over FP64 device queries: out7 = {warp steps,
+// lane visits, far-field evaluations, FP32 exact triangles, FP64 near-field
+// triangles, FP64 decision re-checks, threshold re-evaluations}.
+void soup_walk_stats(const gwn_soup_impl& s, float beta, const double* Q, int64_t nQ,
+                     unsigned long long* out7, cudaStream_t st);
 void soup_eval(const gwn_soup_impl& s, float beta, const void* Q, int q_dtype, int64_t nQ,
                void* W, int w_dtype, int precision, cudaStream_t st);
 

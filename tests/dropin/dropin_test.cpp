@@ -1,0 +1,82 @@
+// The reference's own hot-path tests, written against the igl:: drop-in
+// headers (include/igl_gb300/igl/*.h) and run on the GPU through libgwn.so:
+//   tests/include/igl/fast_winding_number.cpp:17-53  one_point_cloud (1e-15)
+//   tests/include/igl/signed_distance.cpp:4-42       single tet (FWN sign)
+// plus the octree and exact winding number on the same data.  Prints
+// "name value" lines that the Python test compares with the CPU oracle.
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include <Eigen/Core>
+#include <igl/fast_winding_number.h>
+#include <igl/octree.h>
+#include <igl/winding_number.h>
+
+static int failures = 0;
+static void check_near(const char* what, double a, double b, double tol) {
+  const bool ok = std::fabs(a - b) <= tol;
+  if (!ok) ++failures;
+  std::printf("%s %.17g %.17g %s\n", what, a, b, ok ? "ok" : "FAIL");
+}
+
+int main() {
+  // one_point_cloud
+  Eigen::MatrixXd P(1, 3);
+  P.set({0.1, 0.2, 0.3});
+  Eigen::MatrixXd N(1, 3);
+  const double nn = std::sqrt(16.0 + 25.0 + 36.0);
+  N.set({4 / nn, 5 / nn, 6 / nn});
+  Eigen::VectorXd A(1);
+  A(0) = 0.7;
+  std::vector<std::vector<int>> O_PI;
+  Eigen::MatrixXi O_CH;
+  Eigen::MatrixXd O_CN;
+  Eigen::VectorXd O_W;
+  igl::octree(P, O_PI, O_CH, O_CN, O_W);
+  Eigen::MatrixXd O_CM;
+  Eigen::VectorXd O_R;
+  Eigen::MatrixXd O_EC;
+  igl::fast_winding_number(P, N, A, O_PI, O_CH, 2, O_CM, O_R, O_EC);
+  Eigen::MatrixXd Q(4, 3);
+  Q.set({0, 0, 0, 4, -3, 2, -1, 1, 3, 0, 5, -2});
+  Eigen::VectorXd WiP;
+  igl::fast_winding_number(P, N, A, O_PI, O_CH, O_CM, O_R, O_EC, Q, 2, WiP);
+  const double cached[4] = {0.38779369004261133, -0.00041235296362485, -0.00362978253577090,
+                            -0.00041235296362485};
+  for (int i = 0; i < 4; ++i) check_near("one_point_cloud", WiP(i), cached[i], 1e-15);
+  std::printf("octree_cells %ld rows_of_EC %ld\n", (long)O_CH.rows(), (long)O_EC.rows());
+
+  // single tet (signed_distance.cpp:4-42): (.5,.5,.5) is outside
+  Eigen::MatrixXd V(4, 3);
+  V.set({0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 1});
+  Eigen::MatrixXi F(4, 3);
+  F.set({0, 1, 3, 0, 2, 1, 0, 3, 2, 1, 2, 3});
+  Eigen::MatrixXd T(2, 3);
+  T.set({0.5, 0.5, 0.5, 0.1, 0.1, 0.1});
+  igl::FastWindingNumberBVH bvh;
+  igl::fast_winding_number(V, F, 2, bvh);
+  Eigen::VectorXd Ws;
+  igl::fast_winding_number(bvh, 2.0f, T, Ws);
+  check_near("tet_soup_outside", Ws(0), 0.0, 1e-6);
+  check_near("tet_soup_inside", Ws(1), 1.0, 1e-6);
+  Eigen::RowVector3d p;
+  p(0, 0) = 0.1;
+  p(0, 1) = 0.1;
+  p(0, 2) = 0.1;
+  check_near("tet_soup_point", igl::fast_winding_number(bvh, 2.0f, p), 1.0, 1e-6);
+  Eigen::VectorXd We;
+  igl::winding_number(V, F, T, We);
+  check_near("tet_exact_outside", We(0), 0.0, 1e-15);
+  check_near("tet_exact_inside", We(1), 1.0, 1e-15);
+  check_near("tet_exact_point", igl::winding_number(V, F, p), 1.0, 1e-15);
+  Eigen::VectorXd W1;
+  igl::fast_winding_number(V, F, T, W1);
+  check_near("tet_soup_oneshot", W1(1), 1.0, 1e-6);
+  // cloud one shot from the tet's face centroids
+  Eigen::VectorXd Wc;
+  igl::fast_winding_number(P, N, A, Q, Wc);
+  for (int i = 0; i < 4; ++i) check_near("one_point_cloud_oneshot", Wc(i), cached[i], 1e-15);
+  std::printf("failures %d\n", failures);
+  return failures ? 1 : 0;
+}

@@ -1,0 +1,36 @@
+"""The igl:: drop-in headers (include/igl_gb300/igl/) compile against the C
+ABI, and -- on a GPU -- reproduce the reference's own Catch2 tests
+(one_point_cloud at 1e-15, the single-tet sign) through libgwn.so."""
+import os
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SRC = os.path.join(ROOT, "tests", "dropin", "dropin_test.cpp")
+OUT_DIR = os.path.join(ROOT, "tests", "dropin", "_build")
+
+
+def compile_dropin(gwn_lib):
+    from libigl_gb300 import _native
+    os.makedirs(OUT_DIR, exist_ok=True)
+    exe = os.path.join(OUT_DIR, "dropin_test")
+    libdir = os.path.dirname(_native.LIB_PATH)
+    cmd = ["g++", "-O1", "-std=c++17", "-I", os.path.join(ROOT, "tests", "dropin", "eigen_shim"),
+           "-I", os.path.join(ROOT, "include", "igl_gb300"), SRC, "-o", exe, "-L", libdir,
+           "-lgwn", f"-Wl,-rpath,{libdir}"]
+    subprocess.run(cmd, check=True)
+    return exe
+
+
+def test_dropin_headers_compile(gwn_lib):
+    assert os.path.exists(compile_dropin(gwn_lib))
+
+
+@pytest.mark.gpu
+def test_dropin_reference_tests_on_gpu(gwn_lib, cuda):
+    exe = compile_dropin(gwn_lib)
+    r = subprocess.run([exe], capture_output=True, text=True)
+    print(r.stdout)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "failures 0" in r.stdout
