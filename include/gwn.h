@@ -78,6 +78,27 @@ int gwn_winding_number(const double* V, int64_t nV, int dim, const int32_t* F, i
                        const void* O, int o_dtype, int64_t nO, void* W, int w_dtype,
                        int precision, int mem, void* stream);
 
+/* No-allocation variant of gwn_winding_number (no counterpart in the
+ * reference).  For callers that must not allocate device memory during a
+ * call: hosts that own every device allocation through their own memory
+ * pool and forbid foreign cudaMalloc, or latency-critical loops in which
+ * cudaMalloc / cudaFree would synchronize the device.  Device pointers only
+ * (V nV x 3, F nF x 3 triangles, O nO x 3, W nO, all float64), mixed
+ * precision, work enqueued on `stream`; nothing is allocated: the call's
+ * scratch is a static device array inside libgwn sized for
+ * GWN_NOALLOC_MAX_TRIANGLES triangles (about 4.2 MB, held by every GPU that
+ * loads the library until the process exits); larger nF is rejected with
+ * GWN_ERR_INVALID_ARGUMENT.  All calls share that array and leave their
+ * contents in it, so calls that overlap on the GPU (on different streams)
+ * race; calls on one stream are ordered.  The first call on a device looks up
+ * the array's device address: make it before any stream capture.
+ * dev_status (optional device pointer, zeroed by the caller) receives
+ * GWN_STATUS_* bits for failures found on the device. */
+#define GWN_NOALLOC_MAX_TRIANGLES 65536
+int gwn_winding_number_noalloc(const double* V, int64_t nV, const int32_t* F, int64_t nF,
+                               const double* O, int64_t nO, double* W, unsigned int* dev_status,
+                               void* stream);
+
 /* ------------------------------------------------------------------------
  * Triangle-soup fast winding number (Barnes-Hut over a GPU-built BVH with the
  * HDK order-0/1/2 far field).

@@ -35,6 +35,7 @@ SIGNATURES = {
     "gwn_version": ([], _i),
     "gwn_device_status": ([_p, _i], _i),
     "gwn_winding_number": ([_p, _i64, _i, _p, _i64, _p, _i, _i64, _p, _i, _i, _i, _p], _i),
+    "gwn_winding_number_noalloc": ([_p, _i64, _p, _i64, _p, _i64, _p, _p, _p], _i),
     "gwn_soup_build": ([_p, _i64, _p, _i64, _i, _i, _p, _p], _i),
     "gwn_soup_eval": ([_p, _f, _p, _i, _i64, _p, _i, _i, _i, _p], _i),
     "gwn_soup_stats_get": ([_p, _p], _i),

@@ -26,6 +26,8 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <mutex>
+#include <string>
 
 #include "gwn_common.cuh"
 #include "gwn_internal.cuh"
@@ -564,6 +566,258 @@ void run_exact(const ExactArgs& a, cudaStream_t st) {
     else if (wd) launch_exact2<float, double>(a, st);
     else launch_exact2<float, float>(a, st);
   }
+}
+
+
+// ---------------------------------------------------------------------------
+// No-allocation variant (gwn_winding_number_noalloc).
+//
+// For callers that must not allocate device memory during a call -- hosts
+// that own every device allocation through their own pool and forbid foreign
+// cudaMalloc, or latency-critical loops where cudaMalloc / cudaFree would
+// synchronize the device.  The caller passes device inputs and outputs; the
+// call's scratch (packed FP32 triangle tiles, tile bounding spheres, bbox
+// words) lives in the file-scope array below, sized for kNoAllocMaxTris
+// triangles (4,203,616 bytes, held by every GPU that loads the library until
+// the process exits).  Every call shares the array and leaves its contents
+// behind, so calls that overlap on the GPU (different streams) race; calls
+// on one stream are ordered.  The first call on a device looks up the
+// array's device address (cudaGetSymbolAddress, with that device current);
+// make that first call before any stream capture.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int64_t kNoAllocMaxTris = 65536;
+constexpr int kNoAllocMaxTiles = (int)(kNoAllocMaxTris / kTile);
+struct NoAllocScratch {
+  TriF tris[kNoAllocMaxTris];          // 4 MiB
+  float4 meta[kNoAllocMaxTiles];       // 8 KiB
+  unsigned long long mm[6];            // bbox as ordered bits
+  unsigned status;                     // used when the caller passes no status word
+};
+static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
+
+__global__ void noalloc_init_kernel(NoAllocScratch* s) {
+  const int i = threadIdx.x;
+  if (i < 3) s->mm[i] = ~0ull;
+  else if (i < 6) s->mm[i] = 0ull;
+  else if (i == 6) s->status = 0u;
+}
+
+// FP32 packing only (near pairs read the caller's FP64 V/F directly).
+__global__ void noalloc_pack_kernel(const double* __restrict__ V, int64_t nV,
+                                    const int32_t* __restrict__ F, int64_t nF, int64_t nPad,
+                                    const unsigned long long* __restrict__ mm,
+                                    TriF* __restrict__ out, unsigned* __restrict__ status) {
+  const int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (f >= nPad) return;
+  double diag2 = 0;
+  for (int d = 0; d < 3; ++d) {
+    const double e = from_ordered_bits(mm[3 + d]) - from_ordered_bits(mm[d]);
+    if (isfinite(e) && e > 0) diag2 += e * e;
+  }
+  const double eps = kNearFrac * sqrt(diag2);
+  TriF t;
+  if (f >= nF) {
+    t.r0 = make_float4(0.f, 0.f, 0.f, 0.f);
+    t.r1 = t.r0;
+    t.r2 = t.r0;
+    t.r3 = make_float4(0.f, 0.f, 0.f, -1.f);
+    out[f] = t;
+    return;
+  }
+  int32_t idx[3];
+  for (int c = 0; c < 3; ++c) {
+    idx[c] = F[f * 3 + c];
+    if (idx[c] < 0 || idx[c] >= nV) {
+      atomicOr(status, kStatusBadInput);
+      idx[c] = 0;
+    }
+  }
+  double p[3][3];
+  for (int c = 0; c < 3; ++c)
+    for (int d = 0; d < 3; ++d) p[c][d] = V[(int64_t)idx[c] * 3 + d];
+  double e1[3], e2[3], n[3], m[3];
+  for (int d = 0; d < 3; ++d) {
+    e1[d] = p[1][d] - p[0][d];
+    e2[d] = p[2][d] - p[0][d];
+    m[d] = (e1[d] + e2[d]) / 3.0;
+  }
+  n[0] = e1[1] * e2[2] - e1[2] * e2[1];
+  n[1] = e1[2] * e2[0] - e1[0] * e2[2];
+  n[2] = e1[0] * e2[1] - e1[1] * e2[0];
+  double r2 = m[0] * m[0] + m[1] * m[1] + m[2] * m[2], t1 = 0, t2 = 0;
+  for (int d = 0; d < 3; ++d) {
+    t1 += (m[d] - e1[d]) * (m[d] - e1[d]);
+    t2 += (m[d] - e2[d]) * (m[d] - e2[d]);
+  }
+  const double R = sqrt(fmax(r2, fmax(t1, t2)));
+  const double rr = (R + eps) * (R + eps) * (1.0 + 1e-5) + 1e-30;
+  t.r0 = make_float4((float)p[0][0], (float)p[0][1], (float)p[0][2], (float)e1[0]);
+  t.r1 = make_float4((float)e1[1], (float)e1[2], (float)e2[0], (float)e2[1]);
+  t.r2 = make_float4((float)e2[2], (float)n[0], (float)n[1], (float)n[2]);
+  t.r3 = make_float4((float)(p[0][0] + m[0]), (float)(p[0][1] + m[1]), (float)(p[0][2] + m[2]),
+                     isfinite(rr) ? (float)rr : INFINITY);
+  out[f] = t;
+}
+
+__device__ __forceinline__ double vos_term64_indexed(const double* __restrict__ V,
+                                                     const int32_t* __restrict__ F, int64_t nV,
+                                                     int64_t f, double qx, double qy, double qz) {
+  int32_t i0 = F[f * 3], i1 = F[f * 3 + 1], i2 = F[f * 3 + 2];
+  if (i0 < 0 || i0 >= nV) i0 = 0;
+  if (i1 < 0 || i1 >= nV) i1 = 0;
+  if (i2 < 0 || i2 >= nV) i2 = 0;
+  return vos_term64(V + (int64_t)i0 * 3, V + (int64_t)i1 * 3, V + (int64_t)i2 * 3, qx, qy, qz);
+}
+
+// The mixed sweep of exact3_mixed_kernel over the static tiles; FP64 near
+// pairs read the caller's V/F; no re-evaluation list is kept.
+__global__ void __launch_bounds__(kThreads) noalloc_mixed_kernel(
+    const TriF* __restrict__ tris, const float4* __restrict__ meta, int ntiles,
+    const double* __restrict__ V, int64_t nV, const int32_t* __restrict__ F,
+    const double* __restrict__ Q, int64_t nQ, double* __restrict__ W,
+    unsigned* __restrict__ status) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  Smem3& sm = *reinterpret_cast<Smem3*>(smem_raw);
+  const int tid = threadIdx.x;
+  const int64_t qi = blockIdx.x * (int64_t)kThreads + tid;
+  const bool valid = qi < nQ;
+  double qx = 0, qy = 0, qz = 0;
+  if (valid) load_q3(Q, qi, qx, qy, qz);
+  const float fx = (float)qx, fy = (float)qy, fz = (float)qz;
+  constexpr uint32_t kTileBytes = sizeof(TriF) * kTile;
+  if (tid == 0) {
+    for (int s = 0; s < kStages; ++s) mbar_init(&sm.bar[s], 1);
+    fence_mbar_init();
+    for (int s = 0; s < kStages && s < ntiles; ++s) {
+      mbar_arrive_expect_tx(&sm.bar[s], kTileBytes);
+      bulk_g2s(&sm.tiles[s][0], tris + (int64_t)s * kTile, kTileBytes, &sm.bar[s]);
+    }
+  }
+  __syncthreads();
+  float acc = 0.f, comp = 0.f;
+  double near_acc = 0.0;
+  bool any_near = false, ok = true;
+  int stop_tile = 0;
+  for (int t = 0; t < ntiles; ++t) {
+    const int s = t % kStages;
+    const bool got = mbar_wait_bounded(&sm.bar[s], (uint32_t)((t / kStages) & 1));
+    if (!__syncthreads_and(got)) {
+      ok = false;
+      stop_tile = t;
+      break;
+    }
+    const float4 mt = __ldg(&meta[t]);
+    const float dx = fx - mt.x, dy = fy - mt.y, dz = fz - mt.z;
+    const bool tile_near = valid && fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < mt.w;
+    float ssum = 0.f;
+    const TriF* tile = sm.tiles[s];
+    if (__any_sync(0xffffffffu, tile_near)) {
+      for (int k = 0; k < kTile; ++k) {
+        const TriF tr = tile[k];
+        const float ex = tr.r3.x - fx, ey = tr.r3.y - fy, ez = tr.r3.z - fz;
+        if (valid && fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < tr.r3.w) {
+          near_acc += vos_term64_indexed(V, F, nV, (int64_t)t * kTile + k, qx, qy, qz);
+          any_near = true;
+        } else {
+          ssum += vos_term32(tr, fx, fy, fz);
+        }
+      }
+    } else {
+#pragma unroll 4
+      for (int k = 0; k < kTile; ++k) ssum += vos_term32(tile[k], fx, fy, fz);
+    }
+    const float y = ssum - comp;
+    const float tt = acc + y;
+    comp = (tt - acc) - y;
+    acc = tt;
+    __syncthreads();
+    if (tid == 0 && t + kStages < ntiles) {
+      fence_proxy_async_smem();
+      mbar_arrive_expect_tx(&sm.bar[s], kTileBytes);
+      bulk_g2s(&sm.tiles[s][0], tris + (int64_t)(t + kStages) * kTile, kTileBytes, &sm.bar[s]);
+    }
+  }
+  if (!ok) {
+    if (tid == 0) {
+      atomicOr(status, kStatusWaitTimeout);
+      drain_ring(sm.bar, kStages, stop_tile, ntiles);
+    }
+    return;
+  }
+  if (!valid) return;
+  W[qi] = any_near ? ((double)acc + near_acc) * kInv2Pi : (double)(acc * kInv2PiF);
+}
+
+// Warp per query: results within 1e-3 of 0.5 are recomputed in FP64 over
+// every triangle (lanes stride the faces; fixed xor-tree reduction).
+__global__ void noalloc_refine_kernel(const double* __restrict__ V, int64_t nV,
+                                      const int32_t* __restrict__ F, int64_t nF,
+                                      const double* __restrict__ Q, int64_t nQ,
+                                      double* __restrict__ W) {
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t qi = warp; qi < nQ; qi += nwarps) {
+    if (!(fabs(W[qi] - 0.5) <= kBand)) continue;  // uniform across the warp
+    double qx, qy, qz;
+    load_q3(Q, qi, qx, qy, qz);
+    double acc = 0.0;
+    for (int64_t f = lane; f < nF; f += 32) acc += vos_term64_indexed(V, F, nV, f, qx, qy, qz);
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) W[qi] = acc / (2.0 * kPi);
+  }
+}
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+NoAllocScratch* g_noalloc_ptr[kNoAllocMaxDevices] = {};  // per device, from cudaGetSymbolAddress
+
+NoAllocScratch* noalloc_scratch_for_current_device() {
+  int dev = 0;
+  GWN_CUDA(cudaGetDevice(&dev));
+  GWN_REQUIRE(dev >= 0 && dev < kNoAllocMaxDevices, "device ordinal out of range");
+  std::lock_guard<std::mutex> lk(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    GWN_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    GWN_REQUIRE(p != nullptr, "static scratch has no device address");
+    g_noalloc_ptr[dev] = static_cast<NoAllocScratch*>(p);
+  }
+  return g_noalloc_ptr[dev];
+}
+
+}  // namespace
+
+int64_t noalloc_max_triangles() { return kNoAllocMaxTris; }
+
+void run_exact_noalloc(const double* V, int64_t nV, const int32_t* F, int64_t nF, const double* Q,
+                       int64_t nQ, double* W, unsigned* dev_status, cudaStream_t st) {
+  GWN_REQUIRE(nF <= kNoAllocMaxTris,
+              "gwn_winding_number_noalloc: nF = " + std::to_string(nF) +
+                  " exceeds the static scratch limit of " + std::to_string(kNoAllocMaxTris) +
+                  " triangles");
+  NoAllocScratch* s = noalloc_scratch_for_current_device();
+  unsigned* status = dev_status ? dev_status : &s->status;
+  launch_kernel(noalloc_init_kernel, 1, 32, 0, st, s);
+  if (nQ == 0) return;
+  if (nV > 0)
+    launch_kernel(bbox_kernel, std::max(1, std::min(num_sms() * 4, (int)((nV + 255) / 256))), 256,
+                  0, st, V, nV, 3, s->mm);
+  const int64_t nPad = ((nF + kTile - 1) / kTile) * (int64_t)kTile;
+  const int ntiles = (int)(nPad / kTile);
+  if (nPad > 0) {
+    launch_kernel(noalloc_pack_kernel, (unsigned)((nPad + 255) / 256), 256, 0, st, V, nV, F, nF,
+                  nPad, s->mm, s->tris, status);
+    launch_kernel(tile_meta_kernel, ntiles, kTile, 0, st, s->tris, ntiles, s->mm, s->meta);
+  }
+  const size_t smem = sizeof(Smem3);
+  GWN_CUDA(cudaFuncSetAttribute(noalloc_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem));
+  launch_kernel(noalloc_mixed_kernel, (unsigned)((nQ + kThreads - 1) / kThreads), kThreads, smem,
+                st, s->tris, s->meta, ntiles, V, nV, F, Q, nQ, W, status);
+  launch_kernel(noalloc_refine_kernel, num_sms() * 8, 256, 0, st, V, nV, F, nF, Q, nQ, W);
 }
 
 }  // namespace gwn

@@ -574,4 +574,22 @@ int gwn_profile_read(char* names, int names_cap, float* ms, int max_phases, int*
 
 unsigned long long gwn_launch_count(void) { return g_launches.load(); }
 
+
+int gwn_winding_number_noalloc(const double* V, int64_t nV, const int32_t* F, int64_t nF,
+                               const double* O, int64_t nO, double* W, unsigned int* dev_status,
+                               void* stream) {
+  return guarded("gwn_winding_number_noalloc", [&] {
+    GWN_REQUIRE(nV >= 0 && nF >= 0 && nO >= 0, "sizes must be non-negative");
+    GWN_REQUIRE(nF == 0 || (V && F), "V and F must be non-null");
+    GWN_REQUIRE(nO == 0 || (O && W), "O and W must be non-null");
+    GWN_REQUIRE(nO < (int64_t(1) << 31), "at most 2^31-1 queries per call");
+    GWN_REQUIRE(nF <= noalloc_max_triangles(),
+                "nF = " + std::to_string(nF) + " exceeds the no-allocation limit of " +
+                    std::to_string(noalloc_max_triangles()) + " triangles");
+    ensure_device();
+    run_exact_noalloc(V, nV, F, nF, static_cast<const double*>(O), nO, W, dev_status,
+                      as_stream(stream));
+  });
+}
+
 }  // extern "C"

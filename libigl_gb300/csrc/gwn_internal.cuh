@@ -27,4 +27,10 @@ struct ExactArgs {
 
 void run_exact(const ExactArgs& a, cudaStream_t st);
 
+// No-allocation exact winding number (device pointers, mixed precision,
+// triangles); scratch in a static device array of fixed capacity.
+int64_t noalloc_max_triangles();
+void run_exact_noalloc(const double* V, int64_t nV, const int32_t* F, int64_t nF, const double* Q,
+                       int64_t nQ, double* W, unsigned* dev_status, cudaStream_t st);
+
 }  // namespace gwn
