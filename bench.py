@@ -56,6 +56,14 @@ def parse():
                     help="target CPU work for the CPU baseline sample")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--workload", choices=["soup", "exact", "cloud", "precision", "served"],
+                    default="soup",
+                    help="soup = the headline line; the others are extra measurement lines")
+    ap.add_argument("--served-seconds", type=float, default=4.0,
+                    help="served: length of the Poisson arrival trace")
+    ap.add_argument("--served-meshes", type=int, default=256)
+    ap.add_argument("--fp64-sample", type=int, default=5000,
+                    help="precision study: FP64 reference queries per (decade, side)")
     return ap.parse_args()
 
 
@@ -211,11 +219,310 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def timed_steps(fn, steps, warmup, stream):
+    """Run fn() warmup times, then time `steps` calls with CUDA events."""
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    ev[0].record(stream)
+    for k in range(steps):
+        fn()
+        ev[k + 1].record(stream)
+    torch.cuda.synchronize()
+    per = [ev[k].elapsed_time(ev[k + 1]) for k in range(steps)]
+    return ev[0].elapsed_time(ev[-1]), per
+
+
+def run_exact_line(args):
+    """Configuration C1: exact winding number, icosphere subdiv 4 (5120
+    triangles, radial noise), 100k float64 queries in [-1.5,1.5]^3."""
+    import torch
+    import libigl_gb300 as G
+    from libigl_gb300 import synth
+    from oracle import oracle as O
+    V, F, Q = synth.exact_workload(seed=0, subdiv=4, nq=100_000)
+    dV, dF, dQ = (torch.from_numpy(x).cuda() for x in (V, F, Q))
+    stream = torch.cuda.current_stream()
+    out = {}
+    for prec in ("mixed", "fp64"):
+        W = None
+
+        def step():
+            nonlocal W
+            W = G.winding_number(dV, dF, dQ, precision=prec)
+        total, per = timed_steps(step, args.steps, args.warmup, stream)
+        out[prec] = (Q.shape[0] * args.steps / (total / 1e3), total / args.steps, W.cpu().numpy())
+    Wm, W64 = out["mixed"][2], out["fp64"][2]
+    t0 = time.perf_counter()
+    Wref = O.winding_number_hier(V, F, Q)
+    cpu_s = time.perf_counter() - t0
+    err = np.abs(Wm - Wref)
+    line = {"metric": METRIC, "value": out["mixed"][0], "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["mixed"][1],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "exact_icosphere4_noise_100kq", "triangles": int(F.shape[0]),
+                       "queries": int(Q.shape[0])},
+            "accuracy": {"max_abs_dW_vs_cpu_fp64": float(err.max()),
+                         "p99_abs_dW": float(np.quantile(err, 0.99)),
+                         "labels_identical": bool(np.array_equal(Wm > 0.5, Wref > 0.5)),
+                         "fp64_gpu_vs_cpu_max": float(np.abs(W64 - Wref).max())},
+            "plain_fp64": {"value": out["fp64"][0], "ms_per_step": out["fp64"][1],
+                           "mixed_speedup": out["mixed"][0] / out["fp64"][0]},
+            "cpu_baseline": {"value": Q.shape[0] / cpu_s, "unit": UNIT, "cores": O.num_threads(0),
+                             "kind": "port",
+                             "sample": "all 100k queries, hierarchical exact restatement "
+                                       "(oracle/wn_hier.cpp), build included"}}
+    print(json.dumps(line), flush=True)
+
+
+def run_cloud_line(args):
+    """Configuration C3: point-cloud FWN, 2M torus samples, 8M queries,
+    order 2, beta 2."""
+    import torch
+    import libigl_gb300 as G
+    from libigl_gb300 import synth
+    from oracle import oracle as O
+    P, Nn, A = synth.torus_cloud(seed=3, n=2_000_000)
+    Q = synth.cloud_queries(seed=4, nq=8_000_000)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    tree = G.Octree(torch.from_numpy(P).cuda())
+    torch.cuda.synchronize()
+    octree_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ce = G.CloudExpansion(torch.from_numpy(P).cuda(), torch.from_numpy(Nn).cuda(),
+                          torch.from_numpy(A).cuda(), order=2, tree=tree)
+    torch.cuda.synchronize()
+    pre_s = time.perf_counter() - t0
+    dQ = torch.from_numpy(Q).cuda()
+    stream = torch.cuda.current_stream()
+    res = {}
+    for prec, steps in (("mixed", args.steps), ("fp64", max(1, args.steps // 5))):
+        W = None
+
+        def step():
+            nonlocal W
+            W = ce.eval(dQ, 2.0, precision=prec)
+        total, per = timed_steps(step, steps, min(args.warmup, 3), stream)
+        res[prec] = (Q.shape[0] * steps / (total / 1e3), total / steps, W.cpu().numpy())
+    Wm, W64 = res["mixed"][2], res["fp64"][2]
+    err = np.abs(Wm - W64)
+    out_band = np.abs(W64 - 0.5) > 1e-3
+    # CPU oracle (restated reference) on a sample of the queries
+    nc = O.num_threads(0)
+    t0 = time.perf_counter()
+    ot = O.octree(P)
+    CM, R, EC = O.cloud_precompute(P, Nn, A, ot, 2)
+    cpu_pre = time.perf_counter() - t0
+    sample = Q[:200_000]
+    t0 = time.perf_counter()
+    Wc = O.cloud_eval(P, Nn, A, ot, CM, R, EC, sample, 2.0)
+    cpu_s = time.perf_counter() - t0
+    line = {"metric": METRIC, "value": res["mixed"][0], "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["mixed"][1],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "cloud_torus_2Mpts_8Mq", "points": int(P.shape[0]),
+                       "queries": int(Q.shape[0]), "order": 2, "beta": 2.0,
+                       "cells": int(tree.sizes()[0])},
+            "accuracy": {"max_abs_dW": float(err.max()), "p99_abs_dW": float(np.quantile(err, 0.99)),
+                         "label_mismatch_outside_band":
+                             int(((Wm > 0.5) != (W64 > 0.5))[out_band].sum()),
+                         "fp64_vs_cpu_oracle_max": float(np.abs(W64[:len(sample)] - Wc).max()),
+                         "queries_compared": int(Q.shape[0])},
+            "plain_fp64": {"value": res["fp64"][0], "ms_per_step": res["fp64"][1],
+                           "mixed_speedup": res["mixed"][0] / res["fp64"][0]},
+            "octree_s": octree_s, "precompute_s": pre_s,
+            "cpu_baseline": {"value": len(sample) / cpu_s, "unit": UNIT, "cores": nc,
+                             "kind": "port", "precompute_s": cpu_pre,
+                             "sample": f"first {len(sample)} queries (oracle restatement of "
+                                       "fast_winding_number.cpp), octree+precompute timed apart"}}
+    print(json.dumps(line), flush=True)
+
+
+def run_precision_study(args):
+    """Configuration C4: 500k-triangle deformed geodesic sphere (nu = 158)
+    with one 2000-triangle hole; 1M queries at 10^-k (k = 1..7) along vertex
+    normals, inside and outside.  Mixed vs plain FP64, exact and soup paths,
+    per decade: max / p99 |dW| and label mismatches outside 0.5 +- 1e-3."""
+    import torch
+    import libigl_gb300 as G
+    from libigl_gb300 import synth
+    V, F, Q, dec, side = synth.precision_workload(seed=5)
+    dV, dF, dQ = (torch.from_numpy(x).cuda() for x in (V, F, Q))
+    rng = np.random.default_rng(0)
+    # FP64 reference sample: fp64_sample queries per (decade, side)
+    idx = []
+    for k in range(1, 8):
+        for sd in (-1.0, 1.0):
+            cand = np.nonzero((dec == k) & (side == sd))[0]
+            idx.append(rng.choice(cand, size=min(args.fp64_sample, cand.size), replace=False))
+    idx = np.sort(np.concatenate(idx))
+    report = {"triangles": int(F.shape[0]), "queries": int(Q.shape[0]),
+              "fp64_reference_queries": int(idx.size)}
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    We_m = G.winding_number(dV, dF, dQ, precision="mixed").cpu().numpy()
+    report["exact_mixed_s"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    We_64 = G.winding_number(dV, dF, dQ[idx], precision="fp64").cpu().numpy()
+    report["exact_fp64_s_sample"] = time.perf_counter() - t0
+    bvh = G.FastWindingNumberBVH(dV, dF, 2)
+    Ws_m = bvh.eval(dQ, 2.0, "mixed").cpu().numpy()
+    Ws_64 = bvh.eval(dQ, 2.0, "fp64").cpu().numpy()
+
+    def stats(a, b, mask):
+        e = np.abs(a - b)[mask]
+        out = np.abs(b - 0.5)[mask] > 1e-3
+        return {"n": int(mask.sum()), "max": float(e.max()), "p99": float(np.quantile(e, 0.99)),
+                "label_mismatch_outside_band": int(((a > 0.5) != (b > 0.5))[mask][out].sum())}
+    per = []
+    for k in range(1, 8):
+        m_all = dec == k
+        m_s = dec[idx] == k
+        per.append({"distance": 10.0 ** -k,
+                    "exact_mixed_vs_fp64": stats(We_m[idx], We_64, m_s),
+                    "soup_mixed_vs_fp64": stats(Ws_m, Ws_64, m_all),
+                    "soup_fp64_vs_exact_fp64": stats(Ws_64[idx], We_64, m_s)})
+    report["per_decade"] = per
+    print(json.dumps({"workload": "precision_study_geodesic158_hole2000_1Mq", **report}),
+          flush=True)
+
+
+def _served_mesh(spec):
+    from libigl_gb300 import synth
+    V, F = synth.served_mesh(spec)
+    return np.ascontiguousarray(V), np.ascontiguousarray(F, np.int32)
+
+
+def run_served_line(args):
+    """Configuration C5: 256 SH-deformed geodesic spheres (F log-uniform in
+    [1e3, 2e6], 20% with a hole) resident under a 120 GB HBM budget;
+    Poisson arrivals at 2000 requests/s, each a uniform mesh with n_q
+    log-uniform in [1e3, 1e6] float32 queries uniform in that mesh's box.
+    Reports served throughput and p50/p99 submit-to-result latency, then the
+    saturated throughput of the first 1000 requests in mixed precision and in
+    plain FP64 through the same server."""
+    import multiprocessing as mp
+    import threading
+    import torch
+    import libigl_gb300 as G
+    from libigl_gb300 import synth
+    specs = synth.served_meshes(seed=6, count=args.served_meshes)
+    t0 = time.perf_counter()
+    order = sorted(range(len(specs)), key=lambda i: -specs[i]["nu"])
+    with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
+        gen = pool.map(_served_mesh, [specs[i] for i in order], chunksize=1)
+    meshes = [None] * len(specs)
+    for i, m in zip(order, gen):
+        meshes[i] = m
+    gen_s = time.perf_counter() - t0
+    torch.cuda.set_device(0)
+    S = G.Server(hbm_budget_bytes=120 << 30, max_batch_queries=1 << 22, slots=3)
+    ids = [S.add_mesh(V, F) for V, F in meshes]
+    ntri = np.array([F.shape[0] for _, F in meshes])
+    rng = np.random.default_rng(7)
+    pool_n = 1_000_000
+    pools = []
+    for V, _ in meshes:
+        lo, hi = V.min(0), V.max(0)
+        pools.append((lo + rng.random((pool_n, 3)) * (hi - lo)).astype(np.float32))
+    # warm-up: one small request per mesh builds every tree (admission)
+    t0 = time.perf_counter()
+    reqs = [S.submit(ids[k], pools[k][:256]) for k in range(len(ids))]
+    for r in reqs:
+        r.wait()
+    warm_s = time.perf_counter() - t0
+    st0 = S.stats()
+    # the trace
+    rate = 2000.0
+    nreq = int(rate * args.served_seconds)
+    arr = np.cumsum(rng.exponential(1.0 / rate, nreq))
+    mesh_of = rng.integers(len(ids), size=nreq)
+    nq_of = np.exp(rng.uniform(np.log(1e3), np.log(1e6), nreq)).astype(np.int64)
+    off_of = (rng.random(nreq) * (pool_n - nq_of)).astype(np.int64)
+    lat = np.zeros(nreq)
+    done_t = np.zeros(nreq)
+    handles = [None] * nreq
+    ready = threading.Semaphore(0)
+
+    def waiter():
+        for i in range(nreq):
+            ready.acquire()
+            _, lat[i] = handles[i].wait()
+            done_t[i] = time.perf_counter()
+    wt = threading.Thread(target=waiter)
+    wt.start()
+    launches0 = G.launch_count()
+    t_start = time.perf_counter()
+    for i in range(nreq):
+        delay = t_start + arr[i] - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        k = int(mesh_of[i])
+        handles[i] = S.submit(ids[k], pools[k][off_of[i]:off_of[i] + nq_of[i]])
+        ready.release()
+    wt.join()
+    span = done_t.max() - t_start
+    st1 = S.stats()
+    launches = G.launch_count() - launches0
+    served_q = int(nq_of.sum())
+
+    def saturated(precision, n):
+        t = time.perf_counter()
+        hs = [S.submit(ids[int(mesh_of[i])],
+                       pools[int(mesh_of[i])][off_of[i]:off_of[i] + nq_of[i]], 2.0, precision)
+              for i in range(n)]
+        for h in hs:
+            h.wait()
+        return int(nq_of[:n].sum()) / (time.perf_counter() - t)
+    nsat = min(1000, nreq)
+    sat_mixed = saturated("mixed", nsat)
+    sat_fp64 = saturated("fp64", nsat)
+    st2 = S.stats()
+    S.close()
+    walk_ms = st1["walk_gpu_ms"] - st0["walk_gpu_ms"]
+    line = {"metric": METRIC, "value": served_q / span, "unit": UNIT, "n_gpus": 1,
+            "steps": 1, "warmup": 1, "ms_per_step": span * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "served_256_meshes_poisson_2000rps", "meshes": len(ids),
+                       "triangles_total": int(ntri.sum()), "requests": nreq,
+                       "queries": served_q, "offered_qps": served_q / arr[-1],
+                       "qdtype": "f32", "hbm_budget_gb": 120, "slots": 3,
+                       "max_batch_queries": 1 << 22},
+            "p50_ms": float(np.percentile(lat, 50) * 1e3),
+            "p99_ms": float(np.percentile(lat, 99) * 1e3),
+            "mean_ms": float(lat.mean() * 1e3),
+            "batches": st1["batches"] - st0["batches"],
+            "walk_gpu_ms": walk_ms,
+            "batch_gpu_ms": st1["batch_gpu_ms"] - st0["batch_gpu_ms"],
+            "refined": st1["refined"] - st0["refined"],
+            "resident": {"meshes": st1["resident_meshes"], "bytes": st1["resident_bytes"],
+                         "builds": st1["builds"], "evictions": st1["evictions"],
+                         "admission_s": warm_s},
+            "saturated_first_1000": {"mixed_qps": sat_mixed, "fp64_qps": sat_fp64,
+                                     "mixed_over_fp64": sat_mixed / sat_fp64,
+                                     "batches": st2["batches"] - st1["batches"]},
+            "mesh_generation_s": gen_s, "gpu_launches": launches,
+            "kernels_per_batch": st1["kernels_per_batch"]}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload != "soup":
+        import torch
+        if args.workload != "served":  # served starts its generator pool first
+            torch.cuda.set_device(local)
+        {"exact": run_exact_line, "cloud": run_cloud_line, "precision": run_precision_study,
+         "served": run_served_line}[args.workload](args)
         return
     import torch
     import libigl_gb300 as G

@@ -201,6 +201,67 @@ int gwn_cloud_eval_arrays(const double* P, const double* N, const double* A, int
                           double beta, double* W, int precision);
 
 /* ------------------------------------------------------------------------
+ * Served evaluation (no counterpart in the reference: libigl evaluates one
+ * mesh per call).  A server keeps triangle meshes resident on the device as
+ * built soup trees and evaluates requests against them, each request being
+ * igl::fast_winding_number(bvh, accuracy_scale, Q, W)
+ * (include/igl/fast_winding_number.h:189-194) for its mesh.
+ *
+ *  - gwn_server_create: hbm_budget_bytes bounds the device bytes of resident
+ *    trees; a tree is built when a request first needs it, and the least
+ *    recently used trees with no request in flight are evicted to make room.
+ *    max_batch_queries bounds the queries of one batch (each request's
+ *    count is padded to a multiple of 32); `slots` batches may be on the
+ *    device at once.  A worker thread forms a batch from the pending
+ *    requests whenever a slot is free (continuous batching) and runs it as
+ *    one captured CUDA graph on that slot's stream.
+ *  - gwn_server_add_mesh copies V (#V x 3 double) and F (#F x 3 int32) into
+ *    the server; the tree is the one gwn_soup_build makes (`order`).
+ *  - gwn_server_submit queues one request; Q (host, #Q x 3, q_dtype) and W
+ *    (host, #Q, w_dtype) must stay valid until gwn_server_wait returns for
+ *    it.  precision as for gwn_soup_eval.  Results equal gwn_soup_eval's on
+ *    the same mesh and queries.
+ *  - gwn_server_wait blocks until the request finished (timeout_s < 0: no
+ *    limit; GWN_ERR_TIMEOUT when it runs out, the request stays queued),
+ *    returns its status, and reports submit-to-result latency in seconds.
+ *    Every submitted request must be waited for once.
+ *  - gwn_server_destroy finishes every queued request, then frees the
+ *    server; no other call on the server may be running or follow.
+ * ---------------------------------------------------------------------- */
+typedef struct gwn_server gwn_server;
+
+typedef struct gwn_server_stats {
+  int64_t requests_done;
+  int64_t queries_done;
+  int64_t batches;
+  int64_t builds;             /* trees built (first use or after eviction) */
+  int64_t evictions;
+  int64_t resident_meshes;
+  int64_t resident_bytes;
+  int64_t peak_resident_bytes;
+  int64_t budget_bytes;
+  int64_t refined;            /* queries re-evaluated in plain FP64 (|W-0.5| <= 1e-3) */
+  int64_t pending;            /* submitted, not yet in a batch */
+  int64_t kernels_per_batch;  /* kernel nodes of one batch graph */
+  double batch_gpu_ms;        /* sum over batches of the graph's device time */
+  double walk_gpu_ms;         /* sum over batches of the walk kernel's time */
+} gwn_server_stats;
+
+int gwn_server_create(int64_t hbm_budget_bytes, int64_t max_batch_queries, int32_t slots,
+                      gwn_server** out);
+int gwn_server_add_mesh(gwn_server* server, const double* V, int64_t nV, const int32_t* F,
+                        int64_t nF, int order, int64_t* mesh_id);
+/* GWN_ERR_BUSY while the mesh has requests queued or in flight. */
+int gwn_server_remove_mesh(gwn_server* server, int64_t mesh_id);
+int gwn_server_submit(gwn_server* server, int64_t mesh_id, const void* Q, int q_dtype,
+                      int64_t nQ, void* W, int w_dtype, float accuracy_scale, int precision,
+                      int64_t* request_id);
+int gwn_server_wait(gwn_server* server, int64_t request_id, double timeout_s,
+                    double* latency_s);
+int gwn_server_stats_get(gwn_server* server, gwn_server_stats* out);
+int gwn_server_destroy(gwn_server* server);
+
+/* ------------------------------------------------------------------------
  * Per-phase timing (no counterpart in the reference; for benchmarks and
  * profiling).  After gwn_profile_enable(1), every call on this thread records
  * CUDA events around its phases on its stream (e.g. "order_queries", "walk",

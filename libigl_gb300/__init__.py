@@ -10,6 +10,8 @@ meaning:
 * ``octree(P)``                          -- igl::octree
 * ``fast_winding_number_cloud_precompute`` / ``fast_winding_number_cloud`` /
   ``fast_winding_number_cloud_oneshot``  -- point-cloud overloads
+* ``Server``                             -- resident meshes, continuously batched
+  soup requests (no libigl counterpart)
 
 Arrays may be NumPy arrays (host memory: the call copies in, computes on the
 GPU, copies out) or CUDA torch tensors (device memory: the work is enqueued on
@@ -24,12 +26,14 @@ import numpy as np
 
 from . import _native as N
 from ._native import GwnError
+from .serve import Server
 
 __all__ = [
     "GwnError", "winding_number", "FastWindingNumberBVH",
     "fast_winding_number_soup_precompute", "fast_winding_number_soup",
     "Octree", "octree", "CloudExpansion", "fast_winding_number_cloud_precompute",
     "fast_winding_number_cloud", "fast_winding_number_cloud_oneshot", "device_status",
+    "Server",
 ]
 
 _PREC = {"fp64": N.GWN_PLAIN_FP64, "plain": N.GWN_PLAIN_FP64, "mixed": N.GWN_MIXED}

@@ -28,7 +28,13 @@ void set_last_error(const std::string& msg) { g_last_error = msg; }
 namespace {
 std::atomic<unsigned long long> g_launches{0};
 }
-void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+static thread_local int t_count_paused = 0;
+void count_launch() {
+  if (!t_count_paused) g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+void count_launches(unsigned long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+LaunchCountPause::LaunchCountPause() { ++t_count_paused; }
+LaunchCountPause::~LaunchCountPause() { --t_count_paused; }
 
 namespace {
 struct PhaseRec {

@@ -188,6 +188,14 @@ void profile_begin_call();
 // Every kernel of the library is launched through launch_kernel: the launch
 // is checked and counted (gwn_launch_count()).
 void count_launch();
+// Adds n launches (kernels run by a graph launch).
+void count_launches(unsigned long long n);
+// While alive, launches made by this thread are not counted (graph capture:
+// the captured kernels are counted when the graph is launched).
+struct LaunchCountPause {
+  LaunchCountPause();
+  ~LaunchCountPause();
+};
 #ifdef __CUDACC__
 template <typename... KArgs, typename... Args>
 inline void launch_kernel(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,

@@ -92,11 +92,15 @@ constexpr int kRsThreads = 256;
 constexpr int kRsRounds = 16;
 constexpr int kRsTile = kRsThreads * kRsRounds;
 
+// n_dev (optional): the element count is min(n, *n_dev), read on the device,
+// so that a captured graph can sort batches of varying size.
 template <typename K>
 __global__ void __launch_bounds__(kRsThreads) rs_hist_kernel(const K* __restrict__ keys,
                                                              int64_t n, int shift,
                                                              uint32_t* __restrict__ counts,
-                                                             int ntiles) {
+                                                             int ntiles,
+                                                             const uint32_t* __restrict__ n_dev) {
+  if (n_dev) n = min(n, (int64_t)*n_dev);
   __shared__ uint32_t h[256];
   h[threadIdx.x] = 0;
   __syncthreads();
@@ -114,7 +118,8 @@ template <typename K>
 __global__ void __launch_bounds__(kRsThreads) rs_scatter_kernel(
     const K* __restrict__ kin, const int32_t* __restrict__ vin, K* __restrict__ kout,
     int32_t* __restrict__ vout, int64_t n, int shift, const uint32_t* __restrict__ offsets,
-    int ntiles) {
+    int ntiles, const uint32_t* __restrict__ n_dev) {
+  if (n_dev) n = min(n, (int64_t)*n_dev);
   __shared__ uint32_t s_base[256];
   __shared__ uint32_t s_warp[kRsThreads / 32][256];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -159,7 +164,17 @@ __global__ void __launch_bounds__(kRsThreads) rs_scatter_kernel(
 
 }  // namespace
 
-void exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, cudaStream_t st) {
+int64_t scan_scratch_elems(int64_t n) {
+  int64_t total = 0;
+  while (n > kScanTile) {
+    n = (n + kScanTile - 1) / kScanTile;
+    total += n;
+  }
+  return total;
+}
+
+void exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, cudaStream_t st,
+                        uint32_t* scratch) {
   if (n <= 0) return;
   const int64_t nt = (n + kScanTile - 1) / kScanTile;
   if (nt == 1) {
@@ -167,11 +182,16 @@ void exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, cudaStream
     GWN_CUDA(cudaGetLastError());
     return;
   }
-  DevBuf<uint32_t> partials((size_t)nt, st);
-  launch_kernel(scan_partials_kernel, (unsigned)nt, kScanThreads, 0, st, in, n, partials.get());
+  DevBuf<uint32_t> own;
+  uint32_t* partials = scratch;
+  if (!partials) {
+    own.alloc((size_t)nt, st);
+    partials = own.get();
+  }
+  launch_kernel(scan_partials_kernel, (unsigned)nt, kScanThreads, 0, st, in, n, partials);
   GWN_CUDA(cudaGetLastError());
-  exclusive_scan_u32(partials.get(), partials.get(), nt, st);
-  launch_kernel(scan_tiles_kernel, (unsigned)nt, kScanThreads, 0, st, in, out, n, partials.get());
+  exclusive_scan_u32(partials, partials, nt, st, scratch ? scratch + nt : nullptr);
+  launch_kernel(scan_tiles_kernel, (unsigned)nt, kScanThreads, 0, st, in, out, n, partials);
   GWN_CUDA(cudaGetLastError());
 }
 
@@ -187,18 +207,46 @@ void radix_sort_pairs(K* keys, int32_t* vals, K* keys_tmp, int32_t* vals_tmp, in
   K* kb = keys_tmp;
   int32_t* vb = vals_tmp;
   for (int shift = begin_bit; shift < end_bit; shift += 8) {
-    launch_kernel(rs_hist_kernel<K>, ntiles, kRsThreads, 0, st, ka, n, shift, counts.get(), ntiles);
-    GWN_CUDA(cudaGetLastError());
+    launch_kernel(rs_hist_kernel<K>, ntiles, kRsThreads, 0, st, ka, n, shift, counts.get(), ntiles,
+                  (const uint32_t*)nullptr);
     exclusive_scan_u32(counts.get(), counts.get(), (int64_t)ntiles * 256, st);
-    launch_kernel(rs_scatter_kernel<K>, ntiles, kRsThreads, 0, st, ka, va, kb, vb, n, shift, counts.get(),
-                                                        ntiles);
-    GWN_CUDA(cudaGetLastError());
+    launch_kernel(rs_scatter_kernel<K>, ntiles, kRsThreads, 0, st, ka, va, kb, vb, n, shift,
+                  counts.get(), ntiles, (const uint32_t*)nullptr);
     std::swap(ka, kb);
     std::swap(va, vb);
   }
   if (ka != keys) {
     GWN_CUDA(cudaMemcpyAsync(keys, ka, (size_t)n * sizeof(K), cudaMemcpyDeviceToDevice, st));
     GWN_CUDA(cudaMemcpyAsync(vals, va, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToDevice, st));
+  }
+}
+
+void radix_sort_scratch_elems(int64_t cap, int64_t* counts_elems, int64_t* scan_elems) {
+  const int64_t ntiles = (cap + kRsTile - 1) / kRsTile;
+  *counts_elems = ntiles * 256;
+  *scan_elems = scan_scratch_elems(ntiles * 256);
+}
+
+void radix_sort_pairs_devn(uint32_t* keys, int32_t* vals, uint32_t* keys_tmp, int32_t* vals_tmp,
+                           int64_t cap, const uint32_t* n_dev, int begin_bit, int end_bit,
+                           uint32_t* counts, uint32_t* scan_scratch, cudaStream_t st) {
+  GWN_REQUIRE(((end_bit - begin_bit) / 8) % 2 == 0 && (end_bit - begin_bit) % 8 == 0,
+              "radix_sort_pairs_devn: an even number of 8-bit passes");
+  if (cap <= 0) return;
+  GWN_REQUIRE(cap < (int64_t(1) << 32), "radix sort: at most 2^32-1 elements");
+  const int ntiles = (int)((cap + kRsTile - 1) / kRsTile);
+  uint32_t* ka = keys;
+  int32_t* va = vals;
+  uint32_t* kb = keys_tmp;
+  int32_t* vb = vals_tmp;
+  for (int shift = begin_bit; shift < end_bit; shift += 8) {
+    launch_kernel(rs_hist_kernel<uint32_t>, ntiles, kRsThreads, 0, st, ka, cap, shift, counts,
+                  ntiles, n_dev);
+    exclusive_scan_u32(counts, counts, (int64_t)ntiles * 256, st, scan_scratch);
+    launch_kernel(rs_scatter_kernel<uint32_t>, ntiles, kRsThreads, 0, st, ka, va, kb, vb, cap,
+                  shift, counts, ntiles, n_dev);
+    std::swap(ka, kb);
+    std::swap(va, vb);
   }
 }
 

@@ -49,6 +49,7 @@
 #include "bh_common.cuh"
 #include "gwn_common.cuh"
 #include "soup.cuh"
+#include "soup_walk.cuh"
 #include "sort.cuh"
 
 namespace gwn {
@@ -56,9 +57,9 @@ namespace gwn {
 namespace {
 
 constexpr double kNearFrac = 1e-3;
-constexpr double kBand = 1e-3;
-constexpr float kInv4PiF = 0.079577471545947667884f;
-constexpr double kInv4Pi = 0.079577471545947667884;
+using soupwalk::EvalParams;
+using soupwalk::kBand;
+using soupwalk::kInv4Pi;
 
 // Per-node FP64 build data (moments about the node's own average point P).
 struct BuildM {
@@ -441,106 +442,6 @@ __global__ void emit_kernel(const BuildM* __restrict__ M, const int32_t* __restr
   }
 }
 
-// --------------------------------------------------------------- evaluate --
-// Far field of one node about its average point, FWNFS.h:7195-7251, with
-// (dx,dy,dz) = q - P and r2 = |q - P|^2.  T is float or double.
-template <typename T>
-struct Far {
-  T N[3], Nii[3], Nxy_yx, Nyz_zy, Nzx_xz, Niii[3], perm, c2[6];
-};
-
-template <typename T>
-__device__ __forceinline__ T far_field(const Far<T>& m, T dx, T dy, T dz, T r2, int order) {
-  // m1 = 1/|q-P|, m2 = m1^2 (FP64: 1/r2 then sqrt, as the reference;
-  // FP32: one reciprocal square root)
-  T m1, m2;
-  if (sizeof(T) == 4) {
-    m1 = g_rsqrt(r2);
-    m2 = m1 * m1;
-  } else {
-    m2 = T(1) / r2;
-    m1 = g_sqrt(m2);
-  }
-  const T qx = dx * m1, qy = dy * m1, qz = dz * m1;
-  T omega = -m2 * (qx * m.N[0] + qy * m.N[1] + qz * m.N[2]);
-  if (order >= 1) {
-    const T q2x = qx * qx, q2y = qy * qy, q2z = qz * qz;
-    const T m3 = m2 * m1;
-    omega += m3 * (m.Nii[0] + m.Nii[1] + m.Nii[2] -
-                   T(3) * (q2x * m.Nii[0] + q2y * m.Nii[1] + q2z * m.Nii[2] + qx * qy * m.Nxy_yx +
-                           qx * qz * m.Nzx_xz + qy * qz * m.Nyz_zy));
-    if (order >= 2) {
-      const T q3x = q2x * qx, q3y = q2y * qy, q3z = q2z * qz;
-      const T m4 = m2 * m2;
-      const T t0x = m.c2[3] + m.c2[4], t0y = m.c2[5] + m.c2[0], t0z = m.c2[1] + m.c2[2];
-      const T t1x = qy * m.c2[0] + qz * m.c2[1];
-      const T t1y = qz * m.c2[2] + qx * m.c2[3];
-      const T t1z = qx * m.c2[4] + qy * m.c2[5];
-      omega += m4 * (T(1.5) * (qx * (T(3) * m.Niii[0] + t0x) + qy * (T(3) * m.Niii[1] + t0y) +
-                               qz * (T(3) * m.Niii[2] + t0z)) -
-                     T(7.5) * (q3x * m.Niii[0] + q3y * m.Niii[1] + q3z * m.Niii[2] +
-                               qx * qy * qz * m.perm + q2x * t1x + q2y * t1y + q2z * t1z));
-    }
-  }
-  return omega;
-}
-
-// Exact triangle solid angle, FWNFS.h:6070-6110 (normalised corner vectors).
-template <typename T>
-__device__ __forceinline__ T tri_solid_angle(T ax, T ay, T az, T bx, T by, T bz, T cx, T cy,
-                                             T cz) {
-  const T la2 = ax * ax + ay * ay + az * az;
-  const T lb2 = bx * bx + by * by + bz * bz;
-  const T lc2 = cx * cx + cy * cy + cz * cz;
-  if (la2 == T(0) || lb2 == T(0) || lc2 == T(0)) return T(0);
-  if (sizeof(T) == 4) {  // normalise with reciprocal square roots
-    const T ia = g_rsqrt(la2), ib = g_rsqrt(lb2), ic = g_rsqrt(lc2);
-    ax *= ia; ay *= ia; az *= ia;
-    bx *= ib; by *= ib; bz *= ib;
-    cx *= ic; cy *= ic; cz *= ic;
-  } else {  // FP64: length then divide, as FWNFS.h:6085-6095
-    const T la = g_sqrt(la2), lb = g_sqrt(lb2), lc = g_sqrt(lc2);
-    ax /= la; ay /= la; az /= la;
-    bx /= lb; by /= lb; bz /= lb;
-    cx /= lc; cy /= lc; cz /= lc;
-  }
-  const T ux = bx - ax, uy = by - ay, uz = bz - az;
-  const T vx = cx - ax, vy = cy - ay, vz = cz - az;
-  const T num = ax * (uy * vz - uz * vy) + ay * (uz * vx - ux * vz) + az * (ux * vy - uy * vx);
-  if (num == T(0)) return T(0);
-  const T den = T(1) + (ax * bx + ay * by + az * bz) + (ax * cx + ay * cy + az * cz) +
-                (bx * cx + by * cy + bz * cz);
-  return T(2) * g_atan2(num, den);
-}
-
-__device__ __forceinline__ Far<float> load_far(const SoupNodeF* r) {
-  const float4 b = __ldg(&r->b), c = __ldg(&r->c), d = __ldg(&r->d), e = __ldg(&r->e),
-               f = __ldg(&r->f);
-  Far<float> m;
-  m.N[0] = b.x; m.N[1] = b.y; m.N[2] = b.z;
-  m.Nii[0] = b.w; m.Nii[1] = c.x; m.Nii[2] = c.y;
-  m.Nxy_yx = c.z; m.Nyz_zy = c.w; m.Nzx_xz = d.x;
-  m.Niii[0] = d.y; m.Niii[1] = d.z; m.Niii[2] = d.w;
-  m.perm = e.x; m.c2[0] = e.y; m.c2[1] = e.z; m.c2[2] = e.w;
-  m.c2[3] = f.x; m.c2[4] = f.y; m.c2[5] = f.z;
-  return m;
-}
-
-__device__ __forceinline__ Far<double> load_far(const SoupNodeD* r) {
-  Far<double> m;
-  for (int d = 0; d < 3; ++d) {
-    m.N[d] = r->N[d];
-    m.Nii[d] = r->Nii[d];
-    m.Niii[d] = r->Niii[d];
-  }
-  m.Nxy_yx = r->Nxy_yx;
-  m.Nyz_zy = r->Nyz_zy;
-  m.Nzx_xz = r->Nzx_xz;
-  m.perm = r->perm;
-  for (int k = 0; k < 6; ++k) m.c2[k] = r->c2[k];
-  return m;
-}
-
 template <typename QT>
 __device__ __forceinline__ void read_query(const QT* Q, const int32_t* perm, const int32_t* list,
                                            int64_t i, int64_t& qi, double& x, double& y,
@@ -551,20 +452,7 @@ __device__ __forceinline__ void read_query(const QT* Q, const int32_t* perm, con
   z = (double)Q[qi * 3 + 2];
 }
 
-struct EvalParams {
-  const SoupNodeF* nf;
-  const SoupNodeD* nd;
-  const float4* tf;
-  const double* td;
-  int nnodes;
-  int order;
-  float beta2f;
-  double beta2d;
-  float eps;       // near-field distance (1e-3 * bbox diagonal)
-  float cmax;      // max |coordinate| of any node centre
-  unsigned* status;
-};
-
+// --------------------------------------------------------------- evaluate --
 // Mixed-precision warp-coherent walk.  One query per lane.  kStats builds
 // an instrumented copy that counts its work into `stats` (see
 // gwn_soup_walk_stats); the timed kernel is the kStats = false instance.
@@ -575,92 +463,26 @@ __global__ void __launch_bounds__(128) soup_eval_mixed_kernel(EvalParams prm, co
                                                               int32_t* __restrict__ refine_list,
                                                               unsigned* __restrict__ refine_count,
                                                               unsigned long long* __restrict__ stats = nullptr) {
-  unsigned long long st_steps = 0, st_visits = 0, st_far = 0, st_exact32 = 0, st_exact64 = 0,
-                     st_recheck = 0;
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const bool valid = i < nQ;
   int64_t qi = 0;
   double qx = 0, qy = 0, qz = 0;
   if (valid) read_query(Q, perm, (const int32_t*)nullptr, i, qi, qx, qy, qz);
-  const float fx = (float)qx, fy = (float)qy, fz = (float)qz;
-  const float S = fmaxf(fabsf(fx), fmaxf(fabsf(fy), fabsf(fz))) + prm.cmax;
-  const float sigma = guard_sigma(S);
-  float acc = 0.f;
-  double acc64 = 0.0;
-  int resume = valid ? 0 : 0x7fffffff;
-  int node = 0;
-  const unsigned full = 0xffffffffu;
-  while (node < prm.nnodes) {
-    const SoupNodeF* r = prm.nf + node;
-    const float4 a = __ldg(&r->a);
-    const int link = __float_as_int(__ldg(&r->f).w);
-    bool open = false;
-    if (kStats) ++st_steps;
-    if (node >= resume) {
-      if (kStats) ++st_visits;
-      const bool leaf = link < 0;
-      if (node == 0 && !leaf) {
-        open = true;
-      } else {
-        const float dx = fx - a.x, dy = fy - a.y, dz = fz - a.z;
-        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-        const float thr = a.w * prm.beta2f;
-        bool near = r2 <= thr;
-        if (in_guard_band(r2, thr, sigma)) {
-          const SoupNodeD* rd = prm.nd + node;
-          near = open_test64(qx, qy, qz, rd->P[0], rd->P[1], rd->P[2], rd->maxP2, prm.beta2d);
-          if (kStats) ++st_recheck;
-        }
-        if (!near) {
-          if (kStats) ++st_far;
-          const float om = far_field<float>(load_far(r), dx, dy, dz, r2, prm.order);
-          if (isfinite(om)) {
-            acc += om;
-            resume = leaf ? node + 1 : link;
-          } else {
-            near = true;
-          }
-        }
-        if (near) {
-          if (leaf) {
-            const int slot = ~link;
-            const float rad = sqrtf(a.w) + prm.eps;
-            if (r2 <= rad * rad * 1.0001f) {
-              if (kStats) ++st_exact64;
-              const double* t = prm.td + (int64_t)slot * 9;
-              acc64 += tri_solid_angle<double>(t[0] - qx, t[1] - qy, t[2] - qz, t[3] - qx,
-                                               t[4] - qy, t[5] - qz, t[6] - qx, t[7] - qy,
-                                               t[8] - qz);
-            } else {
-              if (kStats) ++st_exact32;
-              const float4 t0 = __ldg(&prm.tf[(int64_t)slot * 3]);
-              const float4 t1 = __ldg(&prm.tf[(int64_t)slot * 3 + 1]);
-              const float4 t2 = __ldg(&prm.tf[(int64_t)slot * 3 + 2]);
-              acc += tri_solid_angle<float>(t0.x - fx, t0.y - fy, t0.z - fz, t0.w - fx, t1.x - fy,
-                                            t1.y - fz, t1.z - fx, t1.w - fy, t2.x - fz);
-            }
-            resume = node + 1;
-          } else {
-            open = true;
-          }
-        }
-      }
-    }
-    if (__any_sync(full, open))
-      node = node + 1;
-    else
-      node = __reduce_min_sync(full, resume);
-  }
+  __shared__ soupwalk::NearQueue near_q[4];
+  float acc;
+  double acc64;
+  soupwalk::WalkCounters c;
+  soupwalk::walk_mixed<kStats>(prm, valid, qx, qy, qz, acc, acc64, c, near_q[threadIdx.x >> 5]);
   if (kStats) {
-    if ((threadIdx.x & 31) == 0) atomicAdd(&stats[0], st_steps);
-    atomicAdd(&stats[1], st_visits);
-    atomicAdd(&stats[2], st_far);
-    atomicAdd(&stats[3], st_exact32);
-    atomicAdd(&stats[4], st_exact64);
-    atomicAdd(&stats[5], st_recheck);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&stats[0], c.steps);
+    atomicAdd(&stats[1], c.visits);
+    atomicAdd(&stats[2], c.far);
+    atomicAdd(&stats[3], c.exact32);
+    atomicAdd(&stats[4], c.exact64);
+    atomicAdd(&stats[5], c.recheck);
   }
   if (!valid) return;
-  const double w = acc64 != 0.0 ? ((double)acc + acc64) * kInv4Pi : (double)(acc * kInv4PiF);
+  const double w = soupwalk::mixed_result(acc, acc64);
   W[qi] = (WT)w;
   if (fabs(w - 0.5) <= kBand) {
     const unsigned s = atomicAdd(refine_count, 1u);
@@ -682,48 +504,7 @@ __global__ void __launch_bounds__(128) soup_eval_fp64_kernel(EvalParams prm, con
   int64_t qi = 0;
   double qx = 0, qy = 0, qz = 0;
   if (valid) read_query(Q, perm, list, i, qi, qx, qy, qz);
-  double acc = 0.0;
-  int resume = valid ? 0 : 0x7fffffff;
-  int node = 0;
-  const unsigned full = 0xffffffffu;
-  while (node < prm.nnodes) {
-    const SoupNodeD* r = prm.nd + node;
-    bool open = false;
-    if (node >= resume) {
-      const long long link = r->link;
-      const bool leaf = link < 0;
-      if (node == 0 && !leaf) {
-        open = true;
-      } else {
-        bool near = open_test64(qx, qy, qz, r->P[0], r->P[1], r->P[2], r->maxP2, prm.beta2d);
-        const double dx = qx - r->P[0], dy = qy - r->P[1], dz = qz - r->P[2];
-        const double r2 = dx * dx + dy * dy + dz * dz;
-        if (!near) {
-          const double om = far_field<double>(load_far(r), dx, dy, dz, r2, prm.order);
-          if (isfinite(om)) {
-            acc += om;
-            resume = leaf ? node + 1 : (int)link;
-          } else {
-            near = true;
-          }
-        }
-        if (near) {
-          if (leaf) {
-            const double* t = prm.td + (int64_t)(~link) * 9;
-            acc += tri_solid_angle<double>(t[0] - qx, t[1] - qy, t[2] - qz, t[3] - qx, t[4] - qy,
-                                           t[5] - qz, t[6] - qx, t[7] - qy, t[8] - qz);
-            resume = node + 1;
-          } else {
-            open = true;
-          }
-        }
-      }
-    }
-    if (__any_sync(full, open))
-      node = node + 1;
-    else
-      node = __reduce_min_sync(full, resume);
-  }
+  const double acc = soupwalk::walk_fp64(prm, valid, qx, qy, qz);
   if (valid) W[qi] = (WT)(acc * kInv4Pi);
 }
 

@@ -1,0 +1,394 @@
+// Device-side pieces of the triangle-soup Barnes-Hut walk shared by the
+// single-mesh evaluation (soup.cu) and the multi-mesh served batches
+// (serve.cu): node records -> far field, exact triangle term, and the three
+// walks (mixed warp-coherent, plain FP64 warp-coherent, plain FP64 per lane).
+//
+// Reference: UT_SolidAngle::computeSolidAngle (include/igl/
+// FastWindingNumberForSoups.h:7148-7284) and UTsignedSolidAngleTri
+// (FastWindingNumberForSoups.h:6070-6110).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "bh_common.cuh"
+#include "gwn_common.cuh"
+#include "soup.cuh"
+
+namespace gwn {
+namespace soupwalk {
+
+constexpr double kBand = 1e-3;  // |W - 0.5| band re-evaluated in plain FP64
+constexpr float kInv4PiF = 0.079577471545947667884f;
+constexpr double kInv4Pi = 0.079577471545947667884;
+
+// Far field of one node about its average point, FWNFS.h:7195-7251, with
+// (dx,dy,dz) = q - P and r2 = |q - P|^2.  T is float or double.
+template <typename T>
+struct Far {
+  T N[3], Nii[3], Nxy_yx, Nyz_zy, Nzx_xz, Niii[3], perm, c2[6];
+};
+
+template <typename T>
+__device__ __forceinline__ T far_field(const Far<T>& m, T dx, T dy, T dz, T r2, int order) {
+  // m1 = 1/|q-P|, m2 = m1^2 (FP64: 1/r2 then sqrt, as the reference;
+  // FP32: one reciprocal square root)
+  T m1, m2;
+  if (sizeof(T) == 4) {
+    m1 = g_rsqrt(r2);
+    m2 = m1 * m1;
+  } else {
+    m2 = T(1) / r2;
+    m1 = g_sqrt(m2);
+  }
+  const T qx = dx * m1, qy = dy * m1, qz = dz * m1;
+  T omega = -m2 * (qx * m.N[0] + qy * m.N[1] + qz * m.N[2]);
+  if (order >= 1) {
+    const T q2x = qx * qx, q2y = qy * qy, q2z = qz * qz;
+    const T m3 = m2 * m1;
+    omega += m3 * (m.Nii[0] + m.Nii[1] + m.Nii[2] -
+                   T(3) * (q2x * m.Nii[0] + q2y * m.Nii[1] + q2z * m.Nii[2] + qx * qy * m.Nxy_yx +
+                           qx * qz * m.Nzx_xz + qy * qz * m.Nyz_zy));
+    if (order >= 2) {
+      const T q3x = q2x * qx, q3y = q2y * qy, q3z = q2z * qz;
+      const T m4 = m2 * m2;
+      const T t0x = m.c2[3] + m.c2[4], t0y = m.c2[5] + m.c2[0], t0z = m.c2[1] + m.c2[2];
+      const T t1x = qy * m.c2[0] + qz * m.c2[1];
+      const T t1y = qz * m.c2[2] + qx * m.c2[3];
+      const T t1z = qx * m.c2[4] + qy * m.c2[5];
+      omega += m4 * (T(1.5) * (qx * (T(3) * m.Niii[0] + t0x) + qy * (T(3) * m.Niii[1] + t0y) +
+                               qz * (T(3) * m.Niii[2] + t0z)) -
+                     T(7.5) * (q3x * m.Niii[0] + q3y * m.Niii[1] + q3z * m.Niii[2] +
+                               qx * qy * qz * m.perm + q2x * t1x + q2y * t1y + q2z * t1z));
+    }
+  }
+  return omega;
+}
+
+// Exact triangle solid angle, FWNFS.h:6070-6110 (normalised corner vectors).
+template <typename T>
+__device__ __forceinline__ T tri_solid_angle(T ax, T ay, T az, T bx, T by, T bz, T cx, T cy,
+                                             T cz) {
+  const T la2 = ax * ax + ay * ay + az * az;
+  const T lb2 = bx * bx + by * by + bz * bz;
+  const T lc2 = cx * cx + cy * cy + cz * cz;
+  if (la2 == T(0) || lb2 == T(0) || lc2 == T(0)) return T(0);
+  if (sizeof(T) == 4) {  // normalise with reciprocal square roots
+    const T ia = g_rsqrt(la2), ib = g_rsqrt(lb2), ic = g_rsqrt(lc2);
+    ax *= ia; ay *= ia; az *= ia;
+    bx *= ib; by *= ib; bz *= ib;
+    cx *= ic; cy *= ic; cz *= ic;
+  } else {  // FP64: length then divide, as FWNFS.h:6085-6095
+    const T la = g_sqrt(la2), lb = g_sqrt(lb2), lc = g_sqrt(lc2);
+    ax /= la; ay /= la; az /= la;
+    bx /= lb; by /= lb; bz /= lb;
+    cx /= lc; cy /= lc; cz /= lc;
+  }
+  const T ux = bx - ax, uy = by - ay, uz = bz - az;
+  const T vx = cx - ax, vy = cy - ay, vz = cz - az;
+  const T num = ax * (uy * vz - uz * vy) + ay * (uz * vx - ux * vz) + az * (ux * vy - uy * vx);
+  if (num == T(0)) return T(0);
+  const T den = T(1) + (ax * bx + ay * by + az * bz) + (ax * cx + ay * cy + az * cz) +
+                (bx * cx + by * cy + bz * cz);
+  return T(2) * g_atan2(num, den);
+}
+
+__device__ __forceinline__ Far<float> load_far(const SoupNodeF* r) {
+  const float4 b = __ldg(&r->b), c = __ldg(&r->c), d = __ldg(&r->d), e = __ldg(&r->e),
+               f = __ldg(&r->f);
+  Far<float> m;
+  m.N[0] = b.x; m.N[1] = b.y; m.N[2] = b.z;
+  m.Nii[0] = b.w; m.Nii[1] = c.x; m.Nii[2] = c.y;
+  m.Nxy_yx = c.z; m.Nyz_zy = c.w; m.Nzx_xz = d.x;
+  m.Niii[0] = d.y; m.Niii[1] = d.z; m.Niii[2] = d.w;
+  m.perm = e.x; m.c2[0] = e.y; m.c2[1] = e.z; m.c2[2] = e.w;
+  m.c2[3] = f.x; m.c2[4] = f.y; m.c2[5] = f.z;
+  return m;
+}
+
+__device__ __forceinline__ Far<double> load_far(const SoupNodeD* r) {
+  Far<double> m;
+  for (int d = 0; d < 3; ++d) {
+    m.N[d] = r->N[d];
+    m.Nii[d] = r->Nii[d];
+    m.Niii[d] = r->Niii[d];
+  }
+  m.Nxy_yx = r->Nxy_yx;
+  m.Nyz_zy = r->Nyz_zy;
+  m.Nzx_xz = r->Nzx_xz;
+  m.perm = r->perm;
+  for (int k = 0; k < 6; ++k) m.c2[k] = r->c2[k];
+  return m;
+}
+
+template <typename QT>
+__device__ __forceinline__ void read_query(const QT* Q, const int32_t* perm, const int32_t* list,
+                                           int64_t i, int64_t& qi, double& x, double& y,
+                                           double& z) {
+  qi = list ? (int64_t)list[i] : (perm ? (int64_t)perm[i] : i);
+  x = (double)Q[qi * 3 + 0];
+  y = (double)Q[qi * 3 + 1];
+  z = (double)Q[qi * 3 + 2];
+}
+
+struct EvalParams {
+  const SoupNodeF* nf;
+  const SoupNodeD* nd;
+  const float4* tf;
+  const double* td;
+  int nnodes;
+  int order;
+  float beta2f;
+  double beta2d;
+  float eps;       // near-field distance (1e-3 * bbox diagonal)
+  float cmax;      // max |coordinate| of any node centre
+  unsigned* status;
+};
+
+// FP64 solid angle of the triangle t[0..8] (xyz of three corners) seen from
+// q, in the unnormalised van Oosterom-Strackee form of igl::solid_angle
+// (include/igl/solid_angle.cpp:22-48): with A, B, C the corners relative to
+// q, tan(Omega/2) = A.(B x C) / (|A||B||C| + (A.B)|C| + (A.C)|B| + (B.C)|A|).
+// Equal to the normalised form of tri_solid_angle up to rounding, without
+// its nine divisions.  A corner at q or a zero determinant gives 0, as there.
+__device__ __forceinline__ double solid_angle_vos64(const double* __restrict__ t, double qx,
+                                                    double qy, double qz) {
+  const double ax = t[0] - qx, ay = t[1] - qy, az = t[2] - qz;
+  const double bx = t[3] - qx, by = t[4] - qy, bz = t[5] - qz;
+  const double cx = t[6] - qx, cy = t[7] - qy, cz = t[8] - qz;
+  const double la2 = ax * ax + ay * ay + az * az;
+  const double lb2 = bx * bx + by * by + bz * bz;
+  const double lc2 = cx * cx + cy * cy + cz * cz;
+  if (la2 == 0.0 || lb2 == 0.0 || lc2 == 0.0) return 0.0;
+  const double det = ax * (by * cz - bz * cy) + ay * (bz * cx - bx * cz) + az * (bx * cy - by * cx);
+  if (det == 0.0) return 0.0;
+  const double la = sqrt(la2), lb = sqrt(lb2), lc = sqrt(lc2);
+  const double den = la * lb * lc + (ax * bx + ay * by + az * bz) * lc +
+                     (ax * cx + ay * cy + az * cz) * lb + (bx * cx + by * cy + bz * cz) * la;
+  return 2.0 * atan2(det, den);
+}
+
+// Per-warp queue of FP64 near-field terms (triangle slot, owning lane).
+// The walk does not evaluate an FP64 triangle term where it arises: the
+// lanes that need one append it here, and when the queue would overflow (and
+// at the end of the walk) the warp evaluates up to 32 queued terms at once,
+// one per lane, so that each FP64 instruction serves the whole warp instead
+// of the few lanes that share a leaf.  Every lane still adds its own terms in
+// node order, so the sum does not depend on the other lanes of the warp.
+struct NearQueue {
+  int2 e[32];
+};
+
+__device__ __forceinline__ void flush_near64(const double* __restrict__ td, const NearQueue& q,
+                                             int n, double qx, double qy, double qz,
+                                             double& acc64) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  __syncwarp();
+  int2 e = make_int2(0, lane);
+  if (lane < n) e = q.e[lane];
+  const double ox = __shfl_sync(full, qx, e.y), oy = __shfl_sync(full, qy, e.y),
+               oz = __shfl_sync(full, qz, e.y);
+  double v = 0.0;
+  if (lane < n) v = solid_angle_vos64(td + (int64_t)e.x * 9, ox, oy, oz);
+  for (int k = 0; k < n; ++k) {
+    const double vk = __shfl_sync(full, v, k);
+    const int ok = __shfl_sync(full, e.y, k);
+    if (ok == lane) acc64 += vk;
+  }
+  __syncwarp();
+}
+
+// Work counters of the instrumented walk (only touched when kStats).
+struct WalkCounters {
+  unsigned long long steps = 0, visits = 0, far = 0, exact32 = 0, exact64 = 0, recheck = 0;
+};
+
+// Mixed-precision warp-coherent walk of one query per lane.  All 32 lanes of
+// the warp must call it together (invalid lanes pass valid = false).  FP32
+// records and arithmetic; the open test is redone in FP64 inside the guard
+// band; exact triangle terms within eps of the query are taken in FP64
+// through the warp's NearQueue `nq` (shared memory).  Returns the
+// solid-angle sum as an FP32 part and an FP64 part.
+template <bool kStats>
+__device__ __forceinline__ void walk_mixed(const EvalParams& prm, bool valid, double qx, double qy,
+                                           double qz, float& acc, double& acc64,
+                                           WalkCounters& c, NearQueue& nq) {
+  const int lane = threadIdx.x & 31;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  int nqueued = 0;  // warp-uniform
+  const float fx = (float)qx, fy = (float)qy, fz = (float)qz;
+  const float S = fmaxf(fabsf(fx), fmaxf(fabsf(fy), fabsf(fz))) + prm.cmax;
+  const float sigma = guard_sigma(S);
+  acc = 0.f;
+  acc64 = 0.0;
+  int resume = valid ? 0 : 0x7fffffff;
+  int node = 0;
+  const unsigned full = 0xffffffffu;
+  while (node < prm.nnodes) {
+    const SoupNodeF* r = prm.nf + node;
+    const float4 a = __ldg(&r->a);
+    const int link = __float_as_int(__ldg(&r->f).w);
+    bool open = false;
+    bool want64 = false;
+    int slot64 = 0;
+    if (kStats) ++c.steps;
+    if (node >= resume) {
+      if (kStats) ++c.visits;
+      const bool leaf = link < 0;
+      if (node == 0 && !leaf) {
+        open = true;
+      } else {
+        const float dx = fx - a.x, dy = fy - a.y, dz = fz - a.z;
+        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        const float thr = a.w * prm.beta2f;
+        bool near = r2 <= thr;
+        if (in_guard_band(r2, thr, sigma)) {
+          const SoupNodeD* rd = prm.nd + node;
+          near = open_test64(qx, qy, qz, rd->P[0], rd->P[1], rd->P[2], rd->maxP2, prm.beta2d);
+          if (kStats) ++c.recheck;
+        }
+        if (!near) {
+          if (kStats) ++c.far;
+          const float om = far_field<float>(load_far(r), dx, dy, dz, r2, prm.order);
+          if (isfinite(om)) {
+            acc += om;
+            resume = leaf ? node + 1 : link;
+          } else {
+            near = true;
+          }
+        }
+        if (near) {
+          if (leaf) {
+            const int slot = ~link;
+            const float rad = sqrtf(a.w) + prm.eps;
+            if (r2 <= rad * rad * 1.0001f) {
+              if (kStats) ++c.exact64;
+              want64 = true;
+              slot64 = slot;
+            } else {
+              if (kStats) ++c.exact32;
+              const float4 t0 = __ldg(&prm.tf[(int64_t)slot * 3]);
+              const float4 t1 = __ldg(&prm.tf[(int64_t)slot * 3 + 1]);
+              const float4 t2 = __ldg(&prm.tf[(int64_t)slot * 3 + 2]);
+              acc += tri_solid_angle<float>(t0.x - fx, t0.y - fy, t0.z - fz, t0.w - fx, t1.x - fy,
+                                            t1.y - fz, t1.z - fx, t1.w - fy, t2.x - fz);
+            }
+            resume = node + 1;
+          } else {
+            open = true;
+          }
+        }
+      }
+    }
+    const unsigned m64 = __ballot_sync(full, want64);
+    if (m64) {
+      const int k = __popc(m64);
+      if (nqueued + k > 32) {
+        flush_near64(prm.td, nq, nqueued, qx, qy, qz, acc64);
+        nqueued = 0;
+      }
+      if (want64) nq.e[nqueued + __popc(m64 & lt_mask)] = make_int2(slot64, lane);
+      nqueued += k;
+    }
+    if (__any_sync(full, open))
+      node = node + 1;
+    else
+      node = __reduce_min_sync(full, resume);
+  }
+  if (nqueued) flush_near64(prm.td, nq, nqueued, qx, qy, qz, acc64);
+}
+
+// Winding number from the two parts of walk_mixed.
+__device__ __forceinline__ double mixed_result(float acc, double acc64) {
+  return acc64 != 0.0 ? ((double)acc + acc64) * kInv4Pi : (double)(acc * kInv4PiF);
+}
+
+// Plain FP64 warp-coherent walk (same calling rule as walk_mixed); returns
+// the solid-angle sum.
+__device__ __forceinline__ double walk_fp64(const EvalParams& prm, bool valid, double qx,
+                                            double qy, double qz) {
+  double acc = 0.0;
+  int resume = valid ? 0 : 0x7fffffff;
+  int node = 0;
+  const unsigned full = 0xffffffffu;
+  while (node < prm.nnodes) {
+    const SoupNodeD* r = prm.nd + node;
+    bool open = false;
+    if (node >= resume) {
+      const long long link = r->link;
+      const bool leaf = link < 0;
+      if (node == 0 && !leaf) {
+        open = true;
+      } else {
+        bool near = open_test64(qx, qy, qz, r->P[0], r->P[1], r->P[2], r->maxP2, prm.beta2d);
+        const double dx = qx - r->P[0], dy = qy - r->P[1], dz = qz - r->P[2];
+        const double r2 = dx * dx + dy * dy + dz * dz;
+        if (!near) {
+          const double om = far_field<double>(load_far(r), dx, dy, dz, r2, prm.order);
+          if (isfinite(om)) {
+            acc += om;
+            resume = leaf ? node + 1 : (int)link;
+          } else {
+            near = true;
+          }
+        }
+        if (near) {
+          if (leaf) {
+            const double* t = prm.td + (int64_t)(~link) * 9;
+            acc += tri_solid_angle<double>(t[0] - qx, t[1] - qy, t[2] - qz, t[3] - qx, t[4] - qy,
+                                           t[5] - qz, t[6] - qx, t[7] - qy, t[8] - qz);
+            resume = node + 1;
+          } else {
+            open = true;
+          }
+        }
+      }
+    }
+    if (__any_sync(full, open))
+      node = node + 1;
+    else
+      node = __reduce_min_sync(full, resume);
+  }
+  return acc;
+}
+
+// Plain FP64 walk of one query by one thread, no warp cooperation (for
+// sparse re-evaluation lists whose lanes may belong to different meshes).
+// Visits the same nodes and adds the same terms, in the same order, as
+// walk_fp64 does for that query.
+__device__ inline double walk_fp64_lane(const EvalParams& prm, double qx, double qy, double qz) {
+  double acc = 0.0;
+  int node = 0;
+  while (node < prm.nnodes) {
+    const SoupNodeD* r = prm.nd + node;
+    const long long link = r->link;
+    const bool leaf = link < 0;
+    if (node == 0 && !leaf) {
+      ++node;
+      continue;
+    }
+    bool near = open_test64(qx, qy, qz, r->P[0], r->P[1], r->P[2], r->maxP2, prm.beta2d);
+    const double dx = qx - r->P[0], dy = qy - r->P[1], dz = qz - r->P[2];
+    const double r2 = dx * dx + dy * dy + dz * dz;
+    if (!near) {
+      const double om = far_field<double>(load_far(r), dx, dy, dz, r2, prm.order);
+      if (isfinite(om)) {
+        acc += om;
+        node = leaf ? node + 1 : (int)link;
+        continue;
+      }
+    }
+    if (leaf) {
+      const double* t = prm.td + (int64_t)(~link) * 9;
+      acc += tri_solid_angle<double>(t[0] - qx, t[1] - qy, t[2] - qz, t[3] - qx, t[4] - qy,
+                                     t[5] - qz, t[6] - qx, t[7] - qy, t[8] - qz);
+    }
+    ++node;
+  }
+  return acc;
+}
+
+}  // namespace soupwalk
+}  // namespace gwn

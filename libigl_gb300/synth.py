@@ -87,8 +87,16 @@ def geodesic_sphere(nu: int):
     allP = P.reshape(-1, 3)
     allF = (tris[None, :, :] + (np.arange(20) * npts)[:, None, None]).reshape(-1, 3)
     key = np.round(allP * 1e9).astype(np.int64)
-    _, first, inv = np.unique(key, axis=0, return_index=True, return_inverse=True)
-    inv = inv.reshape(-1)
+    # unique rows in lexicographic order (first occurrence kept), as
+    # np.unique(key, axis=0) orders them, via a stable numeric lexsort
+    order = np.lexsort((key[:, 2], key[:, 1], key[:, 0]))
+    ks = key[order]
+    new_grp = np.ones(ks.shape[0], bool)
+    new_grp[1:] = np.any(ks[1:] != ks[:-1], axis=1)
+    gid = np.cumsum(new_grp) - 1
+    first = order[new_grp]
+    inv = np.empty(key.shape[0], np.int64)
+    inv[order] = gid
     V = allP[first]
     V /= np.linalg.norm(V, axis=1, keepdims=True)
     F = inv[allF]
@@ -143,6 +151,9 @@ def delete_random_faces(F, rng, frac: float):
 
 
 def face_adjacency(F):
+    """Edge-adjacent faces in CSR form (offsets, neighbours); each face's
+    neighbours in the order the edge pairs are found, as lists of the same
+    order would hold them."""
     e = np.concatenate([F[:, [0, 1]], F[:, [1, 2]], F[:, [2, 0]]]).astype(np.int64)
     fid = np.tile(np.arange(F.shape[0]), 3)
     e.sort(axis=1)
@@ -151,16 +162,19 @@ def face_adjacency(F):
     ks, fs = key[order], fid[order]
     same = ks[1:] == ks[:-1]
     a, b = fs[:-1][same], fs[1:][same]
-    nbr = [[] for _ in range(F.shape[0])]
-    for x, y in zip(a.tolist(), b.tolist()):
-        nbr[x].append(y)
-        nbr[y].append(x)
-    return nbr
+    # pair k appends b to a's list and a to b's list: sort the (owner, k)
+    # entries stably by owner to get each list in pair order
+    owner = np.stack([a, b], 1).reshape(-1)
+    other = np.stack([b, a], 1).reshape(-1)
+    srt = np.argsort(owner, kind="stable")
+    off = np.zeros(F.shape[0] + 1, np.int64)
+    np.add.at(off, owner + 1, 1)
+    return np.cumsum(off), other[srt]
 
 
 def delete_patch(F, rng, nfaces: int):
     """Remove one connected patch of `nfaces` faces grown by BFS from a seeded face."""
-    nbr = face_adjacency(F)
+    off, nb = face_adjacency(F)
     start = int(rng.integers(F.shape[0]))
     seen = {start}
     order = [start]
@@ -168,7 +182,7 @@ def delete_patch(F, rng, nfaces: int):
     while len(order) < nfaces and head < len(order):
         f = order[head]
         head += 1
-        for g in nbr[f]:
+        for g in nb[off[f]:off[f + 1]].tolist():
             if g not in seen and len(order) < nfaces:
                 seen.add(g)
                 order.append(g)
