@@ -401,12 +401,71 @@ __device__ __forceinline__ void read_q(const QT* Q, const int32_t* perm, const i
   z = (double)Q[qi * 3 + 2];
 }
 
+// Per-warp queue of FP64 near-field terms of the mixed walk: code >= 0 is a
+// point slot (exact dipole term), code < 0 is ~node (the node's expansion in
+// FP64).  Lanes append the terms they need and the warp evaluates up to 32
+// queued terms at once, one per lane, so each FP64 instruction serves the
+// whole warp; each lane still adds its own terms in walk order.
+struct CloudNearQueue {
+  int2 e[32];
+};
+
+__device__ __forceinline__ void flush_cloud64(const CloudEvalParams& prm,
+                                              const CloudNearQueue& q, int n, double qx,
+                                              double qy, double qz, double& acc64) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  __syncwarp();
+  int2 e = make_int2(0, lane);
+  if (lane < n) e = q.e[lane];
+  const double ox = __shfl_sync(full, qx, e.y), oy = __shfl_sync(full, qy, e.y),
+               oz = __shfl_sync(full, qz, e.y);
+  double v = 0.0;
+  if (lane < n) {
+    if (e.x >= 0) {
+      const double* pd = prm.pd + (int64_t)e.x * 6;
+      v = dipole64(pd[0] - ox, pd[1] - oy, pd[2] - oz, pd[3], pd[4], pd[5]);
+    } else {
+      const CloudNodeD* rd = prm.nd + ~e.x;
+      const double lx = __dsub_rn(rd->cm[0], ox), ly = __dsub_rn(rd->cm[1], oy),
+                   lz = __dsub_rn(rd->cm[2], oz);
+      v = expansion<double>(rd->ec, lx, ly, lz, sqrt(lx * lx + ly * ly + lz * lz),
+                            prm.num_terms);
+    }
+  }
+  for (int k = 0; k < n; ++k) {
+    const double vk = __shfl_sync(full, v, k);
+    const int ok = __shfl_sync(full, e.y, k);
+    if (ok == lane) acc64 += vk;
+  }
+  __syncwarp();
+}
+
+__device__ __forceinline__ void queue_cloud64(const CloudEvalParams& prm, CloudNearQueue& q,
+                                              int& nqueued, bool want, int code, double qx,
+                                              double qy, double qz, double& acc64) {
+  const unsigned full = 0xffffffffu;
+  const unsigned m = __ballot_sync(full, want);
+  if (!m) return;
+  const int k = __popc(m);
+  if (nqueued + k > 32) {
+    flush_cloud64(prm, q, nqueued, qx, qy, qz, acc64);
+    nqueued = 0;
+  }
+  const int lane = threadIdx.x & 31;
+  if (want) q.e[nqueued + __popc(m & ((1u << lane) - 1u))] = make_int2(code, lane);
+  nqueued += k;
+}
+
 template <typename QT, typename WT>
 __global__ void __launch_bounds__(128) cloud_eval_mixed_kernel(CloudEvalParams prm, const QT* __restrict__ Q,
                                                                const int32_t* __restrict__ perm,
                                                                int64_t nQ, WT* __restrict__ W,
                                                                int32_t* __restrict__ refine_list,
                                                                unsigned* __restrict__ refine_count) {
+  __shared__ CloudNearQueue near_q[4];
+  CloudNearQueue& nq = near_q[threadIdx.x >> 5];
+  int nqueued = 0;  // warp-uniform
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const bool valid = i < nQ;
   int64_t qi = 0;
@@ -423,28 +482,32 @@ __global__ void __launch_bounds__(128) cloud_eval_mixed_kernel(CloudEvalParams p
   while (node < prm.nnodes) {
     const CloudNodeF* r = prm.nf + node;
     const int4 l = __ldg(&r->l);
+    const bool visit = node >= resume;
     bool open = false;
-    if (node >= resume) {
-      const bool leaf = l.w != 0;
-      if (leaf) {
-        for (int j = 0; j < l.z; ++j) {
-          const int64_t slot = (int64_t)l.y + j;
+    if (l.w != 0) {  // leaf (the node, hence the branch, is warp-uniform)
+      for (int j = 0; j < l.z; ++j) {
+        const int64_t slot = (int64_t)l.y + j;
+        bool want = false;
+        if (visit) {
           const float4 p = __ldg(&prm.pf[slot * 2]);
           const float lx = p.x - fx, ly = p.y - fy, lz = p.z - fz;
           const float r2 = fmaf(lz, lz, fmaf(ly, ly, lx * lx));
           if (r2 <= p.w) {
-            const double* pd = prm.pd + slot * 6;
-            acc64 += dipole64(pd[0] - qx, pd[1] - qy, pd[2] - qz, pd[3], pd[4], pd[5]);
+            want = true;
           } else {
             const float4 an = __ldg(&prm.pf[slot * 2 + 1]);
             const float rn = sqrtf(r2);
             acc += fmaf(lx, an.x, fmaf(ly, an.y, lz * an.z)) / (kPi4F * (r2 * rn));
           }
         }
-        resume = l.x;
-      } else if (node == 0) {
-        open = true;
-      } else {
+        queue_cloud64(prm, nq, nqueued, want, (int)slot, qx, qy, qz, acc64);
+      }
+      if (visit) resume = l.x;
+    } else if (node == 0) {
+      open = visit;
+    } else {
+      bool want = false;
+      if (visit) {
         const float4 a = __ldg(&r->a);
         const float dx = a.x - fx, dy = a.y - fy, dz = a.z - fz;
         const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
@@ -458,11 +521,7 @@ __global__ void __launch_bounds__(128) cloud_eval_mixed_kernel(CloudEvalParams p
         if (far) {
           const float rn2 = __ldg(&r->e[9]).w;
           if (r2 <= rn2) {  // strong expansion close to the query: FP64
-            const CloudNodeD* rd = prm.nd + node;
-            const double lx = __dsub_rn(rd->cm[0], qx), ly = __dsub_rn(rd->cm[1], qy),
-                         lz = __dsub_rn(rd->cm[2], qz);
-            acc64 += expansion<double>(rd->ec, lx, ly, lz, sqrt(lx * lx + ly * ly + lz * lz),
-                                       prm.num_terms);
+            want = true;
           } else {
             float ec[40];
 #pragma unroll
@@ -480,12 +539,14 @@ __global__ void __launch_bounds__(128) cloud_eval_mixed_kernel(CloudEvalParams p
           open = true;
         }
       }
+      queue_cloud64(prm, nq, nqueued, want, ~node, qx, qy, qz, acc64);
     }
     if (__any_sync(full, open))
       node = node + 1;
     else
       node = __reduce_min_sync(full, resume);
   }
+  if (nqueued) flush_cloud64(prm, nq, nqueued, qx, qy, qz, acc64);
   if (!valid) return;
   const double w = acc64 != 0.0 ? (double)acc + acc64 : (double)acc;
   W[qi] = (WT)w;

@@ -260,7 +260,34 @@ __global__ void tile_meta_kernel(const TriF* __restrict__ tris, int ntiles,
 struct Smem3 {
   TriF tiles[kStages][kTile];
   uint64_t bar[kStages];
+  int2 near_q[kThreads / 32][32];  // per-warp queue of (triangle, lane) near pairs
 };
+
+// Evaluate the n queued near pairs of this warp in FP64, one per lane, so each
+// FP64 instruction serves the whole warp instead of the few lanes that share
+// a triangle; every lane then adds its own terms in queue (= triangle) order.
+__device__ __forceinline__ void flush_near_pairs(const double* __restrict__ tris64,
+                                                 const int2* q, int n, double qx, double qy,
+                                                 double qz, double& near_acc) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  __syncwarp();
+  int2 e = make_int2(0, lane);
+  if (lane < n) e = q[lane];
+  const double ox = __shfl_sync(full, qx, e.y), oy = __shfl_sync(full, qy, e.y),
+               oz = __shfl_sync(full, qz, e.y);
+  double v = 0.0;
+  if (lane < n) {
+    const double* g = tris64 + (int64_t)e.x * 9;
+    v = vos_term64(g, g + 3, g + 6, ox, oy, oz);
+  }
+  for (int k = 0; k < n; ++k) {
+    const double vk = __shfl_sync(full, v, k);
+    const int ok = __shfl_sync(full, e.y, k);
+    if (ok == lane) near_acc += vk;
+  }
+  __syncwarp();
+}
 
 template <typename QT, typename WT>
 __global__ void __launch_bounds__(kThreads) exact3_mixed_kernel(
@@ -293,6 +320,9 @@ __global__ void __launch_bounds__(kThreads) exact3_mixed_kernel(
   bool any_near = false;
   bool ok = true;
   int stop_tile = 0;
+  int nqueued = 0;  // warp-uniform length of this warp's near-pair queue
+  int2* nq = sm.near_q[tid >> 5];
+  const unsigned lane_lt = (1u << (tid & 31)) - 1u;
   for (int t = 0; t < ntiles; ++t) {
     const int s = t % kStages;
     const uint32_t parity = (uint32_t)((t / kStages) & 1);
@@ -313,12 +343,19 @@ __global__ void __launch_bounds__(kThreads) exact3_mixed_kernel(
         const TriF tr = tile[k];
         const float ex = tr.r3.x - fx, ey = tr.r3.y - fy, ez = tr.r3.z - fz;
         const bool near = valid && fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < tr.r3.w;
-        if (near) {
-          const double* g = tris64 + ((int64_t)t * kTile + k) * 9;
-          near_acc += vos_term64(g, g + 3, g + 6, qx, qy, qz);
-          any_near = true;
-        } else {
-          ssum += vos_term32(tr, fx, fy, fz);
+        if (!near) ssum += vos_term32(tr, fx, fy, fz);
+        // near pairs go to the warp's queue and are evaluated in FP64 32 at a
+        // time, one per lane (flush_near_pairs)
+        const unsigned m = __ballot_sync(0xffffffffu, near);
+        if (m) {
+          const int c = __popc(m);
+          if (nqueued + c > 32) {
+            flush_near_pairs(tris64, nq, nqueued, qx, qy, qz, near_acc);
+            nqueued = 0;
+          }
+          if (near) nq[nqueued + __popc(m & lane_lt)] = make_int2(t * kTile + k, tid & 31);
+          nqueued += c;
+          any_near |= near;
         }
       }
     } else {
@@ -343,6 +380,7 @@ __global__ void __launch_bounds__(kThreads) exact3_mixed_kernel(
     }
     return;
   }
+  if (nqueued) flush_near_pairs(tris64, nq, nqueued, qx, qy, qz, near_acc);
   if (!valid) return;
   double w;
   if (any_near)

@@ -457,7 +457,7 @@ __device__ __forceinline__ void read_query(const QT* Q, const int32_t* perm, con
 // an instrumented copy that counts its work into `stats` (see
 // gwn_soup_walk_stats); the timed kernel is the kStats = false instance.
 template <typename QT, typename WT, bool kStats = false>
-__global__ void __launch_bounds__(128) soup_eval_mixed_kernel(EvalParams prm, const QT* __restrict__ Q,
+__global__ void __launch_bounds__(128, 8) soup_eval_mixed_kernel(EvalParams prm, const QT* __restrict__ Q,
                                                               const int32_t* __restrict__ perm,
                                                               int64_t nQ, WT* __restrict__ W,
                                                               int32_t* __restrict__ refine_list,
