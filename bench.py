@@ -472,16 +472,23 @@ def run_served_line(args):
     served_q = int(nq_of.sum())
 
     def saturated(precision, n):
+        a = S.stats()
         t = time.perf_counter()
         hs = [S.submit(ids[int(mesh_of[i])],
                        pools[int(mesh_of[i])][off_of[i]:off_of[i] + nq_of[i]], 2.0, precision)
               for i in range(n)]
         for h in hs:
             h.wait()
-        return int(nq_of[:n].sum()) / (time.perf_counter() - t)
+        wall = time.perf_counter() - t
+        b = S.stats()
+        return {"qps": int(nq_of[:n].sum()) / wall, "wall_s": wall,
+                "walk_gpu_ms": b["walk_gpu_ms"] - a["walk_gpu_ms"],
+                "batch_gpu_ms": b["batch_gpu_ms"] - a["batch_gpu_ms"],
+                "batches": b["batches"] - a["batches"]}
     nsat = min(1000, nreq)
-    sat_mixed = saturated("mixed", nsat)
-    sat_fp64 = saturated("fp64", nsat)
+    sat_m = saturated("mixed", nsat)
+    sat_d = saturated("fp64", nsat)
+    sat_mixed, sat_fp64 = sat_m["qps"], sat_d["qps"]
     st2 = S.stats()
     S.close()
     walk_ms = st1["walk_gpu_ms"] - st0["walk_gpu_ms"]
@@ -505,7 +512,7 @@ def run_served_line(args):
                          "admission_s": warm_s},
             "saturated_first_1000": {"mixed_qps": sat_mixed, "fp64_qps": sat_fp64,
                                      "mixed_over_fp64": sat_mixed / sat_fp64,
-                                     "batches": st2["batches"] - st1["batches"]},
+                                     "mixed": sat_m, "fp64": sat_d},
             "mesh_generation_s": gen_s, "gpu_launches": launches,
             "kernels_per_batch": st1["kernels_per_batch"]}
     print(json.dumps(line), flush=True)

@@ -44,6 +44,7 @@
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <functional>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -247,6 +248,70 @@ __global__ void __launch_bounds__(256) serve_out_kernel(const ServeHeader* __res
   }
 }
 
+// A small fork-join pool for the host-side copies of a batch (queries into
+// the pinned stage, results out to the callers' arrays): run(n, f) calls
+// f(0..n-1) on the pool threads and the calling thread, and returns when all
+// calls have returned.
+class CopyPool {
+ public:
+  explicit CopyPool(int threads) {
+    for (int i = 0; i < threads; ++i) th_.emplace_back([this] { loop(); });
+  }
+  ~CopyPool() {
+    {
+      std::lock_guard<std::mutex> g(mu_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    for (auto& t : th_) t.join();
+  }
+  void run(int n, const std::function<void(int)>& f) {
+    if (n <= 0) return;
+    std::unique_lock<std::mutex> lk(mu_);
+    job_ = &f;
+    njobs_ = n;
+    next_ = 0;
+    finished_ = 0;
+    ++gen_;
+    cv_.notify_all();
+    work(lk);
+    done_.wait(lk, [&] { return finished_ == njobs_; });
+    job_ = nullptr;
+  }
+
+ private:
+  void work(std::unique_lock<std::mutex>& lk) {
+    while (job_ && next_ < njobs_) {
+      const int i = next_++;
+      const std::function<void(int)>* f = job_;
+      lk.unlock();
+      (*f)(i);
+      lk.lock();
+      if (++finished_ == njobs_) done_.notify_all();
+    }
+  }
+  void loop() {
+    std::unique_lock<std::mutex> lk(mu_);
+    uint64_t seen = 0;
+    for (;;) {
+      cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
+      if (stop_) return;
+      seen = gen_;
+      work(lk);
+    }
+  }
+  std::vector<std::thread> th_;
+  std::mutex mu_;
+  std::condition_variable cv_, done_;
+  const std::function<void(int)>* job_ = nullptr;
+  int njobs_ = 0, next_ = 0, finished_ = 0;
+  uint64_t gen_ = 0;
+  bool stop_ = false;
+};
+
+// Pieces of at most kCopyPiece queries per copy task.
+constexpr int64_t kCopyPiece = 1 << 16;
+
 double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch())
       .count();
@@ -337,6 +402,8 @@ struct gwn_server {
 
   gwn_server_stats stats{};
   int64_t resident_bytes = 0;
+  std::unique_ptr<CopyPool> pool;
+  std::vector<std::pair<int, int64_t>> pieces;  // (request, first query) of the batch being copied
 
   ~gwn_server();
   void capture(SrvSlot& s);
@@ -542,12 +609,22 @@ bool gwn_server::form_and_launch(SrvSlot& s, std::unique_lock<std::mutex>& lk) {
     d.precision = r->precision;
     hr[i] = d;
     const size_t qb = (size_t)r->nq * 3 * dtype_size(r->q_dtype);
-    std::memcpy(stage + boff, r->Q, qb);
     boff += (int64_t)((qb + 15) / 16 * 16);
     s.out_off[i] = dense;
     dense += r->nq;
     aoff += (int32_t)((r->nq + 31) / 32 * 32);
   }
+  pieces.clear();
+  for (size_t i = 0; i < take.size(); ++i)
+    for (int64_t k = 0; k < take[i]->nq; k += kCopyPiece) pieces.emplace_back((int)i, k);
+  pool->run((int)pieces.size(), [&](int t) {
+    const SrvReq* r = take[(size_t)pieces[t].first];
+    const ServeReq& d = hr[pieces[t].first];
+    const int64_t k0 = pieces[t].second, n = std::min(kCopyPiece, r->nq - k0);
+    const size_t qs = 3 * dtype_size(r->q_dtype);
+    std::memcpy(stage + d.q_byte_off + k0 * qs,
+                static_cast<const unsigned char*>(r->Q) + k0 * qs, (size_t)n * qs);
+  });
   hh->nreq = (uint32_t)take.size();
   hh->n_aligned = (uint32_t)aoff;
   hh->nq_total = (uint32_t)dense;
@@ -583,17 +660,22 @@ void gwn_server::finish(SrvSlot& s, std::unique_lock<std::mutex>& lk) {
   cudaEventElapsedTime(&ms, s.ev_start, s.ev_done);
   cudaEventElapsedTime(&wms, s.ev_walk0, s.ev_walk1);
   int64_t nq = 0;
+  pieces.clear();
   for (size_t i = 0; i < s.reqs.size(); ++i) {
-    SrvReq* r = s.reqs[i];
-    const double* src = hout + s.out_off[i];
-    if (r->w_dtype == GWN_F64) {
-      std::memcpy(r->W, src, (size_t)r->nq * sizeof(double));
-    } else {
-      float* w = static_cast<float*>(r->W);
-      for (int64_t k = 0; k < r->nq; ++k) w[k] = (float)src[k];
-    }
-    nq += r->nq;
+    for (int64_t k = 0; k < s.reqs[i]->nq; k += kCopyPiece) pieces.emplace_back((int)i, k);
+    nq += s.reqs[i]->nq;
   }
+  pool->run((int)pieces.size(), [&](int t) {
+    SrvReq* r = s.reqs[(size_t)pieces[t].first];
+    const int64_t k0 = pieces[t].second, n = std::min(kCopyPiece, r->nq - k0);
+    const double* src = hout + s.out_off[(size_t)pieces[t].first] + k0;
+    if (r->w_dtype == GWN_F64) {
+      std::memcpy(static_cast<double*>(r->W) + k0, src, (size_t)n * sizeof(double));
+    } else {
+      float* w = static_cast<float*>(r->W) + k0;
+      for (int64_t k = 0; k < n; ++k) w[k] = (float)src[k];
+    }
+  });
   lk.lock();
   for (SrvReq* r : s.reqs) {
     r->mesh->inflight--;
@@ -698,6 +780,10 @@ int gwn_server_create(int64_t hbm_budget_bytes, int64_t max_batch_queries, int32
     S->cap = max_batch_queries / 32 * 32;
     S->stats.budget_bytes = hbm_budget_bytes;
     GWN_CUDA(cudaStreamCreateWithFlags(&S->build_st, cudaStreamNonBlocking));
+    {
+      const unsigned hc = std::thread::hardware_concurrency();
+      S->pool.reset(new CopyPool((int)std::min(7u, std::max(1u, hc / 2))));
+    }
     int64_t counts_n = 0, scan_n = 0;
     radix_sort_scratch_elems(S->cap, &counts_n, &scan_n);
     for (int i = 0; i < slots; ++i) {
