@@ -1,6 +1,8 @@
 """CPU tests of the oracle itself: pinned against the reference's own golden
 vectors and known answers (tests/include/igl/fast_winding_number.cpp:17-53,
 tests/include/igl/signed_distance.cpp:4-42) and against analytic cases."""
+import os
+
 import numpy as np
 import pytest
 
@@ -130,3 +132,37 @@ def test_soup_port_reproduces_reference_fixtures_bit_for_bit():
         V, F, Q, Wref = z[name + "/V"], z[name + "/F"], z[name + "/Q"], z[name + "/W_ref"]
         W = O.SoupPort(V, F, order=2).eval(Q, 2.0)
         assert np.array_equal(W, Wref), name
+
+
+def test_pair_atan2_polynomial_in_fp32():
+    """The FP32 atan2 of the exact kernel's pair terms (exact.cu,
+    atan2_pairs): its coefficients, evaluated in float32 with the kernel's
+    octant reduction, stay within a few ulp of atan2 everywhere."""
+    import re
+    src = open(os.path.join(os.path.dirname(__file__), "..", "libigl_gb300", "csrc",
+                            "exact.cu")).read()
+    body = src[src.index("float atan2_pairs("):]
+    body = body[:body.index("\n}\n")]
+    coef = [np.float32(float(x)) for x in
+            re.findall(r"(?:float p = |p = fmaf\(p, s, )(-?[0-9.]+(?:e[-+][0-9]+)?)f", body)]
+    assert len(coef) == 9  # degree 8, highest first
+    f32 = np.float32
+    rng = np.random.default_rng(0)
+    ang = rng.uniform(-np.pi, np.pi, 400_000)
+    rad = 10.0 ** rng.uniform(-6, 6, ang.size)
+    y = (rad * np.sin(ang)).astype(f32)
+    x = (rad * np.cos(ang)).astype(f32)
+    ax, ay = np.abs(x), np.abs(y)
+    mx, mn = np.maximum(ax, ay), np.minimum(ax, ay)
+    t = (mn / mx).astype(f32)
+    s = (t * t).astype(f32)
+    p = coef[0]
+    for c in coef[1:]:
+        p = (p * s + c).astype(f32)
+    r = (t * p).astype(f32)
+    r = np.where(ay > ax, (f32(np.pi / 2) - r).astype(f32), r)
+    r = np.where(x < 0, (f32(np.pi) - r).astype(f32), r)
+    r = np.copysign(r, y)
+    ref = np.arctan2(y.astype(np.float64), x.astype(np.float64))
+    err = np.abs(r - ref)
+    assert np.all(err <= 4 * np.spacing(np.abs(ref).astype(f32)) + 1e-12), err.max()
