@@ -56,7 +56,8 @@ def parse():
                     help="target CPU work for the CPU baseline sample")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
-    ap.add_argument("--workload", choices=["soup", "exact", "cloud", "precision", "served"],
+    ap.add_argument("--workload", choices=["soup", "exact", "cloud", "precision", "served",
+                                           "signed_distance"],
                     default="soup",
                     help="soup = the headline line; the others are extra measurement lines")
     ap.add_argument("--served-seconds", type=float, default=4.0,
@@ -518,6 +519,79 @@ def run_served_line(args):
     print(json.dumps(line), flush=True)
 
 
+def run_signed_distance_line(args):
+    """igl::signed_distance with the fast-winding-number sign on the C2 mesh
+    (1,297,489 triangles), 1M float64 queries of the C2 distribution.
+    value = queries/s of the whole call on device-resident arrays (the tree
+    is built inside every call, as the reference builds its AABB and soup
+    tree); e2e = the same call from host arrays; closest_only_qps = closest
+    triangles on a built tree; CPU baseline = the AABB restatement
+    (oracle/aabb.cpp) + the reference's soup winding number on the host
+    cores, on a 200k-query sample, trees built apart."""
+    import torch
+    import libigl_gb300 as G
+    from libigl_gb300 import synth
+    from oracle import oracle as O
+    V, F = synth.soup_mesh(seed=1, subdiv=8)
+    Q = synth.soup_queries(V, F, seed=2, nq=1_000_000)
+    dQ, dV, dF = (torch.from_numpy(x).cuda() for x in (Q, V, F))
+    stream = torch.cuda.current_stream()
+    out = {}
+    FWN = G.SIGNED_DISTANCE_TYPE_FAST_WINDING_NUMBER
+
+    def step():
+        out["S"], out["I"], out["C"] = G.signed_distance(dQ, dV, dF, FWN)
+    total, per = timed_steps(step, args.steps, args.warmup, stream)
+    launches = G.launch_count_of(step)
+    bvh = G.FastWindingNumberBVH(dV, dF, 2)
+    walk = {}
+
+    def closest_only():
+        walk["D"] = bvh.squared_distance(dQ)
+    tc, _ = timed_steps(closest_only, args.steps, args.warmup, stream)
+    t0 = time.perf_counter()
+    S1, I1, C1 = G.signed_distance(Q, V, F, FWN)
+    one_shot = time.perf_counter() - t0
+    # CPU: AABB restatement + reference soup winding number, on a sample
+    ns = 200_000
+    sample = Q[:ns]
+    t0 = time.perf_counter()
+    tree = O.AABB(V, F)
+    port = O.SoupPort(V.astype(np.float32).astype(np.float64), F, order=2)
+    cpu_build = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    Dc, Ic, Cc = tree.squared_distance(sample)
+    wc = port.eval(sample, 2.0)
+    cpu_s = time.perf_counter() - t0
+    D = walk["D"][0].cpu().numpy()[:ns]
+    Sg = out["S"].cpu().numpy()[:ns]
+    Sc = (1.0 - 2.0 * np.abs(wc)) * np.sqrt(Dc)
+    d_err = np.abs(D - Dc) / np.maximum(Dc, 1e-300)
+    line = {"metric": "signed distance queries/s (closest triangle FP64 + winding-number sign)",
+            "value": Q.shape[0] * args.steps / (total / 1e3), "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": "signed_distance_fwn_icosphere8_sh_1pct_holes_1Mq",
+                       "triangles": int(F.shape[0]), "queries": int(Q.shape[0]),
+                       "sign": "FAST_WINDING_NUMBER (order 2, accuracy 2, mixed)"},
+            "closest_only_qps": Q.shape[0] * args.steps / (tc / 1e3),
+            "e2e": {"value": Q.shape[0] / one_shot, "unit": UNIT,
+                    "h2d_bytes_per_step": int(Q.nbytes + V.nbytes + F.nbytes),
+                    "d2h_bytes_per_step": int(Q.shape[0] * (8 + 4 + 24))},
+            "accuracy": {"sqrD_max_rel_vs_cpu_aabb": float(d_err.max()),
+                         "S_max_abs_vs_cpu": float(np.abs(Sg - Sc).max()),
+                         "sign_mismatch": int(((Sg < 0) != (Sc < 0))[np.abs(wc - 0.5) > 0.05].sum()),
+                         "queries_compared": ns},
+            "gpu_launches": launches,
+            "cpu_baseline": {"value": ns / cpu_s, "unit": UNIT, "cores": O.num_threads(0),
+                             "kind": "port", "build_s": cpu_build,
+                             "sample": f"first {ns} queries: igl::AABB restatement "
+                                       "(oracle/aabb.cpp) + reference soup winding number "
+                                       "(oracle/soup_hdk.cpp), trees built apart"}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -529,7 +603,8 @@ def main():
         if args.workload != "served":  # served starts its generator pool first
             torch.cuda.set_device(local)
         {"exact": run_exact_line, "cloud": run_cloud_line, "precision": run_precision_study,
-         "served": run_served_line}[args.workload](args)
+         "served": run_served_line,
+         "signed_distance": run_signed_distance_line}[args.workload](args)
         return
     import torch
     import libigl_gb300 as G

@@ -201,6 +201,44 @@ int gwn_cloud_eval_arrays(const double* P, const double* N, const double* A, int
                           double beta, double* W, int precision);
 
 /* ------------------------------------------------------------------------
+ * Closest triangle and signed distance (the caller of the winding number
+ * that libigl builds on it).
+ *
+ * gwn_soup_squared_distance: igl::AABB<V,3>::squared_distance(V,F,P,sqrD,I,C)
+ * (include/igl/AABB.h:386-397, AABB.cpp:1135-1205) over the triangles of a
+ * soup handle: per query the smallest squared distance below up_sqr_d
+ * (up_sqr_d and I = -1 if none; pass INFINITY for no bound), the input index
+ * of that triangle and the closest point (#Q x 3 float64).  Non-finite
+ * queries give up_sqr_d and I = -1.
+ *
+ * gwn_signed_distance: igl::signed_distance(P,V,F,sign_type,lower_bound,
+ * upper_bound,S,I,C,N) (include/igl/signed_distance.h:61-71,
+ * signed_distance.cpp:20-137, 372-424) for 3-D triangles.  sign_type takes
+ * igl::SignedDistanceType's values; GWN_SD_PSEUDONORMAL is not implemented
+ * (GWN_ERR_INVALID_ARGUMENT).  The sign factor is 1 (UNSIGNED),
+ * 1 - 2 W with the exact winding number (WINDING_NUMBER, DEFAULT) or
+ * 1 - 2 |W| with the soup fast winding number, order 2, accuracy 2
+ * (FAST_WINDING_NUMBER); `precision` selects how that W is computed.
+ * Distances outside the bounds give S = NaN, I = #F + 1, C = 0; an empty F
+ * gives S = NaN, I = -1, C = NaN.  The defaults of the reference's
+ * bound-less overload are lower_bound = DBL_MIN, upper_bound = DBL_MAX.
+ * ---------------------------------------------------------------------- */
+enum {
+  GWN_SD_PSEUDONORMAL = 0,
+  GWN_SD_WINDING_NUMBER = 1,
+  GWN_SD_DEFAULT = 2,
+  GWN_SD_UNSIGNED = 3,
+  GWN_SD_FAST_WINDING_NUMBER = 4
+};
+int gwn_soup_squared_distance(const gwn_soup* soup, const void* Q, int q_dtype, int64_t nQ,
+                              double up_sqr_d, double* sqrD, int32_t* I, double* C, int mem,
+                              void* stream);
+int gwn_signed_distance(const double* P, int64_t nP, const double* V, int64_t nV,
+                        const int32_t* F, int64_t nF, int sign_type, double lower_bound,
+                        double upper_bound, double* S, int32_t* I, double* C, int precision,
+                        int mem, void* stream);
+
+/* ------------------------------------------------------------------------
  * Served evaluation (no counterpart in the reference: libigl evaluates one
  * mesh per call).  A server keeps triangle meshes resident on the device as
  * built soup trees and evaluates requests against them, each request being

@@ -33,7 +33,7 @@ __all__ = [
     "fast_winding_number_soup_precompute", "fast_winding_number_soup",
     "Octree", "octree", "CloudExpansion", "fast_winding_number_cloud_precompute",
     "fast_winding_number_cloud", "fast_winding_number_cloud_oneshot", "device_status",
-    "Server",
+    "Server", "signed_distance",
 ]
 
 _PREC = {"fp64": N.GWN_PLAIN_FP64, "plain": N.GWN_PLAIN_FP64, "mixed": N.GWN_MIXED}
@@ -204,6 +204,24 @@ class FastWindingNumberBVH:
                                          tri.ctypes.data_as(C.c_void_p)))
         links = nodes[:, 23].copy().view(np.int64)
         return nodes, links, tri
+
+    def squared_distance(self, Q, up_sqr_d: float = float("inf")):
+        """igl::AABB::squared_distance(V,F,Q,sqrD,I,C) over this mesh's
+        triangles: (sqrD, I, C) -- smallest squared distance (below
+        up_sqr_d), input triangle index (-1 if none) and closest point."""
+        L = N.load()
+        Qa = _Arg(Q)
+        if len(Qa.shape) != 2 or Qa.shape[1] != 3:
+            raise ValueError("Q must be #Q x 3")
+        n = Qa.shape[0]
+        D = _empty_like_mem(Qa.mem, (n,), np.float64, like=Qa)
+        I = _empty_like_mem(Qa.mem, (n,), np.int32, like=Qa)
+        Cp = _empty_like_mem(Qa.mem, (n, 3), np.float64, like=Qa)
+        stream = _stream_ptr() if Qa.mem == N.GWN_DEVICE else None
+        N.check(L.gwn_soup_squared_distance(self._h, Qa.ptr, Qa.code, n, C.c_double(up_sqr_d),
+                                            _ptr_of(D), _ptr_of(I), _ptr_of(Cp), Qa.mem,
+                                            stream))
+        return D, I, Cp
 
     def walk_stats(self, Q, accuracy_scale: float = 2.0) -> dict:
         """Work counters of one instrumented mixed evaluation of Q (float64)."""
@@ -420,6 +438,46 @@ def fast_winding_number_cloud_oneshot(P, Nrm, A, Q, order: int = 2, beta: float 
     finally:
         ce.close()
         ce.tree.close()
+
+
+# ------------------------------------------------------- signed distance --
+SIGNED_DISTANCE_TYPE_PSEUDONORMAL = 0
+SIGNED_DISTANCE_TYPE_WINDING_NUMBER = 1
+SIGNED_DISTANCE_TYPE_DEFAULT = 2
+SIGNED_DISTANCE_TYPE_UNSIGNED = 3
+SIGNED_DISTANCE_TYPE_FAST_WINDING_NUMBER = 4
+
+
+def signed_distance(P, V, F, sign_type=SIGNED_DISTANCE_TYPE_DEFAULT, lower_bound=None,
+                    upper_bound=None, precision=None):
+    """igl::signed_distance(P,V,F,sign_type,lower_bound,upper_bound,S,I,C,N)
+    (include/igl/signed_distance.h:61-71) for 3-D triangles: (S, I, C).
+
+    Bounds default to the reference's bound-less overload (DBL_MIN, DBL_MAX).
+    ``precision`` selects how the sign's winding number is computed; by
+    default plain FP64 for the exact winding number (as the reference) and
+    mixed precision for the fast winding number (the reference's is FP32).
+    Host arrays or CUDA torch tensors (all of one kind)."""
+    L = N.load()
+    Pa = _Arg(P, np.float64)
+    Va = _Arg(V, np.float64)
+    Fa = _Arg(F, np.int32, allowed=(np.int32,))
+    _same_mem(Pa, Va, Fa)
+    if len(Pa.shape) != 2 or Pa.shape[1] != 3 or Va.shape[1:] != (3,) or Fa.shape[1:] != (3,):
+        raise ValueError("P and V must be #P x 3 / #V x 3 and F #F x 3 (3-D triangles)")
+    if precision is None:
+        precision = "mixed" if sign_type == SIGNED_DISTANCE_TYPE_FAST_WINDING_NUMBER else "fp64"
+    lo = np.finfo(np.float64).tiny if lower_bound is None else float(lower_bound)
+    hi = np.finfo(np.float64).max if upper_bound is None else float(upper_bound)
+    n = Pa.shape[0]
+    S = _empty_like_mem(Pa.mem, (n,), np.float64, like=Pa)
+    I = _empty_like_mem(Pa.mem, (n,), np.int32, like=Pa)
+    Cp = _empty_like_mem(Pa.mem, (n, 3), np.float64, like=Pa)
+    stream = _stream_ptr() if Pa.mem == N.GWN_DEVICE else None
+    N.check(L.gwn_signed_distance(Pa.ptr, n, Va.ptr, Va.shape[0], Fa.ptr, Fa.shape[0],
+                                  int(sign_type), C.c_double(lo), C.c_double(hi), _ptr_of(S),
+                                  _ptr_of(I), _ptr_of(Cp), _prec(precision), Pa.mem, stream))
+    return S, I, Cp
 
 
 # ------------------------------------------------------------- profiling --

@@ -581,6 +581,67 @@ int gwn_profile_read(char* names, int names_cap, float* ms, int max_phases, int*
 unsigned long long gwn_launch_count(void) { return g_launches.load(); }
 
 
+int gwn_soup_squared_distance(const gwn_soup* soup, const void* Q, int q_dtype, int64_t nQ,
+                              double up_sqr_d, double* sqrD, int32_t* I, double* C, int mem,
+                              void* stream) {
+  return guarded("gwn_soup_squared_distance", [&] {
+    GWN_REQUIRE(soup != nullptr, "soup handle is null");
+    GWN_REQUIRE(nQ >= 0, "nQ must be non-negative");
+    GWN_REQUIRE(nQ == 0 || (Q && sqrD && I && C), "Q, sqrD, I and C must be non-null");
+    GWN_REQUIRE(nQ < (int64_t(1) << 31), "at most 2^31-1 queries per call");
+    check_dtype(q_dtype, "Q");
+    check_mem(mem);
+    ensure_device();
+    check_device_of(soup->impl.device);
+    cudaStream_t st = as_stream(stream);
+    StagedBytes dQ(Q, (size_t)nQ * 3 * dtype_size(q_dtype), mem, st);
+    Staged<double> dD(sqrD, (size_t)nQ, mem, st, false);
+    Staged<int32_t> dI(I, (size_t)nQ, mem, st, false);
+    Staged<double> dC(C, (size_t)nQ * 3, mem, st, false);
+    soup_squared_distance(soup->impl, dQ.dev, q_dtype, nQ, up_sqr_d, dD.dev, dI.dev, dC.dev, st);
+    if (mem == GWN_HOST && nQ) {
+      GWN_CUDA(cudaMemcpyAsync(sqrD, dD.dev, (size_t)nQ * 8, cudaMemcpyDeviceToHost, st));
+      GWN_CUDA(cudaMemcpyAsync(I, dI.dev, (size_t)nQ * 4, cudaMemcpyDeviceToHost, st));
+      GWN_CUDA(cudaMemcpyAsync(C, dC.dev, (size_t)nQ * 24, cudaMemcpyDeviceToHost, st));
+      GWN_CUDA(cudaStreamSynchronize(st));
+    }
+  });
+}
+
+int gwn_signed_distance(const double* P, int64_t nP, const double* V, int64_t nV,
+                        const int32_t* F, int64_t nF, int sign_type, double lower_bound,
+                        double upper_bound, double* S, int32_t* I, double* C, int precision,
+                        int mem, void* stream) {
+  return guarded("gwn_signed_distance", [&] {
+    GWN_REQUIRE(nP >= 0 && nV >= 0 && nF >= 0, "sizes must be non-negative");
+    GWN_REQUIRE(nP == 0 || (P && S && I && C), "P, S, I and C must be non-null");
+    GWN_REQUIRE(nF == 0 || (V && F), "V and F must be non-null");
+    GWN_REQUIRE(nP < (int64_t(1) << 31), "at most 2^31-1 queries per call");
+    GWN_REQUIRE(sign_type >= GWN_SD_PSEUDONORMAL && sign_type <= GWN_SD_FAST_WINDING_NUMBER,
+                "sign_type must be one of GWN_SD_*");
+    GWN_REQUIRE(sign_type != GWN_SD_PSEUDONORMAL,
+                "GWN_SD_PSEUDONORMAL is not implemented (use a winding-number sign)");
+    check_precision(precision);
+    check_mem(mem);
+    ensure_device();
+    cudaStream_t st = as_stream(stream);
+    Staged<double> dP(P, (size_t)nP * 3, mem, st);
+    Staged<double> dV(V, (size_t)nV * 3, mem, st);
+    Staged<int32_t> dF(F, (size_t)nF * 3, mem, st);
+    Staged<double> dS(S, (size_t)nP, mem, st, false);
+    Staged<int32_t> dI(I, (size_t)nP, mem, st, false);
+    Staged<double> dC(C, (size_t)nP * 3, mem, st, false);
+    signed_distance_run(dP.dev, nP, dV.dev, nV, dF.dev, nF, sign_type, lower_bound, upper_bound,
+                        dS.dev, dI.dev, dC.dev, precision, st);
+    if (mem == GWN_HOST && nP) {
+      GWN_CUDA(cudaMemcpyAsync(S, dS.dev, (size_t)nP * 8, cudaMemcpyDeviceToHost, st));
+      GWN_CUDA(cudaMemcpyAsync(I, dI.dev, (size_t)nP * 4, cudaMemcpyDeviceToHost, st));
+      GWN_CUDA(cudaMemcpyAsync(C, dC.dev, (size_t)nP * 24, cudaMemcpyDeviceToHost, st));
+      GWN_CUDA(cudaStreamSynchronize(st));
+    }
+  });
+}
+
 int gwn_winding_number_noalloc(const double* V, int64_t nV, const int32_t* F, int64_t nF,
                                const double* O, int64_t nO, double* W, unsigned int* dev_status,
                                void* stream) {

@@ -33,4 +33,11 @@ int64_t noalloc_max_triangles();
 void run_exact_noalloc(const double* V, int64_t nV, const int32_t* F, int64_t nF, const double* Q,
                        int64_t nQ, double* W, unsigned* dev_status, cudaStream_t st);
 
+// igl::signed_distance for 3-D triangles (distance.cu); device pointers;
+// synchronizes `st`.
+void signed_distance_run(const double* P, int64_t nP, const double* V, int64_t nV,
+                         const int32_t* F, int64_t nF, int sign_type, double lower_bound,
+                         double upper_bound, double* S, int32_t* I, double* C, int precision,
+                         cudaStream_t st);
+
 }  // namespace gwn

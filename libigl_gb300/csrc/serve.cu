@@ -416,10 +416,11 @@ struct gwn_server {
 };
 
 // A resident tree's device bytes, estimated before the first build from the
-// node and triangle records (2n-1 nodes of 96 + 192 bytes, 124 bytes per
-// triangle).
+// node and triangle records (2n-1 nodes of 96 + 192 + 32 bytes, 124 bytes
+// per triangle).
 static int64_t estimate_bytes(int64_t nF) {
-  return std::max<int64_t>(1, 2 * nF - 1) * (int64_t)(sizeof(SoupNodeF) + sizeof(SoupNodeD)) +
+  return std::max<int64_t>(1, 2 * nF - 1) *
+             (int64_t)(sizeof(SoupNodeF) + sizeof(SoupNodeD) + 2 * sizeof(float4)) +
          nF * (int64_t)(3 * sizeof(float4) + 9 * sizeof(double) + sizeof(int32_t));
 }
 

@@ -373,7 +373,8 @@ __global__ void bottom_up_kernel(const double* __restrict__ V, const int32_t* __
 __global__ void preorder_kernel(const int32_t* __restrict__ left,
                                 const int32_t* __restrict__ parent,
                                 const int32_t* __restrict__ size, int nnodes, int root,
-                                int32_t* __restrict__ pre, int32_t* __restrict__ depth) {
+                                int32_t* __restrict__ pre, int32_t* __restrict__ depth,
+                                int32_t* __restrict__ depth_max) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   if (x >= nnodes) return;
   int p = 0, dep = 0, cur = x;
@@ -386,6 +387,30 @@ __global__ void preorder_kernel(const int32_t* __restrict__ left,
   }
   pre[x] = p;
   depth[x] = dep;
+  atomicMax(depth_max, dep);
+}
+
+// Closest-point search nodes (see gwn_soup_impl::snode), one thread per
+// internal node.
+__global__ void search_nodes_kernel(const BuildM* __restrict__ M, const int32_t* __restrict__ left,
+                                    const int32_t* __restrict__ right, int n,
+                                    float4* __restrict__ snode) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n - 1) return;
+  const int l = left[i], r = right[i];
+  const int ref_l = l >= n - 1 ? ~(l - (n - 1)) : l;
+  const int ref_r = r >= n - 1 ? ~(r - (n - 1)) : r;
+  const BuildM& ml = M[l];
+  const BuildM& mr = M[r];
+  float4* o = snode + 4 * (int64_t)i;
+  o[0] = make_float4(__double2float_rd(ml.lo[0]), __double2float_rd(ml.lo[1]),
+                     __double2float_rd(ml.lo[2]), __int_as_float(ref_l));
+  o[1] = make_float4(__double2float_ru(ml.hi[0]), __double2float_ru(ml.hi[1]),
+                     __double2float_ru(ml.hi[2]), __int_as_float(ref_r));
+  o[2] = make_float4(__double2float_rd(mr.lo[0]), __double2float_rd(mr.lo[1]),
+                     __double2float_rd(mr.lo[2]), 0.f);
+  o[3] = make_float4(__double2float_ru(mr.hi[0]), __double2float_ru(mr.hi[1]),
+                     __double2float_ru(mr.hi[2]), 0.f);
 }
 
 __global__ void emit_kernel(const BuildM* __restrict__ M, const int32_t* __restrict__ pre,
@@ -438,7 +463,31 @@ __global__ void emit_kernel(const BuildM* __restrict__ M, const int32_t* __restr
     for (int k = 0; k < 9; ++k) td[(int64_t)slot * 9 + k] = v[k];
     tf[(int64_t)slot * 3 + 0] = make_float4((float)v[0], (float)v[1], (float)v[2], (float)v[3]);
     tf[(int64_t)slot * 3 + 1] = make_float4((float)v[4], (float)v[5], (float)v[6], (float)v[7]);
-    tf[(int64_t)slot * 3 + 2] = make_float4((float)v[8], 0.f, 0.f, 0.f);
+    // .y: error slack of the FP32 closest-point screen for this triangle
+    // (distance.cu): 32 u (|e1|^2 |e2|^2 / |e1 x e2|^2) L + 8 u max|v|,
+    // u = 2^-24, L the longest edge; infinite for a (near) degenerate one.
+    float slack = INFINITY;
+    {
+      double e1[3], e2[3], e3[3], cr[3];
+      double l1 = 0, l2 = 0, l3 = 0, vm = 0;
+      for (int d = 0; d < 3; ++d) {
+        e1[d] = v[3 + d] - v[d];
+        e2[d] = v[6 + d] - v[d];
+        e3[d] = v[6 + d] - v[3 + d];
+        l1 += e1[d] * e1[d];
+        l2 += e2[d] * e2[d];
+        l3 += e3[d] * e3[d];
+        vm = fmax(vm, fmax(fabs(v[d]), fmax(fabs(v[3 + d]), fabs(v[6 + d]))));
+      }
+      cr[0] = e1[1] * e2[2] - e1[2] * e2[1];
+      cr[1] = e1[2] * e2[0] - e1[0] * e2[2];
+      cr[2] = e1[0] * e2[1] - e1[1] * e2[0];
+      const double den = cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2];
+      const double cond = den > 0 ? l1 * l2 / den : INFINITY;
+      const double u = 5.9604644775390625e-08;
+      if (cond < 1e6) slack = (float)(32 * u * cond * sqrt(fmax(l1, fmax(l2, l3))) + 8 * u * vm);
+    }
+    tf[(int64_t)slot * 3 + 2] = make_float4((float)v[8], slack, 0.f, 0.f);
   }
 }
 
@@ -583,7 +632,7 @@ void soup_build(gwn_soup_impl& s, const double* V, int64_t nV, const int32_t* F,
   GWN_CUDA(cudaGetLastError());
   launch_kernel(preorder_kernel, (nnodes + 255) / 256, 256, 0, st, left.get(), parent.get(), size.get(),
                                                         nnodes, 0, pre.get(),
-                                                        depth.get());
+                                                        depth.get(), dmax.get());
   GWN_CUDA(cudaGetLastError());
   s.tri_index.alloc((size_t)n);
   GWN_CUDA(cudaMemcpyAsync(s.tri_index.get(), vals.get(), (size_t)n * sizeof(int32_t),
@@ -592,6 +641,10 @@ void soup_build(gwn_soup_impl& s, const double* V, int64_t nV, const int32_t* F,
   s.nd.alloc((size_t)nnodes);
   s.tf.alloc((size_t)n * 3);
   s.td.alloc((size_t)n * 9);
+  s.snode.alloc((size_t)std::max(n - 1, 1) * 4);
+  if (n > 1)
+    launch_kernel(search_nodes_kernel, (n - 1 + 255) / 256, 256, 0, st, (const BuildM*)M.get(),
+                  (const int32_t*)left.get(), (const int32_t*)right.get(), n, s.snode.get());
   launch_kernel(emit_kernel, (nnodes + 255) / 256, 256, 0, st, M.get(), pre.get(), size.get(), n, V, F,
                                                     vals.get(), s.nf.get(), s.nd.get(), s.tf.get(),
                                                     s.td.get());
@@ -612,7 +665,8 @@ void soup_build(gwn_soup_impl& s, const double* V, int64_t nV, const int32_t* F,
   }
   s.eps = kNearFrac * sqrt(diag2);
   s.cmax = cmax;
-  s.bytes = s.nf.bytes() + s.nd.bytes() + s.tf.bytes() + s.td.bytes() + s.tri_index.bytes();
+  s.bytes = s.nf.bytes() + s.nd.bytes() + s.tf.bytes() + s.td.bytes() + s.tri_index.bytes() +
+            s.snode.bytes();
 }
 
 // ------------------------------------------------------------------- eval --

@@ -45,6 +45,11 @@ struct gwn_soup_impl {
   DevMem<float4> tf;     // 3 float4 per slot: a.xyz b.x | b.yz c.xy | c.z
   DevMem<double> td;     // 9 doubles per slot
   DevMem<int32_t> tri_index;  // input triangle id per slot
+  // Closest-point search nodes, one per internal node of the binary tree in
+  // build order (root 0): 4 float4 = boxes of the two children, rounded
+  // outward to FP32, and the children (internal index, or ~slot for a leaf):
+  //   {lo_l.xyz, left}, {hi_l.xyz, right}, {lo_r.xyz, 0}, {hi_r.xyz, 0}.
+  DevMem<float4> snode;
   size_t bytes = 0;
 };
 
@@ -57,5 +62,10 @@ void soup_walk_stats(const gwn_soup_impl& s, float beta, const double* Q, int64_
                      unsigned long long* out7, cudaStream_t st);
 void soup_eval(const gwn_soup_impl& s, float beta, const void* Q, int q_dtype, int64_t nQ,
                void* W, int w_dtype, int precision, cudaStream_t st);
+// Closest triangle of each query (distance.cu): squared distance below
+// up_sqr_d (else up_sqr_d and I = -1), input triangle index, closest point.
+void soup_squared_distance(const gwn_soup_impl& s, const void* Q, int q_dtype, int64_t nQ,
+                           double up_sqr_d, double* sqrD, int32_t* I, double* C,
+                           cudaStream_t st);
 
 }  // namespace gwn

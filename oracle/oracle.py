@@ -20,7 +20,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "liboracle.so")
 REF_SOUP_PATH = os.path.join(HERE, "_ref", "libref_soup.so")
 
-_SOURCES = ["gwn_oracle.cpp", "soup_port.cpp", "soup_hdk.cpp", "wn_hier.cpp"]
+_SOURCES = ["gwn_oracle.cpp", "soup_port.cpp", "soup_hdk.cpp", "wn_hier.cpp", "distance.cpp", "aabb.cpp"]
 
 
 def build(force: bool = False) -> str:
@@ -82,6 +82,17 @@ def lib():
             L.oracle_soup_tree_eval.argtypes = [p, p, p, i64, p, C.c_int, C.c_float, p, i64, p,
                                                 C.c_int]
             L.oracle_soup_leaf.argtypes = [p, p, p, p]
+        if hasattr(L, "oracle_squared_distance"):
+            L.oracle_squared_distance.argtypes = [p, p, i64, p, i64, C.c_double, p, p, p,
+                                                  C.c_int]
+            L.oracle_squared_distance.restype = C.c_int
+            L.oracle_point_triangle.argtypes = [p, p, p, p, p]
+            L.oracle_point_triangle.restype = C.c_double
+        if hasattr(L, "oracle_aabb_build"):
+            L.oracle_aabb_build.argtypes = [p, p, i64]
+            L.oracle_aabb_build.restype = p
+            L.oracle_aabb_free.argtypes = [p]
+            L.oracle_aabb_squared_distance.argtypes = [p, p, i64, C.c_double, p, p, p, C.c_int]
         if hasattr(L, "oracle_winding_number_hier"):
             L.oracle_winding_number_hier.argtypes = [p, i64, p, i64, p, i64, p, C.c_int]
             L.oracle_winding_number_hier.restype = C.c_int
@@ -294,3 +305,83 @@ def soup_tree_eval(V, F, nodes, tri_index, Q, accuracy_scale: float = 2.0, order
                                 order, float(accuracy_scale), _ptr(Q), Q.shape[0], _ptr(W),
                                 nthreads)
     return W
+
+
+# ----------------------------------------------------------- signed distance --
+SIGNED_DISTANCE_TYPE_PSEUDONORMAL = 0
+SIGNED_DISTANCE_TYPE_WINDING_NUMBER = 1
+SIGNED_DISTANCE_TYPE_DEFAULT = 2
+SIGNED_DISTANCE_TYPE_UNSIGNED = 3
+SIGNED_DISTANCE_TYPE_FAST_WINDING_NUMBER = 4
+
+
+def squared_distance(V, F, P, up_sqr_d: float = np.inf, nthreads: int = 0):
+    """Brute-force closest triangle (distance.cpp): (sqrD, I, C)."""
+    V, P = _d(V), _d(P)
+    F = _d(F, np.int32)
+    sqrD = np.empty(P.shape[0])
+    I = np.empty(P.shape[0], np.int32)
+    Cp = np.empty((P.shape[0], 3))
+    lib().oracle_squared_distance(_ptr(V), _ptr(F), F.shape[0], _ptr(P), P.shape[0],
+                                  float(up_sqr_d), _ptr(sqrD), _ptr(I), _ptr(Cp), nthreads)
+    return sqrD, I, Cp
+
+
+def signed_distance(P, V, F, sign_type, lower_bound=None, upper_bound=None):
+    """igl::signed_distance(P,V,F,sign_type,lower,upper,S,I,C,N) for 3-D
+    triangles, restating include/igl/signed_distance.cpp:372-424 (dispatch,
+    empty F) and :83-137 (bounds, per-query sign): (S, I, C).  The default
+    bounds are the reference's (numeric_limits min / max, :426-440)."""
+    P, V = _d(P), _d(V)
+    F = _d(F, np.int32)
+    nP = P.shape[0]
+    if F.shape[0] == 0:
+        return np.full(nP, np.nan), np.full(nP, -1, np.int32), np.full((nP, 3), np.nan)
+    if sign_type == SIGNED_DISTANCE_TYPE_PSEUDONORMAL:
+        raise NotImplementedError("pseudonormal sign is not restated")
+    lo = np.finfo(np.float64).tiny if lower_bound is None else float(lower_bound)
+    hi = np.finfo(np.float64).max if upper_bound is None else float(upper_bound)
+    max_abs = max(abs(lo), abs(hi))
+    with np.errstate(over="ignore"):
+        up2 = float(np.float64(max_abs) ** 2)
+    low2 = max(max_abs - (hi - lo), 0.0) ** 2
+    sqrD, I, Cp = squared_distance(V, F, P, up2)
+    if sign_type in (SIGNED_DISTANCE_TYPE_WINDING_NUMBER, SIGNED_DISTANCE_TYPE_DEFAULT):
+        s = 1.0 - 2.0 * winding_number(V, F, P)
+    elif sign_type == SIGNED_DISTANCE_TYPE_FAST_WINDING_NUMBER:
+        # fast_winding_number(fwn_bvh, 2, q) on the float copy of V (:64-65, 113-116)
+        w = SoupPort(V.astype(np.float32).astype(np.float64), F, order=2).eval(P, 2.0)
+        s = 1.0 - 2.0 * np.abs(w)
+    else:
+        s = np.ones(nP)
+    S = s * np.sqrt(sqrD)
+    out = (sqrD >= up2) | (sqrD < low2)
+    S[out] = np.nan
+    I = I.copy()
+    I[out] = F.shape[0] + 1
+    Cp[out] = 0.0
+    return S, I, Cp
+
+
+class AABB:
+    """igl::AABB<V,3> over triangles, restated (aabb.cpp): build, then
+    squared_distance(P) -> (sqrD, I, C)."""
+
+    def __init__(self, V, F):
+        self.V, self.F = _d(V), _d(F, np.int32)
+        self._h = lib().oracle_aabb_build(_ptr(self.V), _ptr(self.F), self.F.shape[0])
+
+    def squared_distance(self, P, up_sqr_d: float = np.inf, nthreads: int = 0):
+        P = _d(P)
+        sqrD = np.empty(P.shape[0])
+        I = np.empty(P.shape[0], np.int32)
+        Cp = np.empty((P.shape[0], 3))
+        lib().oracle_aabb_squared_distance(self._h, _ptr(P), P.shape[0], float(up_sqr_d),
+                                           _ptr(sqrD), _ptr(I), _ptr(Cp), nthreads)
+        return sqrD, I, Cp
+
+    def __del__(self):
+        try:
+            lib().oracle_aabb_free(self._h)
+        except Exception:
+            pass

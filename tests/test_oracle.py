@@ -166,3 +166,50 @@ def test_pair_atan2_polynomial_in_fp32():
     ref = np.arctan2(y.astype(np.float64), x.astype(np.float64))
     err = np.abs(r - ref)
     assert np.all(err <= 4 * np.spacing(np.abs(ref).astype(f32)) + 1e-12), err.max()
+
+
+def test_signed_distance_oracle_single_tet_golden():
+    """tests/include/igl/signed_distance.cpp:4-42: the point (.5,.5,.5) is
+    sqrt(1/12) from the unit tet for every sign type (1e-15; the fast winding
+    number sign 1e-7)."""
+    V = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], float)
+    F = np.array([[0, 1, 3], [0, 2, 1], [0, 3, 2], [1, 2, 3]], np.int32)
+    P = np.array([[0.5, 0.5, 0.5]])
+    for t, tol in ((O.SIGNED_DISTANCE_TYPE_WINDING_NUMBER, 1e-15),
+                   (O.SIGNED_DISTANCE_TYPE_DEFAULT, 1e-15),
+                   (O.SIGNED_DISTANCE_TYPE_UNSIGNED, 1e-15),
+                   (O.SIGNED_DISTANCE_TYPE_FAST_WINDING_NUMBER, 1e-7)):
+        S, I, Cp = O.signed_distance(P, V, F, t)
+        assert abs(S[0] - np.sqrt(1 / 12)) <= tol, (t, S)
+        assert I[0] == 3 and np.allclose(Cp[0], 1 / 3, atol=1e-15)
+
+
+def test_closest_point_oracle_regions():
+    """Ericson's regions on one triangle: vertex, edge and face closest points
+    against analytic answers."""
+    a, b, c = np.array([0., 0, 0]), np.array([1., 0, 0]), np.array([0., 1, 0])
+    L = O.lib()
+    cases = [([-1, -1, 0.5], [0, 0, 0]), ([2, -0.5, 0], [1, 0, 0]), ([0.5, -1, 1], [0.5, 0, 0]),
+             ([0.2, 0.3, -2], [0.2, 0.3, 0]), ([1, 1, 0], [0.5, 0.5, 0]), ([-1, 0.5, 0], [0, 0.5, 0])]
+    for p, cp in cases:
+        p = np.array(p, float)
+        out = np.empty(3)
+        d2 = L.oracle_point_triangle(O._ptr(p), O._ptr(a), O._ptr(b), O._ptr(c), O._ptr(out))
+        assert np.allclose(out, cp, atol=1e-15), (p, out)
+        assert abs(d2 - np.sum((p - np.array(cp)) ** 2)) < 1e-14
+
+
+def test_aabb_restatement_matches_brute_force():
+    """The AABB restatement (the timed CPU baseline of the signed distance)
+    finds the brute-force minimum distance."""
+    from libigl_gb300 import synth
+    V, F = synth.soup_mesh(seed=31, subdiv=3, delete_frac=0.02)
+    rng = np.random.default_rng(32)
+    P = rng.uniform(V.min(0) - 0.3, V.max(0) + 0.3, size=(3000, 3))
+    P = np.concatenate([P, V[:40]])
+    D, I, Cp = O.AABB(V, F).squared_distance(P)
+    Db, Ib, Cb = O.squared_distance(V, F, P)
+    assert np.array_equal(D, Db)
+    # a closest edge or vertex is shared by several triangles (ties), so the
+    # indices may differ; the closest points agree
+    assert np.abs(Cp - Cb).max() <= 1e-12
