@@ -11,6 +11,7 @@
 #include <Eigen/Core>
 #include <igl/fast_winding_number.h>
 #include <igl/octree.h>
+#include <igl/signed_distance.h>
 #include <igl/winding_number.h>
 
 static int failures = 0;
@@ -77,6 +78,23 @@ int main() {
   Eigen::VectorXd Wc;
   igl::fast_winding_number(P, N, A, Q, Wc);
   for (int i = 0; i < 4; ++i) check_near("one_point_cloud_oneshot", Wc(i), cached[i], 1e-15);
+  // signed_distance single tet (tests/include/igl/signed_distance.cpp:4-42):
+  // every provided sign type gives sqrt(1/12) at (.5,.5,.5)
+  {
+    Eigen::MatrixXd Pq(1, 3);
+    Pq.set({0.5, 0.5, 0.5});
+    const igl::SignedDistanceType types[4] = {
+        igl::SIGNED_DISTANCE_TYPE_WINDING_NUMBER, igl::SIGNED_DISTANCE_TYPE_DEFAULT,
+        igl::SIGNED_DISTANCE_TYPE_UNSIGNED, igl::SIGNED_DISTANCE_TYPE_FAST_WINDING_NUMBER};
+    for (const auto type : types) {
+      Eigen::VectorXd S;
+      Eigen::VectorXi I;
+      Eigen::MatrixXd Cc, Nn;
+      igl::signed_distance(Pq, V, F, type, S, I, Cc, Nn);
+      const double tol = type == igl::SIGNED_DISTANCE_TYPE_FAST_WINDING_NUMBER ? 1e-7 : 1e-15;
+      check_near("signed_distance_tet", S(0), std::sqrt(1.0 / 12.0), tol);
+    }
+  }
   std::printf("failures %d\n", failures);
   return failures ? 1 : 0;
 }
