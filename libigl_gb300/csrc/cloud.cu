@@ -42,6 +42,11 @@ namespace gwn {
 namespace {
 
 constexpr int kChunk = 1024;
+// Cells with at most kSmallCell points are summed by one thread each (both
+// passes, points in list order); larger cells by warps over 1024-point
+// chunks.  Most cells of an octree are small: giving each a warp spent the
+// time in 37-value FP64 warp reductions for a handful of points.
+constexpr int kSmallCell = 64;
 constexpr double kNearFrac = 1e-3;
 constexpr double kBand = 1e-3;
 constexpr double kPi4 = 4.0 * kPi;
@@ -62,7 +67,7 @@ __global__ void an_kernel(const double* __restrict__ N, const double* __restrict
 __global__ void chunk_count_kernel(const int32_t* __restrict__ count, int64_t ncells,
                                    unsigned* __restrict__ nch) {
   const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (c < ncells) nch[c] = (unsigned)((count[c] + kChunk - 1) / kChunk);
+  if (c < ncells) nch[c] = count[c] > kSmallCell ? (unsigned)((count[c] + kChunk - 1) / kChunk) : 0u;
 }
 
 __global__ void chunk_fill_kernel(const unsigned* __restrict__ nch,
@@ -130,6 +135,7 @@ __global__ void combine1_kernel(const int32_t* __restrict__ count, int64_t ncell
                                 double* __restrict__ area) {
   const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (c >= ncells) return;
+  if (count[c] > 0 && count[c] <= kSmallCell) return;  // small_cells_kernel
   double s[7] = {0, 0, 0, 0, 0, 0, 0};
   for (unsigned j = 0; j < nch[c]; ++j)
     for (int k = 0; k < 7; ++k) s[k] += part[(chunk_base[c] + j) * 8 + k];
@@ -206,6 +212,7 @@ __global__ void combine2_kernel(const int32_t* __restrict__ count, int64_t ncell
                                 double* __restrict__ R, double* __restrict__ EC) {
   const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (c >= ncells) return;
+  if (count[c] > 0 && count[c] <= kSmallCell) return;  // small_cells_kernel
   double mx = 0;
   for (unsigned j = 0; j < nch[c]; ++j) mx = fmax(mx, part[(chunk_base[c] + j) * 37]);
   R[c] = mx;
@@ -214,6 +221,73 @@ __global__ void combine2_kernel(const int32_t* __restrict__ count, int64_t ncell
     for (unsigned j = 0; j < nch[c]; ++j) s += part[(chunk_base[c] + j) * 37 + (k - 2)];
     EC[c * num_terms + k] = s;
   }
+}
+
+// Both passes for one small cell per thread: the same terms as pass1 /
+// combine1 / pass2 / combine2, summed over the cell's points in list order
+// (the reference's loop order, fast_winding_number.cpp:57-120).
+template <int NT>
+__global__ void small_cells_kernel(CsrView v, int64_t ncells, const double* __restrict__ P,
+                                   const double* __restrict__ N, const double* __restrict__ A,
+                                   double* __restrict__ CM, double* __restrict__ R,
+                                   double* __restrict__ EC, double* __restrict__ area) {
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  const int32_t cnt = v.count[c];
+  if (cnt <= 0 || cnt > kSmallCell) return;
+  const int64_t s0 = v.start[c];
+  double s[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (int j = 0; j < cnt; ++j) {
+    const int64_t p = v.idx[s0 + j];
+    const double a = A[p];
+    s[0] += a;
+    for (int d = 0; d < 3; ++d) {
+      s[1 + d] += a * P[p * 3 + d];
+      s[4 + d] += a * N[p * 3 + d];
+    }
+  }
+  area[c] = s[0];
+  double cm[3];
+  for (int d = 0; d < 3; ++d) {
+    cm[d] = s[1 + d] / s[0];
+    CM[c * 3 + d] = cm[d];
+    EC[c * NT + d] = s[4 + d];
+  }
+  double mx = 0;
+  double acc[NT > 3 ? NT - 3 : 1];
+#pragma unroll
+  for (int k = 0; k < NT - 3; ++k) acc[k] = 0;
+  for (int j = 0; j < cnt; ++j) {
+    const int64_t p = v.idx[s0 + j];
+    const double a = A[p];
+    double pt[3], n[3];
+    for (int d = 0; d < 3; ++d) {
+      pt[d] = P[p * 3 + d] - cm[d];
+      n[d] = N[p * 3 + d];
+    }
+    const double nrm = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(pt[0], pt[0]), __dmul_rn(pt[1], pt[1])),
+                                      __dmul_rn(pt[2], pt[2])));
+    mx = fmax(mx, nrm);
+    if (NT >= 12) {
+#pragma unroll
+      for (int vv = 0; vv < 3; ++vv)
+#pragma unroll
+        for (int u = 0; u < 3; ++u) acc[u + 3 * vv] += (a * pt[u]) * n[vv];
+    }
+    if (NT == 39) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const double h = 0.5 * pt[k];
+#pragma unroll
+        for (int vv = 0; vv < 3; ++vv)
+#pragma unroll
+          for (int u = 0; u < 3; ++u) acc[9 + 9 * k + u + 3 * vv] += h * ((a * pt[u]) * n[vv]);
+      }
+    }
+  }
+  R[c] = mx;
+#pragma unroll
+  for (int k = 0; k < NT - 3; ++k) EC[c * NT + 3 + k] = acc[k];
 }
 
 // ----------------------------------------------------------------- layout --
@@ -682,7 +756,15 @@ void precompute(gwn_cloud_impl& c, const CsrView& v, int64_t ncells, const doubl
   }
   launch_kernel(combine2_kernel, blocks(ncells), 256, 0, st, v.count, ncells, nch.get(), cbase.get(),
                                                   part.get(), c.num_terms, c.R.get(), c.EC.get());
-  GWN_CUDA(cudaGetLastError());
+  if (c.num_terms == 39)
+    launch_kernel(small_cells_kernel<39>, blocks(ncells, 128), 128, 0, st, v, ncells, P, N, A,
+                  c.CM.get(), c.R.get(), c.EC.get(), c.area.get());
+  else if (c.num_terms == 12)
+    launch_kernel(small_cells_kernel<12>, blocks(ncells, 128), 128, 0, st, v, ncells, P, N, A,
+                  c.CM.get(), c.R.get(), c.EC.get(), c.area.get());
+  else
+    launch_kernel(small_cells_kernel<3>, blocks(ncells, 128), 128, 0, st, v, ncells, P, N, A,
+                  c.CM.get(), c.R.get(), c.EC.get(), c.area.get());
 }
 
 __global__ void count_nonempty_kernel(const int32_t* __restrict__ count, int64_t n,

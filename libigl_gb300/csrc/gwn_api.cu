@@ -89,6 +89,27 @@ static int current_device() {
   return d;
 }
 
+static std::vector<cudaMemPool_t> g_pools;  // per device
+cudaMemPool_t device_pool() {
+  const int d = current_device();
+  std::lock_guard<std::mutex> lk(g_dev_mutex);
+  if ((int)g_pools.size() <= d) g_pools.resize(d + 1, nullptr);
+  if (!g_pools[d]) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = d;
+    cudaMemPool_t pool = nullptr;
+    GWN_CUDA(cudaMemPoolCreate(&pool, &props));
+    uint64_t keep = ~0ull;
+    GWN_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    g_pools[d] = pool;
+  }
+  return g_pools[d];
+}
+
+
 int num_sms() {
   const int d = current_device();
   std::lock_guard<std::mutex> lk(g_dev_mutex);

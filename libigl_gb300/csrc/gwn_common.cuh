@@ -58,7 +58,14 @@ int guarded(const char* where, Fn&& fn) {
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
-// Stream-ordered device buffer (cudaMallocAsync / cudaFreeAsync).
+// The library's stream-ordered memory pool on the current device: memory
+// freed into it stays reserved for the next call instead of being returned
+// to the driver at every synchronization (the default pool's release
+// threshold is 0, which makes every call map its buffers again).
+cudaMemPool_t device_pool();
+
+// Stream-ordered device buffer (cudaMallocFromPoolAsync on device_pool() /
+// cudaFreeAsync).
 template <typename T>
 class DevBuf {
  public:
@@ -80,7 +87,7 @@ class DevBuf {
     stream_ = s;
     n_ = n;
     if (n == 0) return;
-    GWN_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&p_), n * sizeof(T), s));
+    GWN_CUDA(cudaMallocFromPoolAsync(reinterpret_cast<void**>(&p_), n * sizeof(T), device_pool(), s));
   }
   void release() {
     if (p_) cudaFreeAsync(p_, stream_);
