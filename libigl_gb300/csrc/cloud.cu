@@ -127,24 +127,41 @@ __global__ void pass1_kernel(CsrView v, const int32_t* __restrict__ chunk_cell,
   }
 }
 
-__global__ void combine1_kernel(const int32_t* __restrict__ count, int64_t ncells,
-                                const unsigned* __restrict__ nch,
+// Cells with more than kSmallCell points: one warp per cell (the warp that
+// owns the cell's first chunk) sums the chunk partials, lanes striding the
+// chunks, then a fixed xor tree: a deterministic order that does not leave
+// one thread summing thousands of partials of the largest cells.
+__global__ void combine1_kernel(const int32_t* __restrict__ chunk_cell,
                                 const unsigned* __restrict__ chunk_base,
+                                const unsigned* __restrict__ nch, int64_t nchunks,
                                 const double* __restrict__ part, int num_terms,
                                 double* __restrict__ CM, double* __restrict__ EC,
                                 double* __restrict__ area) {
-  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (c >= ncells) return;
-  if (count[c] > 0 && count[c] <= kSmallCell) return;  // small_cells_kernel
+  const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= nchunks) return;
+  const int32_t c = chunk_cell[w];
+  if ((unsigned)w != chunk_base[c]) return;  // not the cell's first chunk
   double s[7] = {0, 0, 0, 0, 0, 0, 0};
-  for (unsigned j = 0; j < nch[c]; ++j)
+  for (unsigned j = lane; j < nch[c]; j += 32)
     for (int k = 0; k < 7; ++k) s[k] += part[(chunk_base[c] + j) * 8 + k];
+  for (int k = 0; k < 7; ++k) s[k] = warp_sum(s[k]);
+  if (lane != 0) return;
   area[c] = s[0];
   for (int d = 0; d < 3; ++d) {
-    CM[c * 3 + d] = count[c] > 0 ? s[1 + d] / s[0] : __longlong_as_double(0x7ff8000000000000LL);
+    CM[c * 3 + d] = s[1 + d] / s[0];
     EC[c * num_terms + d] = s[4 + d];
   }
-  for (int k = 3; k < num_terms; ++k) EC[c * num_terms + k] = 0.0;
+}
+
+// Empty cells: CM = 0/0 (NaN) and zero area, as the reference's sums give.
+__global__ void empty_cells_kernel(const int32_t* __restrict__ count, int64_t ncells,
+                                   double* __restrict__ CM, double* __restrict__ area) {
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= ncells || count[c] != 0) return;
+  const double nan = __longlong_as_double(0x7ff8000000000000LL);
+  CM[c * 3] = CM[c * 3 + 1] = CM[c * 3 + 2] = nan;
+  area[c] = 0.0;
 }
 
 // Pass 2: max |p - CM| and the order-1/2 moments about CM (1 + 36 doubles).
@@ -205,21 +222,25 @@ __global__ void pass2_kernel(CsrView v, const int32_t* __restrict__ chunk_cell,
   }
 }
 
-__global__ void combine2_kernel(const int32_t* __restrict__ count, int64_t ncells,
-                                const unsigned* __restrict__ nch,
+__global__ void combine2_kernel(const int32_t* __restrict__ chunk_cell,
                                 const unsigned* __restrict__ chunk_base,
+                                const unsigned* __restrict__ nch, int64_t nchunks,
                                 const double* __restrict__ part, int num_terms,
                                 double* __restrict__ R, double* __restrict__ EC) {
-  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (c >= ncells) return;
-  if (count[c] > 0 && count[c] <= kSmallCell) return;  // small_cells_kernel
+  const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= nchunks) return;
+  const int32_t c = chunk_cell[w];
+  if ((unsigned)w != chunk_base[c]) return;  // not the cell's first chunk
   double mx = 0;
-  for (unsigned j = 0; j < nch[c]; ++j) mx = fmax(mx, part[(chunk_base[c] + j) * 37]);
-  R[c] = mx;
+  for (unsigned j = lane; j < nch[c]; j += 32) mx = fmax(mx, part[(chunk_base[c] + j) * 37]);
+  mx = warp_max(mx);
+  if (lane == 0) R[c] = mx;
   for (int k = 3; k < num_terms; ++k) {
     double s = 0;
-    for (unsigned j = 0; j < nch[c]; ++j) s += part[(chunk_base[c] + j) * 37 + (k - 2)];
-    EC[c * num_terms + k] = s;
+    for (unsigned j = lane; j < nch[c]; j += 32) s += part[(chunk_base[c] + j) * 37 + (k - 2)];
+    s = warp_sum(s);
+    if (lane == 0) EC[c * num_terms + k] = s;
   }
 }
 
@@ -227,14 +248,14 @@ __global__ void combine2_kernel(const int32_t* __restrict__ count, int64_t ncell
 // combine1 / pass2 / combine2, summed over the cell's points in list order
 // (the reference's loop order, fast_winding_number.cpp:57-120).
 template <int NT>
-__global__ void small_cells_kernel(CsrView v, int64_t ncells, const double* __restrict__ P,
-                                   const double* __restrict__ N, const double* __restrict__ A,
-                                   double* __restrict__ CM, double* __restrict__ R,
-                                   double* __restrict__ EC, double* __restrict__ area) {
-  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (c >= ncells) return;
-  const int32_t cnt = v.count[c];
-  if (cnt <= 0 || cnt > kSmallCell) return;
+__device__ __forceinline__ void small_cell_moments(CsrView v, int64_t c, int32_t cnt,
+                                                        const double* __restrict__ P,
+                                                        const double* __restrict__ N,
+                                                        const double* __restrict__ A,
+                                                        double* __restrict__ CM,
+                                                        double* __restrict__ R,
+                                                        double* __restrict__ area,
+                                                        double* __restrict__ row) {
   const int64_t s0 = v.start[c];
   double s[7] = {0, 0, 0, 0, 0, 0, 0};
   for (int j = 0; j < cnt; ++j) {
@@ -251,7 +272,7 @@ __global__ void small_cells_kernel(CsrView v, int64_t ncells, const double* __re
   for (int d = 0; d < 3; ++d) {
     cm[d] = s[1 + d] / s[0];
     CM[c * 3 + d] = cm[d];
-    EC[c * NT + d] = s[4 + d];
+    row[d] = s[4 + d];
   }
   double mx = 0;
   double acc[NT > 3 ? NT - 3 : 1];
@@ -287,8 +308,39 @@ __global__ void small_cells_kernel(CsrView v, int64_t ncells, const double* __re
   }
   R[c] = mx;
 #pragma unroll
-  for (int k = 0; k < NT - 3; ++k) EC[c * NT + 3 + k] = acc[k];
+  for (int k = 0; k < NT - 3; ++k) row[3 + k] = acc[k];
 }
+
+// One block of 128 threads handles 128 consecutive cells; the EC rows are
+// staged in shared memory per warp and written out coalesced (each warp's 32
+// rows are one contiguous block of EC).
+template <int NT>
+__global__ void __launch_bounds__(128) small_cells_kernel(CsrView v, int64_t ncells,
+                                                          const double* __restrict__ P,
+                                                          const double* __restrict__ N,
+                                                          const double* __restrict__ A,
+                                                          double* __restrict__ CM,
+                                                          double* __restrict__ R,
+                                                          double* __restrict__ EC,
+                                                          double* __restrict__ area) {
+  __shared__ double rows[4][32 * NT];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t c0 = (blockIdx.x * (int64_t)blockDim.x) + warp * 32;  // first cell of the warp
+  const int64_t c = c0 + lane;
+  const int32_t cnt = c < ncells ? v.count[c] : 0;
+  const bool mine = cnt > 0 && cnt <= kSmallCell;
+  const unsigned small_mask = __ballot_sync(0xffffffffu, mine);
+  if (small_mask == 0u) return;  // the whole warp: no small cell
+  if (mine) small_cell_moments<NT>(v, c, cnt, P, N, A, CM, R, area, rows[warp] + lane * NT);
+  __syncwarp();
+  // coalesced write of the small cells' rows
+  double* out = EC + c0 * NT;
+  for (int e = lane; e < 32 * NT; e += 32) {
+    const int row = e / NT;
+    if (c0 + row < ncells && ((small_mask >> row) & 1u)) out[e] = rows[warp][e];
+  }
+}
+
 
 // ----------------------------------------------------------------- layout --
 __global__ void nonempty_keys_kernel(const int64_t* __restrict__ start,
@@ -725,6 +777,9 @@ void precompute(gwn_cloud_impl& c, const CsrView& v, int64_t ncells, const doubl
   c.EC.alloc((size_t)std::max<int64_t>(ncells, 1) * c.num_terms);
   c.area.alloc((size_t)std::max<int64_t>(ncells, 1));
   if (ncells == 0) return;
+  // empty cells keep R = 0 and EC = 0; the kernels below write the others
+  GWN_CUDA(cudaMemsetAsync(c.EC.get(), 0, c.EC.bytes(), st));
+  GWN_CUDA(cudaMemsetAsync(c.R.get(), 0, c.R.bytes(), st));
   DevBuf<unsigned> nch((size_t)ncells, st), cbase((size_t)ncells, st);
   launch_kernel(chunk_count_kernel, blocks(ncells), 256, 0, st, v.count, ncells, nch.get());
   exclusive_scan_u32(nch.get(), cbase.get(), ncells, st);
@@ -739,9 +794,12 @@ void precompute(gwn_cloud_impl& c, const CsrView& v, int64_t ncells, const doubl
   if (nchunks)
     launch_kernel(pass1_kernel, blocks(nchunks * 32), 256, 0, st, v, chunk_cell.get(), cbase.get(), nchunks, P,
                                                       N, A, part.get());
-  launch_kernel(combine1_kernel, blocks(ncells), 256, 0, st, v.count, ncells, nch.get(), cbase.get(),
-                                                  part.get(), c.num_terms, c.CM.get(), c.EC.get(),
-                                                  c.area.get());
+  if (nchunks)
+    launch_kernel(combine1_kernel, blocks(nchunks * 32), 256, 0, st, (const int32_t*)chunk_cell.get(),
+                  (const unsigned*)cbase.get(), (const unsigned*)nch.get(), nchunks,
+                  (const double*)part.get(), c.num_terms, c.CM.get(), c.EC.get(), c.area.get());
+  launch_kernel(empty_cells_kernel, blocks(ncells), 256, 0, st, v.count, ncells, c.CM.get(),
+                c.area.get());
   GWN_CUDA(cudaGetLastError());
   if (nchunks) {
     if (c.num_terms == 39)
@@ -754,8 +812,10 @@ void precompute(gwn_cloud_impl& c, const CsrView& v, int64_t ncells, const doubl
       launch_kernel(pass2_kernel<3>, blocks(nchunks * 32), 256, 0, st, v, chunk_cell.get(), cbase.get(),
                                                            nchunks, P, N, A, c.CM.get(), part.get());
   }
-  launch_kernel(combine2_kernel, blocks(ncells), 256, 0, st, v.count, ncells, nch.get(), cbase.get(),
-                                                  part.get(), c.num_terms, c.R.get(), c.EC.get());
+  if (nchunks)
+    launch_kernel(combine2_kernel, blocks(nchunks * 32), 256, 0, st, (const int32_t*)chunk_cell.get(),
+                  (const unsigned*)cbase.get(), (const unsigned*)nch.get(), nchunks,
+                  (const double*)part.get(), c.num_terms, c.R.get(), c.EC.get());
   if (c.num_terms == 39)
     launch_kernel(small_cells_kernel<39>, blocks(ncells, 128), 128, 0, st, v, ncells, P, N, A,
                   c.CM.get(), c.R.get(), c.EC.get(), c.area.get());

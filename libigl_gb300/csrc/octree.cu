@@ -144,16 +144,27 @@ __global__ void octant_kernel(const double* __restrict__ P, const int32_t* __res
   if (py >= cc[(int64_t)cell * 3 + 1]) o += 2;
   if (pz >= cc[(int64_t)cell * 3 + 2]) o += 4;
   key[m] = (unsigned)k * 8u + (unsigned)o;
-  atomicOr(&seg_mask[k], 1u << o);
+  // All points of a segment hit the same two words: read first and skip the
+  // atomic once the bit is set (at the top levels millions of points share
+  // one segment, and same-address atomics serialize).
+  const unsigned bit = 1u << o;
+  if ((*(volatile unsigned*)&seg_mask[k] & bit) == 0u) atomicOr(&seg_mask[k], bit);
   const int32_t f = act_pt[seg_first[k]];
-  if (px != P[(int64_t)f * 3] || py != P[(int64_t)f * 3 + 1] || pz != P[(int64_t)f * 3 + 2])
+  if ((px != P[(int64_t)f * 3] || py != P[(int64_t)f * 3 + 1] || pz != P[(int64_t)f * 3 + 2]) &&
+      *(volatile unsigned*)&seg_diff[k] == 0u)
     atomicOr(&seg_diff[k], 1u);
 }
 
+// Points per child from the sorted keys: each run of equal keys adds its end
+// and subtracts its start (two uncontended atomics per run; child_count is
+// zero on entry).
 __global__ void child_count_kernel(const unsigned* __restrict__ key, int64_t M,
                                    unsigned* __restrict__ child_count) {
   const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (m < M) atomicAdd(&child_count[key[m]], 1u);
+  if (m >= M) return;
+  const unsigned k = key[m];
+  if (m == 0 || key[m - 1] != k) atomicSub(&child_count[k], (unsigned)m);
+  if (m == M - 1 || key[m + 1] != k) atomicAdd(&child_count[k], (unsigned)(m + 1));
 }
 
 // Whether the FP64 centre recurrence can no longer move `c` on any axis:
