@@ -57,7 +57,7 @@ def parse():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--workload", choices=["soup", "exact", "cloud", "precision", "served",
-                                           "signed_distance"],
+                                           "signed_distance", "knn"],
                     default="soup",
                     help="soup = the headline line; the others are extra measurement lines")
     ap.add_argument("--served-seconds", type=float, default=4.0,
@@ -592,6 +592,60 @@ def run_signed_distance_line(args):
     print(json.dumps(line), flush=True)
 
 
+def run_knn_line(args):
+    """igl::knn on the C3 cloud: the 16 nearest of the 2M torus points for
+    1M of the points themselves (the use of knn before point areas).
+    value = queries/s on a built octree (device arrays); one-shot = octree
+    build + search from host arrays; CPU baseline = the restated reference
+    best-first search (oracle/knn.cpp) on the host cores, 20k-query sample."""
+    import torch
+    import libigl_gb300 as G
+    from libigl_gb300 import synth
+    from oracle import oracle as O
+    P, _, _ = synth.torus_cloud(seed=3, n=2_000_000)
+    Q = P[::2][:1_000_000]
+    k = 16
+    dP, dQ = torch.from_numpy(P).cuda(), torch.from_numpy(Q).cuda()
+    tree = G.Octree(dP)
+    stream = torch.cuda.current_stream()
+    out = {}
+
+    def step():
+        out["I"] = tree.knn(dQ, k)
+    total, _ = timed_steps(step, args.steps, args.warmup, stream)
+    launches = G.launch_count_of(step)
+    t0 = time.perf_counter()
+    I1 = G.knn(Q, P, k)
+    one_shot = time.perf_counter() - t0
+    ns = 20_000
+    t0 = time.perf_counter()
+    ot = O.octree(P)
+    cpu_build = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    Ir = O.knn(Q[:ns], P, k, ot)
+    cpu_s = time.perf_counter() - t0
+    Ig = out["I"].cpu().numpy()
+    line = {"metric": "knn queries/s (k = 16, exact FP64 distances)",
+            "value": Q.shape[0] * args.steps / (total / 1e3), "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": "knn_torus_2Mpts_1Mq_k16", "points": int(P.shape[0]),
+                       "queries": int(Q.shape[0]), "k": k},
+            "e2e": {"value": Q.shape[0] / one_shot, "unit": UNIT,
+                    "h2d_bytes_per_step": int(P.nbytes + Q.nbytes),
+                    "d2h_bytes_per_step": int(Q.shape[0] * k * 4)},
+            "accuracy": {"identical_to_cpu_reference_search": bool(np.array_equal(Ig[:ns], Ir)),
+                         "one_shot_identical": bool(np.array_equal(I1, Ig)),
+                         "queries_compared": ns},
+            "gpu_launches": launches,
+            "cpu_baseline": {"value": ns / cpu_s, "unit": UNIT, "cores": O.num_threads(0),
+                             "kind": "port", "build_s": cpu_build,
+                             "sample": f"first {ns} queries, the reference's best-first search "
+                                       "restated (oracle/knn.cpp), octree built apart"}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -604,7 +658,7 @@ def main():
             torch.cuda.set_device(local)
         {"exact": run_exact_line, "cloud": run_cloud_line, "precision": run_precision_study,
          "served": run_served_line,
-         "signed_distance": run_signed_distance_line}[args.workload](args)
+         "signed_distance": run_signed_distance_line, "knn": run_knn_line}[args.workload](args)
         return
     import torch
     import libigl_gb300 as G

@@ -177,6 +177,17 @@ void gwn_octree_free(gwn_octree* tree);
  *     fast_winding_number.h:76-99 (fast_winding_number.cpp:126-311);
  * beta <= 0 selects the direct O(P*Q) sum (fast_winding_number.cpp:300-310).
  * ---------------------------------------------------------------------- */
+/* k nearest points: igl::knn(P,V,k,point_indices,CH,CN,W,I)
+ *   (include/igl/knn.h, knn.cpp:24-136) over the points the octree was built
+ *   from.  I (nQ x min(k, #points), int32, row-major) receives point indices,
+ *   nearest first; equal distances are ordered by index (the reference leaves
+ *   them to its priority queue).  Distances are the FP64 norm of V(j) - q. */
+int gwn_octree_knn(const gwn_octree* tree, const void* Q, int q_dtype, int64_t nQ, int64_t k,
+                   int32_t* I, int mem, void* stream);
+/* One-shot form: builds the octree of V (nV x 3) and answers the queries P. */
+int gwn_knn(const double* P, int64_t nP, const double* V, int64_t nV, int64_t k, int32_t* I,
+            int mem, void* stream);
+
 typedef struct gwn_cloud gwn_cloud;
 
 int gwn_cloud_build(const gwn_octree* tree, const double* P, const double* N, const double* A,

@@ -33,7 +33,7 @@ __all__ = [
     "fast_winding_number_soup_precompute", "fast_winding_number_soup",
     "Octree", "octree", "CloudExpansion", "fast_winding_number_cloud_precompute",
     "fast_winding_number_cloud", "fast_winding_number_cloud_oneshot", "device_status",
-    "Server", "signed_distance",
+    "Server", "signed_distance", "knn",
 ]
 
 _PREC = {"fp64": N.GWN_PLAIN_FP64, "plain": N.GWN_PLAIN_FP64, "mixed": N.GWN_MIXED}
@@ -307,6 +307,19 @@ class Octree:
         off, idx, *_ = self.export()
         return [idx[off[c]:off[c + 1]].tolist() for c in range(off.shape[0] - 1)]
 
+    def knn(self, Q, k: int):
+        """igl::knn over this octree's points: I (#Q x min(k, #points)),
+        nearest first, equal distances by index."""
+        Qa = _Arg(Q)
+        if len(Qa.shape) != 2 or Qa.shape[1] != 3:
+            raise ValueError("Q must be #Q x 3")
+        cols = min(int(k), self.num_points)
+        I = _empty_like_mem(Qa.mem, (Qa.shape[0], cols), np.int32, like=Qa)
+        stream = _stream_ptr() if Qa.mem == N.GWN_DEVICE else None
+        N.check(N.load().gwn_octree_knn(self._h, Qa.ptr, Qa.code, Qa.shape[0], int(k), _ptr_of(I),
+                                        Qa.mem, stream))
+        return I
+
     def close(self):
         if getattr(self, "_h", None):
             N.load().gwn_octree_free(self._h)
@@ -438,6 +451,20 @@ def fast_winding_number_cloud_oneshot(P, Nrm, A, Q, order: int = 2, beta: float 
     finally:
         ce.close()
         ce.tree.close()
+
+
+def knn(P, V, k: int):
+    """igl::knn(P,V,k,point_indices,CH,CN,W,I) (include/igl/knn.h): the k
+    points of V nearest to each row of P, nearest first (equal distances by
+    index); the octree of V is built inside.  Host arrays or CUDA tensors."""
+    Pa, Va = _Arg(P, np.float64), _Arg(V, np.float64)
+    _same_mem(Pa, Va)
+    cols = min(int(k), Va.shape[0])
+    I = _empty_like_mem(Pa.mem, (Pa.shape[0], cols), np.int32, like=Pa)
+    stream = _stream_ptr() if Pa.mem == N.GWN_DEVICE else None
+    N.check(N.load().gwn_knn(Pa.ptr, Pa.shape[0], Va.ptr, Va.shape[0], int(k), _ptr_of(I),
+                             Pa.mem, stream))
+    return I
 
 
 # ------------------------------------------------------- signed distance --

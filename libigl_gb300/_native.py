@@ -54,6 +54,8 @@ SIGNATURES = {
     "gwn_profile_enable": ([_i], _i),
     "gwn_launch_count": ([], C.c_ulonglong),
     "gwn_soup_squared_distance": ([_p, _p, _i, _i64, _d, _p, _p, _p, _i, _p], _i),
+    "gwn_octree_knn": ([_p, _p, _i, _i64, _i64, _p, _i, _p], _i),
+    "gwn_knn": ([_p, _i64, _p, _i64, _i64, _p, _i, _p], _i),
     "gwn_signed_distance": ([_p, _i64, _p, _i64, _p, _i64, _i, _d, _d, _p, _p, _p, _i, _i, _p],
                             _i),
     "gwn_server_create": ([_i64, _i64, C.c_int32, _p], _i),

@@ -602,6 +602,53 @@ int gwn_profile_read(char* names, int names_cap, float* ms, int max_phases, int*
 unsigned long long gwn_launch_count(void) { return g_launches.load(); }
 
 
+int gwn_octree_knn(const gwn_octree* tree, const void* Q, int q_dtype, int64_t nQ, int64_t k,
+                   int32_t* I, int mem, void* stream) {
+  return guarded("gwn_octree_knn", [&] {
+    GWN_REQUIRE(tree != nullptr, "octree handle is null");
+    GWN_REQUIRE(nQ >= 0 && k >= 0, "nQ and k must be non-negative");
+    const int64_t cols = knn_columns(tree->impl.n, k);
+    GWN_REQUIRE(nQ == 0 || cols == 0 || (Q && I), "Q and I must be non-null");
+    GWN_REQUIRE(nQ < (int64_t(1) << 31), "at most 2^31-1 queries per call");
+    check_dtype(q_dtype, "Q");
+    check_mem(mem);
+    ensure_device();
+    check_device_of(tree->impl.device);
+    cudaStream_t st = as_stream(stream);
+    StagedBytes dQ(Q, (size_t)nQ * 3 * dtype_size(q_dtype), mem, st);
+    Staged<int32_t> dI(I, (size_t)(nQ * cols), mem, st, false);
+    octree_knn(tree->impl, dQ.dev, q_dtype, nQ, k, dI.dev, st);
+    if (mem == GWN_HOST && nQ * cols) {
+      GWN_CUDA(cudaMemcpyAsync(I, dI.dev, (size_t)(nQ * cols) * 4, cudaMemcpyDeviceToHost, st));
+      GWN_CUDA(cudaStreamSynchronize(st));
+    }
+  });
+}
+
+int gwn_knn(const double* P, int64_t nP, const double* V, int64_t nV, int64_t k, int32_t* I,
+            int mem, void* stream) {
+  return guarded("gwn_knn", [&] {
+    GWN_REQUIRE(nP >= 0 && nV >= 0 && k >= 0, "sizes and k must be non-negative");
+    const int64_t cols = knn_columns(nV, k);
+    GWN_REQUIRE(nP == 0 || cols == 0 || (P && V && I), "P, V and I must be non-null");
+    GWN_REQUIRE(nP < (int64_t(1) << 31), "at most 2^31-1 queries per call");
+    check_mem(mem);
+    ensure_device();
+    if (nP == 0 || cols == 0) return;
+    cudaStream_t st = as_stream(stream);
+    Staged<double> dV(V, (size_t)nV * 3, mem, st);
+    Staged<double> dP(P, (size_t)nP * 3, mem, st);
+    Staged<int32_t> dI(I, (size_t)(nP * cols), mem, st, false);
+    gwn_octree_impl tree;
+    GWN_CUDA(cudaGetDevice(&tree.device));
+    octree_build(tree, dV.dev, nV, true, st);
+    octree_knn(tree, dP.dev, GWN_F64, nP, k, dI.dev, st);
+    if (mem == GWN_HOST)
+      GWN_CUDA(cudaMemcpyAsync(I, dI.dev, (size_t)(nP * cols) * 4, cudaMemcpyDeviceToHost, st));
+    GWN_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
 int gwn_soup_squared_distance(const gwn_soup* soup, const void* Q, int q_dtype, int64_t nQ,
                               double up_sqr_d, double* sqrD, int32_t* I, double* C, int mem,
                               void* stream) {

@@ -1,0 +1,331 @@
+// k nearest points through the octree (igl::knn).
+//
+// Reference: include/igl/knn.cpp:24-136.  For every query row of P the k
+// points of V nearest to it, nearest first; when #V <= k every point, sorted
+// (:41-51).  The reference runs a best-first search over the octree of V with
+// one priority queue of cells and points; the result does not depend on the
+// search, only on the distances (the norm of V.row(j) - p, :86-90) -- and, for
+// equal distances, on the queue's order, which the reference leaves to
+// std::priority_queue.  Here equal distances are ordered by point index (the
+// reference's own test, tests/include/igl/knn.cpp:35-41, has such a tie and
+// expects that order).  As in the reference (:121-125, "leaves either have
+// one point, or none"), a leaf contributes only the first point of its list:
+// duplicates beyond the first (which no octree can separate) are never
+// returned, and a row may then hold fewer than k points (the rest is -1,
+// where the reference's loop would run past its empty queue).  When #V <= k
+// every point is returned, duplicates included (:41-51).
+//
+// One thread per query searches the octree of V depth-first, nearer child
+// first (children ordered by the FP32 distance to their box, rounded outward,
+// minus a slack covering the query's FP32 rounding), skipping empty cells and
+// cells whose lower bound exceeds the k-th distance so far, with the k best
+// (distance, index) pairs in a max-heap; point distances are FP64 with the
+// operations pinned.  For k above kKnnMaxK, or a query whose search stack
+// would overflow (an octree much deeper than any dense cloud gives), a plain
+// scan of all points per query is used instead.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "gwn_common.cuh"
+#include "gwn_internal.cuh"
+#include "octree.cuh"
+
+namespace gwn {
+namespace {
+
+constexpr int kKnnMaxK = 64;
+constexpr int kKnnStack = 192;
+
+struct KnnTree {
+  const double* cn;
+  const double* w;
+  const int32_t* ch;
+  const int64_t* start;
+  const int32_t* count;
+  const int32_t* perm;
+  const double* P;
+  int64_t n;
+  float cmax;
+};
+
+__device__ __forceinline__ double point_dist(const double* __restrict__ P, int32_t j, double qx,
+                                             double qy, double qz) {
+  const double dx = __dsub_rn(P[(int64_t)j * 3], qx), dy = __dsub_rn(P[(int64_t)j * 3 + 1], qy),
+               dz = __dsub_rn(P[(int64_t)j * 3 + 2], qz);
+  return sqrt(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+}
+
+// (d, i) before (e, j) in the result order
+__device__ __forceinline__ bool before(double d, int32_t i, double e, int32_t j) {
+  return d < e || (d == e && i < j);
+}
+
+// Max-heap of the best k (root = the worst kept pair).
+struct Heap {
+  double* d;
+  int32_t* i;
+  int n, k;
+  __device__ void offer(double dd, int32_t ii) {
+    if (n < k) {
+      int c = n++;
+      while (c > 0) {  // sift up
+        const int p = (c - 1) >> 1;
+        if (!before(d[p], i[p], dd, ii)) break;
+        d[c] = d[p];
+        i[c] = i[p];
+        c = p;
+      }
+      d[c] = dd;
+      i[c] = ii;
+      return;
+    }
+    if (!before(dd, ii, d[0], i[0])) return;
+    int c = 0;
+    for (;;) {  // sift down
+      const int l = 2 * c + 1, r = l + 1;
+      int m = c;
+      double md = dd;
+      int32_t mi = ii;
+      if (l < n && before(md, mi, d[l], i[l])) {
+        m = l;
+        md = d[l];
+        mi = i[l];
+      }
+      if (r < n && before(md, mi, d[r], i[r])) m = r;
+      if (m == c) break;
+      d[c] = d[m];
+      i[c] = i[m];
+      c = m;
+    }
+    d[c] = dd;
+    i[c] = ii;
+  }
+  // ascending (d, i) into out
+  __device__ void write_sorted(int32_t* out) {
+    // heap sort in place: repeatedly move the root (max) to the end
+    for (int end = n - 1; end > 0; --end) {
+      const double td = d[0];
+      const int32_t ti = i[0];
+      d[0] = d[end];
+      i[0] = i[end];
+      d[end] = td;
+      i[end] = ti;
+      int c = 0;
+      for (;;) {
+        const int l = 2 * c + 1, r = l + 1;
+        int m = c;
+        if (l < end && before(d[m], i[m], d[l], i[l])) m = l;
+        if (r < end && before(d[m], i[m], d[r], i[r])) m = r;
+        if (m == c) break;
+        const double sd = d[c];
+        const int32_t si = i[c];
+        d[c] = d[m];
+        i[c] = i[m];
+        d[m] = sd;
+        i[m] = si;
+        c = m;
+      }
+    }
+    for (int j = 0; j < n; ++j) out[j] = i[j];
+    for (int j = n; j < k; ++j) out[j] = -1;
+  }
+};
+
+// FP32 lower bound of the distance from q to cell c's cube (centre cn, width
+// w), box rounded outward; minus 1e-6 (S + d) for the query's rounding.
+__device__ __forceinline__ float cell_lower_bound(const KnnTree& t, int c, float fx, float fy,
+                                                  float fz, float S) {
+  const double h = 0.5 * t.w[c];
+  float d2 = 0.f;
+  const float fq[3] = {fx, fy, fz};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const double cc = t.cn[(int64_t)c * 3 + a];
+    const float lo = __double2float_rd(cc - h), hi = __double2float_ru(cc + h);
+    const float e = fmaxf(fmaxf(lo - fq[a], fq[a] - hi), 0.f);
+    d2 = fmaf(e, e, d2);
+  }
+  const float d = sqrtf(d2);
+  return fmaxf(d - 1e-6f * (S + d), 0.f);
+}
+
+template <typename QT>
+__global__ void __launch_bounds__(128) knn_octree_kernel(KnnTree t, const QT* __restrict__ Q,
+                                                         int64_t nQ, int k,
+                                                         int32_t* __restrict__ I,
+                                                         int32_t* __restrict__ overflow,
+                                                         unsigned* __restrict__ n_overflow) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= nQ) return;
+  const double qx = (double)Q[q * 3], qy = (double)Q[q * 3 + 1], qz = (double)Q[q * 3 + 2];
+  const float fx = (float)qx, fy = (float)qy, fz = (float)qz;
+  const float S = fmaxf(fabsf(fx), fmaxf(fabsf(fy), fabsf(fz))) + t.cmax;
+  double hd[kKnnMaxK];
+  int32_t hi[kKnnMaxK];
+  Heap heap{hd, hi, 0, k};
+  int stk[kKnnStack];
+  float slb[kKnnStack];
+  int sp = 0;
+  stk[sp] = 0;
+  slb[sp] = 0.f;
+  ++sp;
+  while (sp > 0) {
+    --sp;
+    const int c = stk[sp];
+    const float lb = slb[sp];
+    if (heap.n == k && (double)lb > heap.d[0]) continue;
+    if (t.ch[(int64_t)c * 8] < 0) {  // leaf: its first point (knn.cpp:121-125)
+      const int32_t p = t.perm[t.start[c]];
+      heap.offer(point_dist(t.P, p, qx, qy, qz), p);
+      continue;
+    }
+    int cc[8];
+    float cl[8];
+    int m = 0;
+    for (int o = 0; o < 8; ++o) {
+      const int x = t.ch[(int64_t)c * 8 + o];
+      if (t.count[x] == 0) continue;
+      const float l = cell_lower_bound(t, x, fx, fy, fz, S);
+      if (heap.n == k && (double)l > heap.d[0]) continue;
+      int j = m++;  // insertion by descending bound: the nearest ends up last (popped first)
+      while (j > 0 && cl[j - 1] < l) {
+        cc[j] = cc[j - 1];
+        cl[j] = cl[j - 1];
+        --j;
+      }
+      cc[j] = x;
+      cl[j] = l;
+    }
+    if (sp + m > kKnnStack) {  // too deep for the stack: scanned separately
+      overflow[atomicAdd(n_overflow, 1u)] = (int32_t)q;
+      return;
+    }
+    for (int j = 0; j < m; ++j) {
+      stk[sp] = cc[j];
+      slb[sp] = cl[j];
+      ++sp;
+    }
+  }
+  heap.write_sorted(I + q * k);
+}
+
+// Every point against query `q` (listed queries, or all when list is null),
+// heap in scratch (k pairs per thread).
+// `rep` (optional): only points flagged 1 take part (the first point of each
+// leaf, as the octree search sees them).
+template <typename QT>
+__global__ void knn_scan_kernel(const double* __restrict__ P, int64_t n, const QT* __restrict__ Q,
+                                int64_t nQ, const int32_t* __restrict__ list,
+                                const unsigned* __restrict__ n_list, int k,
+                                const unsigned char* __restrict__ rep,
+                                double* __restrict__ sd, int32_t* __restrict__ si,
+                                int32_t* __restrict__ I) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t cnt = list ? (int64_t)*n_list : nQ;
+  if (t >= cnt) return;
+  const int64_t q = list ? (int64_t)list[t] : t;
+  const double qx = (double)Q[q * 3], qy = (double)Q[q * 3 + 1], qz = (double)Q[q * 3 + 2];
+  Heap heap{sd + t * (int64_t)k, si + t * (int64_t)k, 0, k};
+  for (int64_t j = 0; j < n; ++j)
+    if (!rep || rep[j]) heap.offer(point_dist(P, (int32_t)j, qx, qy, qz), (int32_t)j);
+  heap.write_sorted(I + q * k);
+}
+
+// rep[p] = 1 for the first point of every non-empty leaf (rep zeroed first).
+__global__ void leaf_first_kernel(const int32_t* __restrict__ ch, const int64_t* __restrict__ start,
+                                  const int32_t* __restrict__ count,
+                                  const int32_t* __restrict__ perm, int64_t ncells,
+                                  unsigned char* __restrict__ rep) {
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= ncells || ch[c * 8] >= 0 || count[c] == 0) return;
+  rep[perm[start[c]]] = 1;
+}
+
+__global__ void max_abs_kernel(const double* __restrict__ P, int64_t n,
+                               unsigned long long* __restrict__ out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double m = 0;
+  if (i < n) m = fmax(fabs(P[i * 3]), fmax(fabs(P[i * 3 + 1]), fabs(P[i * 3 + 2])));
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+
+}  // namespace
+
+int64_t knn_columns(int64_t n, int64_t k) { return std::min<int64_t>(n, k); }
+
+template <typename QT>
+static void knn_t(const gwn_octree_impl& tree, const QT* Q, int64_t nQ, int64_t k, int32_t* I,
+                  cudaStream_t st) {
+  const int64_t kk = knn_columns(tree.n, k);
+  if (nQ == 0 || kk == 0) return;
+  // scratch heaps for the scan path, in batches of at most 256 MB
+  const int64_t batch = std::max<int64_t>(1, std::min<int64_t>(nQ, (int64_t(256) << 20) / (12 * kk)));
+  // the octree search's point set: first points of the leaves (#V > k)
+  DevBuf<unsigned char> rep;
+  if (tree.n > k) {
+    rep.alloc((size_t)tree.n, st);
+    rep.zero(st);
+    launch_kernel(leaf_first_kernel, (unsigned)((tree.ncells + 255) / 256), 256, 0, st,
+                  (const int32_t*)tree.ch.get(), (const int64_t*)tree.start.get(),
+                  (const int32_t*)tree.count.get(), (const int32_t*)tree.perm.get(), tree.ncells,
+                  rep.get());
+  }
+  if (kk > kKnnMaxK || tree.n <= k) {  // scan (every point when #V <= k)
+    DevBuf<double> sd((size_t)(batch * kk), st);
+    DevBuf<int32_t> si((size_t)(batch * kk), st);
+    for (int64_t b = 0; b < nQ; b += batch) {
+      const int64_t m = std::min(batch, nQ - b);
+      launch_kernel(knn_scan_kernel<QT>, (unsigned)((m + 127) / 128), 128, 0, st,
+                    (const double*)tree.P.get(), tree.n, Q + b * 3, m, (const int32_t*)nullptr,
+                    (const unsigned*)nullptr, (int)kk, (const unsigned char*)rep.get(), sd.get(),
+                    si.get(), I + b * kk);
+    }
+    return;
+  }
+  DevBuf<unsigned long long> mx(1, st);
+  mx.zero(st);
+  launch_kernel(max_abs_kernel, (unsigned)((tree.n + 255) / 256), 256, 0, st,
+                (const double*)tree.P.get(), tree.n, mx.get());
+  unsigned long long mxh = 0;
+  GWN_CUDA(cudaMemcpyAsync(&mxh, mx.get(), 8, cudaMemcpyDeviceToHost, st));
+  GWN_CUDA(cudaStreamSynchronize(st));
+  double cmax;
+  std::memcpy(&cmax, &mxh, 8);
+  KnnTree t{tree.cn.get(), tree.w.get(), tree.ch.get(), tree.start.get(), tree.count.get(),
+            tree.perm.get(), tree.P.get(), tree.n, (float)cmax};
+  DevBuf<int32_t> over((size_t)nQ, st);
+  DevBuf<unsigned> nover(1, st);
+  nover.zero(st);
+  launch_kernel(knn_octree_kernel<QT>, (unsigned)((nQ + 127) / 128), 128, 0, st, t, Q, nQ, (int)kk,
+                I, over.get(), nover.get());
+  unsigned no = 0;
+  GWN_CUDA(cudaMemcpyAsync(&no, nover.get(), 4, cudaMemcpyDeviceToHost, st));
+  GWN_CUDA(cudaStreamSynchronize(st));
+  if (no == 0) return;
+  // overflowed queries: scan, in batches of the scratch size
+  const int64_t b2 = std::min<int64_t>(batch, no);
+  DevBuf<double> sd((size_t)(b2 * kk), st);
+  DevBuf<int32_t> si((size_t)(b2 * kk), st);
+  for (int64_t b = 0; b < (int64_t)no; b += b2) {
+    const unsigned m = (unsigned)std::min<int64_t>(b2, (int64_t)no - b);
+    DevBuf<unsigned> nm(1, st);
+    GWN_CUDA(cudaMemcpyAsync(nm.get(), &m, 4, cudaMemcpyHostToDevice, st));
+    launch_kernel(knn_scan_kernel<QT>, (unsigned)((m + 127) / 128), 128, 0, st,
+                  (const double*)tree.P.get(), tree.n, Q, nQ, (const int32_t*)over.get() + b,
+                  (const unsigned*)nm.get(), (int)kk, (const unsigned char*)rep.get(), sd.get(),
+                  si.get(), I);
+    GWN_CUDA(cudaStreamSynchronize(st));  // m lives on this frame
+  }
+}
+
+void octree_knn(const gwn_octree_impl& tree, const void* Q, int q_dtype, int64_t nQ, int64_t k,
+                int32_t* I, cudaStream_t st) {
+  if (q_dtype == GWN_F64) knn_t(tree, static_cast<const double*>(Q), nQ, k, I, st);
+  else knn_t(tree, static_cast<const float*>(Q), nQ, k, I, st);
+}
+
+}  // namespace gwn

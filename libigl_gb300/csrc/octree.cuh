@@ -32,4 +32,10 @@ void octree_build(gwn_octree_impl& t, const double* P, int64_t n, bool host_mode
 void octree_export_csr(const gwn_octree_impl& t, int64_t* pi_offsets, int32_t* pi_indices,
                        cudaStream_t st);
 
+// k nearest octree points of each query (knn.cu): I is nQ x min(k, n) point
+// ids, nearest first, equal distances by index.  Device pointers.
+int64_t knn_columns(int64_t n, int64_t k);
+void octree_knn(const gwn_octree_impl& tree, const void* Q, int q_dtype, int64_t nQ, int64_t k,
+                int32_t* I, cudaStream_t st);
+
 }  // namespace gwn

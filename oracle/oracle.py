@@ -20,7 +20,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "liboracle.so")
 REF_SOUP_PATH = os.path.join(HERE, "_ref", "libref_soup.so")
 
-_SOURCES = ["gwn_oracle.cpp", "soup_port.cpp", "soup_hdk.cpp", "wn_hier.cpp", "distance.cpp", "aabb.cpp"]
+_SOURCES = ["gwn_oracle.cpp", "soup_port.cpp", "soup_hdk.cpp", "wn_hier.cpp", "distance.cpp", "aabb.cpp", "knn.cpp"]
 
 
 def build(force: bool = False) -> str:
@@ -88,6 +88,9 @@ def lib():
             L.oracle_squared_distance.restype = C.c_int
             L.oracle_point_triangle.argtypes = [p, p, p, p, p]
             L.oracle_point_triangle.restype = C.c_double
+        if hasattr(L, "oracle_knn"):
+            L.oracle_knn.argtypes = [p, i64, p, i64, i64, p, p, p, p, p, p, C.c_int]
+            L.oracle_knn.restype = C.c_int
         if hasattr(L, "oracle_aabb_build"):
             L.oracle_aabb_build.argtypes = [p, p, i64]
             L.oracle_aabb_build.restype = p
@@ -385,3 +388,17 @@ class AABB:
             lib().oracle_aabb_free(self._h)
         except Exception:
             pass
+
+
+def knn(P, V, k: int, tree: Octree | None = None, nthreads: int = 0):
+    """igl::knn(P,V,k,point_indices,CH,CN,W,I) restated (knn.cpp): the
+    reference's best-first search over the octree of V."""
+    P, V = _d(P), _d(V)
+    if tree is None:
+        tree = octree(V)
+    cols = min(V.shape[0], int(k))
+    I = np.empty((P.shape[0], cols), np.int32)
+    lib().oracle_knn(_ptr(P), P.shape[0], _ptr(V), V.shape[0], int(k), _ptr(tree.pi_off),
+                     _ptr(tree.pi_idx), _ptr(tree.CH), _ptr(tree.CN), _ptr(tree.W), _ptr(I),
+                     nthreads)
+    return I

@@ -10,6 +10,7 @@
 
 #include <Eigen/Core>
 #include <igl/fast_winding_number.h>
+#include <igl/knn.h>
 #include <igl/octree.h>
 #include <igl/signed_distance.h>
 #include <igl/winding_number.h>
@@ -94,6 +95,23 @@ int main() {
       const double tol = type == igl::SIGNED_DISTANCE_TYPE_FAST_WINDING_NUMBER ? 1e-7 : 1e-15;
       check_near("signed_distance_tet", S(0), std::sqrt(1.0 / 12.0), tol);
     }
+  }
+  // knn (tests/include/igl/knn.cpp:8-73), unit-cube corners
+  {
+    Eigen::MatrixXd Vc(8, 3);
+    Vc.set({0, 0, 1, 0, 1, 0, 0, 1, 1, 0, 0, 0, 1, 0, 0, 1, 1, 0, 1, 1, 1, 1, 0, 1});
+    Eigen::MatrixXd Pc(3, 3);
+    Pc.set({0, 0, 0.6, 0.3, 0.1, 0.2, 0.7, 0.6, 0});
+    std::vector<std::vector<int>> pi;
+    Eigen::MatrixXi ch;
+    Eigen::MatrixXd cn;
+    Eigen::VectorXd w;
+    igl::octree(Vc, pi, ch, cn, w);
+    Eigen::MatrixXi I;
+    igl::knn(Pc, Vc, 3, pi, ch, cn, w, I);
+    const int answer[9] = {0, 3, 2, 3, 4, 0, 5, 4, 1};
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) check_near("knn_unit_cube", I(r, c), answer[r * 3 + c], 0.0);
   }
   std::printf("failures %d\n", failures);
   return failures ? 1 : 0;

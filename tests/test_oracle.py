@@ -213,3 +213,15 @@ def test_aabb_restatement_matches_brute_force():
     # a closest edge or vertex is shared by several triangles (ties), so the
     # indices may differ; the closest points agree
     assert np.abs(Cp - Cb).max() <= 1e-12
+
+
+def test_knn_oracle_golden():
+    """tests/include/igl/knn.cpp:8-73: unit-cube corners (with a distance tie
+    in the first query) and the #V <= k branch."""
+    V = np.array([[0, 0, 1], [0, 1, 0], [0, 1, 1], [0, 0, 0], [1, 0, 0], [1, 1, 0], [1, 1, 1],
+                  [1, 0, 1]], float)
+    P = np.array([[0, 0, 0.6], [0.3, 0.1, 0.2], [.7, .6, 0]])
+    assert np.array_equal(O.knn(P, V, 3), [[0, 3, 2], [3, 4, 0], [5, 4, 1]])
+    V2 = np.array([[0, 0, 0], [1, 1, 1]], float)
+    P2 = np.array([[0, 0, 0], [-1, -1, -1], [2, 2, 2]], float)
+    assert np.array_equal(O.knn(P2, V2, 10), [[0, 1], [0, 1], [1, 0]])
