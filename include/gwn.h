@@ -225,11 +225,13 @@ int gwn_cloud_eval_arrays(const double* P, const double* N, const double* A, int
  * gwn_signed_distance: igl::signed_distance(P,V,F,sign_type,lower_bound,
  * upper_bound,S,I,C,N) (include/igl/signed_distance.h:61-71,
  * signed_distance.cpp:20-137, 372-424) for 3-D triangles.  sign_type takes
- * igl::SignedDistanceType's values; GWN_SD_PSEUDONORMAL is not implemented
- * (GWN_ERR_INVALID_ARGUMENT).  The sign factor is 1 (UNSIGNED),
- * 1 - 2 W with the exact winding number (WINDING_NUMBER, DEFAULT) or
+ * igl::SignedDistanceType's values.  The sign factor is 1 (UNSIGNED),
+ * 1 - 2 W with the exact winding number (WINDING_NUMBER, DEFAULT),
  * 1 - 2 |W| with the soup fast winding number, order 2, accuracy 2
- * (FAST_WINDING_NUMBER); `precision` selects how that W is computed.
+ * (FAST_WINDING_NUMBER; `precision` selects how W is computed), or +-1 from
+ * the angle-weighted pseudonormal of the closest feature (PSEUDONORMAL,
+ * pseudonormal_test.cpp:16-135), whose normal is written to N (#P x 3,
+ * optional: NULL skips it; untouched for the other types).
  * Distances outside the bounds give S = NaN, I = #F + 1, C = 0; an empty F
  * gives S = NaN, I = -1, C = NaN.  The defaults of the reference's
  * bound-less overload are lower_bound = DBL_MIN, upper_bound = DBL_MAX.
@@ -246,8 +248,8 @@ int gwn_soup_squared_distance(const gwn_soup* soup, const void* Q, int q_dtype, 
                               void* stream);
 int gwn_signed_distance(const double* P, int64_t nP, const double* V, int64_t nV,
                         const int32_t* F, int64_t nF, int sign_type, double lower_bound,
-                        double upper_bound, double* S, int32_t* I, double* C, int precision,
-                        int mem, void* stream);
+                        double upper_bound, double* S, int32_t* I, double* C, double* N,
+                        int precision, int mem, void* stream);
 
 /* ------------------------------------------------------------------------
  * Served evaluation (no counterpart in the reference: libigl evaluates one

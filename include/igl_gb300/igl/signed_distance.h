@@ -3,14 +3,13 @@
 // the SignedDistanceType enum and the two igl::signed_distance(P,V,F,...)
 // overloads (signed_distance.h:20-31, 61-90) for 3-D triangle meshes.
 //
-// Same argument meaning and outputs (S #P, I #P, C #P x 3; N untouched since
-// the pseudonormal type is not provided).  SIGNED_DISTANCE_TYPE_PSEUDONORMAL
-// and 2-D inputs throw std::runtime_error.  The sign's winding number is
-// plain FP64 for WINDING_NUMBER / DEFAULT (as the reference) and mixed
-// precision for FAST_WINDING_NUMBER (the reference's is FP32); define
-// IGL_GB300_SD_FWN_PRECISION to change the latter.  The other functions of
-// libigl's signed_distance.h (the pseudonormal and per-point helpers) are not
-// declared here.
+// Same argument meaning and outputs (S #P, I #P, C #P x 3, N #P x 3 for the
+// pseudonormal type).  2-D inputs throw std::runtime_error.  The sign's
+// winding number is plain FP64 for WINDING_NUMBER / DEFAULT (as the
+// reference) and mixed precision for FAST_WINDING_NUMBER (the reference's is
+// FP32); define IGL_GB300_SD_FWN_PRECISION to change the latter.  The other
+// functions of libigl's signed_distance.h (the per-point and tree-taking
+// helpers) are not declared here.
 #ifndef IGL_SIGNED_DISTANCE_H
 #define IGL_SIGNED_DISTANCE_H
 
@@ -48,14 +47,15 @@ inline void signed_distance(const Eigen::MatrixBase<DerivedP>& P,
                             Eigen::PlainObjectBase<DerivedI>& I,
                             Eigen::PlainObjectBase<DerivedC>& C,
                             Eigen::PlainObjectBase<DerivedN>& N) {
-  (void)N;
   if (P.cols() != 3 || V.cols() != 3 || (F.rows() > 0 && F.cols() != 3))
     throw std::runtime_error("igl::signed_distance (GPU drop-in): 3-D triangle meshes only");
   const std::vector<double> p = gwn_detail::rows_f64(P);
   const std::vector<double> v = gwn_detail::rows_f64(V);
   const std::vector<int32_t> f = gwn_detail::rows_i32(F);
   const int64_t n = (int64_t)P.rows();
-  std::vector<double> s((size_t)n), c((size_t)n * 3);
+  std::vector<double> s((size_t)n), c((size_t)n * 3), nn;
+  const bool want_n = sign_type == SIGNED_DISTANCE_TYPE_PSEUDONORMAL;
+  if (want_n) nn.resize((size_t)n * 3);
   std::vector<int32_t> idx((size_t)n);
   const int precision = sign_type == SIGNED_DISTANCE_TYPE_FAST_WINDING_NUMBER
                             ? IGL_GB300_SD_FWN_PRECISION
@@ -63,14 +63,18 @@ inline void signed_distance(const Eigen::MatrixBase<DerivedP>& P,
   gwn_detail::check(gwn_signed_distance(p.data(), n, v.data(), (int64_t)V.rows(), f.data(),
                                         (int64_t)F.rows(), (int)sign_type, (double)lower_bound,
                                         (double)upper_bound, s.data(), idx.data(), c.data(),
-                                        precision, GWN_HOST, nullptr));
+                                        want_n ? nn.data() : nullptr, precision, GWN_HOST,
+                                        nullptr));
   S.resize(n, 1);
   I.resize(n, 1);
   C.resize(n, 3);
+  if (want_n) N.resize(n, 3);
   for (int64_t i = 0; i < n; ++i) {
     S(i) = (typename DerivedS::Scalar)s[(size_t)i];
     I(i) = (typename DerivedI::Scalar)idx[(size_t)i];
     for (int d = 0; d < 3; ++d) C(i, d) = (typename DerivedC::Scalar)c[(size_t)i * 3 + d];
+    if (want_n)
+      for (int d = 0; d < 3; ++d) N(i, d) = (typename DerivedN::Scalar)nn[(size_t)i * 3 + d];
   }
 }
 

@@ -476,7 +476,7 @@ SIGNED_DISTANCE_TYPE_FAST_WINDING_NUMBER = 4
 
 
 def signed_distance(P, V, F, sign_type=SIGNED_DISTANCE_TYPE_DEFAULT, lower_bound=None,
-                    upper_bound=None, precision=None):
+                    upper_bound=None, precision=None, return_normals: bool = False):
     """igl::signed_distance(P,V,F,sign_type,lower_bound,upper_bound,S,I,C,N)
     (include/igl/signed_distance.h:61-71) for 3-D triangles: (S, I, C).
 
@@ -484,6 +484,7 @@ def signed_distance(P, V, F, sign_type=SIGNED_DISTANCE_TYPE_DEFAULT, lower_bound
     ``precision`` selects how the sign's winding number is computed; by
     default plain FP64 for the exact winding number (as the reference) and
     mixed precision for the fast winding number (the reference's is FP32).
+    With ``return_normals`` also N (the pseudonormal type's normals, else 0).
     Host arrays or CUDA torch tensors (all of one kind)."""
     L = N.load()
     Pa = _Arg(P, np.float64)
@@ -500,11 +501,15 @@ def signed_distance(P, V, F, sign_type=SIGNED_DISTANCE_TYPE_DEFAULT, lower_bound
     S = _empty_like_mem(Pa.mem, (n,), np.float64, like=Pa)
     I = _empty_like_mem(Pa.mem, (n,), np.int32, like=Pa)
     Cp = _empty_like_mem(Pa.mem, (n, 3), np.float64, like=Pa)
+    Nm = _empty_like_mem(Pa.mem, (n, 3), np.float64, like=Pa)
+    if sign_type != SIGNED_DISTANCE_TYPE_PSEUDONORMAL:
+        Nm[:] = 0
     stream = _stream_ptr() if Pa.mem == N.GWN_DEVICE else None
     N.check(L.gwn_signed_distance(Pa.ptr, n, Va.ptr, Va.shape[0], Fa.ptr, Fa.shape[0],
                                   int(sign_type), C.c_double(lo), C.c_double(hi), _ptr_of(S),
-                                  _ptr_of(I), _ptr_of(Cp), _prec(precision), Pa.mem, stream))
-    return S, I, Cp
+                                  _ptr_of(I), _ptr_of(Cp), _ptr_of(Nm), _prec(precision),
+                                  Pa.mem, stream))
+    return (S, I, Cp, Nm) if return_normals else (S, I, Cp)
 
 
 # ------------------------------------------------------------- profiling --

@@ -56,8 +56,8 @@ SIGNATURES = {
     "gwn_soup_squared_distance": ([_p, _p, _i, _i64, _d, _p, _p, _p, _i, _p], _i),
     "gwn_octree_knn": ([_p, _p, _i, _i64, _i64, _p, _i, _p], _i),
     "gwn_knn": ([_p, _i64, _p, _i64, _i64, _p, _i, _p], _i),
-    "gwn_signed_distance": ([_p, _i64, _p, _i64, _p, _i64, _i, _d, _d, _p, _p, _p, _i, _i, _p],
-                            _i),
+    "gwn_signed_distance": ([_p, _i64, _p, _i64, _p, _i64, _i, _d, _d, _p, _p, _p, _p, _i, _i,
+                             _p], _i),
     "gwn_server_create": ([_i64, _i64, C.c_int32, _p], _i),
     "gwn_server_add_mesh": ([_p, _p, _i64, _p, _i64, _i, _p], _i),
     "gwn_server_remove_mesh": ([_p, _i64], _i),

@@ -1,11 +1,13 @@
 // Closest triangle and signed distance over a built soup tree.
 //
 // Reference: igl::signed_distance (include/igl/signed_distance.cpp:20-137,
-// 372-440) for 3-D triangle meshes with the sign types UNSIGNED,
-// WINDING_NUMBER / DEFAULT and FAST_WINDING_NUMBER, and the closest-point
+// 372-440) for 3-D triangle meshes with every sign type, and the closest-point
 // query it runs per point, igl::AABB::squared_distance
 // (include/igl/AABB.cpp:1135-1205) with point_simplex_squared_distance
-// (include/igl/point_simplex_squared_distance.cpp:40-124).
+// (include/igl/point_simplex_squared_distance.cpp:40-124), and the
+// PSEUDONORMAL sign: the angle-weighted pseudonormal of the closest feature
+// (pseudonormal_test.cpp:16-135 over per_face_normals, per_vertex_normals
+// with angle weights and per_edge_normals with uniform weights).
 //
 // The reference builds an AABB tree; here the closest-triangle query uses
 // the soup tree that the fast winding number already has, with an FP32 box
@@ -30,6 +32,7 @@
 #include "gwn_common.cuh"
 #include "gwn_internal.cuh"
 #include "soup.cuh"
+#include "sort.cuh"
 
 namespace gwn {
 namespace {
@@ -326,6 +329,204 @@ __global__ void __launch_bounds__(128) closest_dfs_kernel(ClosestParams prm,
   C[qi * 3 + 2] = b.c.z;
 }
 
+// ------------------------------------------------------------ pseudonormal --
+// The normals of SIGNED_DISTANCE_TYPE_PSEUDONORMAL (signed_distance.cpp:
+// 69-76): per_face_normals, per_vertex_normals with angle weights,
+// per_edge_normals with uniform weights; sums in the reference's loop order.
+__device__ __forceinline__ D3 vrow(const double* V, const int32_t* F, int64_t f, int c) {
+  const double* p = V + (int64_t)F[f * 3 + c] * 3;
+  return {p[0], p[1], p[2]};
+}
+__device__ __forceinline__ double dnorm(D3 a) { return sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+
+// per_face_normals.cpp:17-30: (V1-V0) x (V2-V0), normalised; zero stays zero.
+__global__ void face_normals_kernel(const double* __restrict__ V, const int32_t* __restrict__ F,
+                                    int64_t nF, double* __restrict__ FN) {
+  const int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (f >= nF) return;
+  const D3 a = vrow(V, F, f, 0), v1 = dsub(vrow(V, F, f, 1), a), v2 = dsub(vrow(V, F, f, 2), a);
+  D3 n{v1.y * v2.z - v1.z * v2.y, v1.z * v2.x - v1.x * v2.z, v1.x * v2.y - v1.y * v2.x};
+  const double r = dnorm(n);
+  if (r == 0) n = {0, 0, 0};
+  else n = {n.x / r, n.y / r, n.z / r};
+  FN[f * 3] = n.x;
+  FN[f * 3 + 1] = n.y;
+  FN[f * 3 + 2] = n.z;
+}
+
+// internal_angles.cpp:15-38: the corner angle 2 atan(|u1 - u2| / |u1 + u2|)
+// of unit edge vectors; entries keyed for the per-vertex sums.
+__global__ void corner_entries_kernel(const double* __restrict__ V, const int32_t* __restrict__ F,
+                                      int64_t nF, double* __restrict__ angle,
+                                      uint32_t* __restrict__ vkey, int32_t* __restrict__ ventry,
+                                      unsigned long long* __restrict__ ekey,
+                                      int32_t* __restrict__ eentry) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= nF * 3) return;
+  const int64_t f = e / 3;
+  const int j = (int)(e % 3);
+  const D3 x = vrow(V, F, f, (j + 2) % 3), y = vrow(V, F, f, j), z = vrow(V, F, f, (j + 1) % 3);
+  const D3 v1 = dsub(x, y), v2 = dsub(z, y);
+  const double n1 = dnorm(v1), n2 = dnorm(v2);
+  const D3 u1{v1.x / n1, v1.y / n1, v1.z / n1}, u2{v2.x / n2, v2.y / n2, v2.z / n2};
+  const D3 dm{u1.x - u2.x, u1.y - u2.y, u1.z - u2.z}, dp{u1.x + u2.x, u1.y + u2.y, u1.z + u2.z};
+  angle[e] = 2.0 * atan(dnorm(dm) / dnorm(dp));
+  vkey[e] = (uint32_t)F[f * 3 + j];
+  ventry[e] = (int32_t)e;
+  // edge opposite corner j (oriented_facets.cpp: (F1,F2), (F2,F0), (F0,F1))
+  const uint32_t a = (uint32_t)F[f * 3 + (j + 1) % 3], b = (uint32_t)F[f * 3 + (j + 2) % 3];
+  ekey[e] = ((unsigned long long)min(a, b) << 32) | (unsigned long long)max(a, b);
+  eentry[e] = (int32_t)e;
+}
+
+// Segmented sums over sorted entries, in entry order within a segment.
+// mode 0: vertex normals, sum of angle(e) * FN(face(e)); mode 1: edge normals,
+// sum of FN(face(e)).  Each segment start writes its normalised sum to
+// out[seg_id(e)] and, for edges, seg_of[entry] for every entry of the segment.
+template <typename K>
+__global__ void segment_normals_kernel(const K* __restrict__ key, const int32_t* __restrict__ ent,
+                                       int64_t n, const double* __restrict__ angle,
+                                       const double* __restrict__ FN, int mode,
+                                       const uint32_t* __restrict__ seg_index,
+                                       double* __restrict__ out, int32_t* __restrict__ seg_of) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n || (i > 0 && key[i - 1] == key[i])) return;
+  double sx = 0, sy = 0, sz = 0;
+  const int64_t slot = mode == 0 ? (int64_t)key[i] : (int64_t)seg_index[i];
+  for (int64_t j = i; j < n && key[j] == key[i]; ++j) {
+    const int32_t e = ent[j];
+    const int64_t f = e / 3;
+    const double w = mode == 0 ? angle[e] : 1.0;
+    sx += w * FN[f * 3];
+    sy += w * FN[f * 3 + 1];
+    sz += w * FN[f * 3 + 2];
+    if (seg_of) seg_of[e] = (int32_t)slot;
+  }
+  const double r = sqrt(sx * sx + sy * sy + sz * sz);
+  if (r > 0) {
+    sx /= r;
+    sy /= r;
+    sz /= r;
+  }
+  out[slot * 3] = sx;
+  out[slot * 3 + 1] = sy;
+  out[slot * 3 + 2] = sz;
+}
+
+__global__ void segment_start_flags_kernel(const unsigned long long* __restrict__ key, int64_t n,
+                                           uint32_t* __restrict__ flag) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) flag[i] = (i == 0 || key[i - 1] != key[i]) ? 1u : 0u;
+}
+
+// pseudonormal_test.cpp:16-135 at the closest point c of face f.
+__device__ void pseudonormal_sign(const double* __restrict__ V, const int32_t* __restrict__ F,
+                                  int64_t nF, const double* __restrict__ FN,
+                                  const double* __restrict__ VN, const double* __restrict__ EN,
+                                  const int32_t* __restrict__ edge_of, int64_t f, D3 q, D3 c,
+                                  double& s, D3& n) {
+  const D3 A = vrow(V, F, f, 0), B = vrow(V, F, f, 1), Cc = vrow(V, F, f, 2);
+  auto fn = [&](int64_t x) -> D3 { return {FN[x * 3], FN[x * 3 + 1], FN[x * 3 + 2]}; };
+  auto vn = [&](int64_t x) -> D3 { return {VN[x * 3], VN[x * 3 + 1], VN[x * 3 + 2]}; };
+  auto en = [&](int corner) -> D3 {
+    const int64_t e = edge_of[f * 3 + corner];
+    return {EN[e * 3], EN[e * 3 + 1], EN[e * 3 + 2]};
+  };
+  // doublearea of (A, B, C): Kahan's formula on the sorted edge lengths
+  double l0 = dnorm(dsub(B, Cc)), l1 = dnorm(dsub(Cc, A)), l2 = dnorm(dsub(A, B));
+  if (l0 < l1) { const double t = l0; l0 = l1; l1 = t; }
+  if (l1 < l2) { const double t = l1; l1 = l2; l2 = t; }
+  if (l0 < l1) { const double t = l0; l0 = l1; l1 = t; }
+  const double arg = (l0 + (l1 + l2)) * (l2 - (l0 - l1)) * (l2 + (l0 - l1)) * (l0 + (l1 - l2));
+  const double area = 2.0 * 0.25 * sqrt(arg);
+  const double kMinDoubleArea = 1e-4, kEps = 1e-12;
+  bool found = false;
+  if (area > kMinDoubleArea) {
+    // barycentric_coordinates.cpp:57-98
+    const D3 v0 = dsub(B, A), v1 = dsub(Cc, A), v2 = dsub(c, A);
+    const double d00 = ddot(v0, v0), d01 = ddot(v0, v1), d11 = ddot(v1, v1);
+    const double d20 = ddot(v2, v0), d21 = ddot(v2, v1);
+    const double denom = d00 * d11 - d01 * d01;
+    const double b1 = (d11 * d20 - d01 * d21) / denom, b2 = (d00 * d21 - d01 * d20) / denom;
+    const double b[3] = {1.0 - (b1 + b2), b1, b2};
+    const int type = (b[0] <= kEps) + (b[1] <= kEps) + (b[2] <= kEps);
+    if (type == 2) {
+      for (int x = 0; x < 3; ++x)
+        if (b[x] > kEps) {
+          n = vn(F[f * 3 + x]);
+          found = true;
+          break;
+        }
+    } else if (type == 1) {
+      for (int x = 0; x < 3; ++x)
+        if (b[x] <= kEps) {
+          n = en(x);
+          found = true;
+          break;
+        }
+    }
+    if (!found) n = fn(f);
+    found = true;
+  } else {
+    for (int v = 0; v < 3 && !found; ++v)
+      if (dnorm(dsub(c, vrow(V, F, f, v))) < kEps) {
+        n = vn(F[f * 3 + v]);
+        found = true;
+      }
+    for (int e = 0; e < 3 && !found; ++e) {
+      // project_to_line_segment(c, s, d)
+      const D3 S = vrow(V, F, f, (e + 1) % 3), Dd = vrow(V, F, f, (e + 2) % 3);
+      const D3 dms = dsub(Dd, S);
+      const double len2 = ddot(dms, dms);
+      const D3 smp = dsub(S, c);
+      double t = -(dms.x * smp.x + dms.y * smp.y + dms.z * smp.z) / len2;
+      double sq;
+      if (t < 0) {
+        sq = ddot(dsub(c, S), dsub(c, S));
+      } else if (t > 1) {
+        sq = ddot(dsub(c, Dd), dsub(c, Dd));
+      } else {
+        const D3 pp{(1 - t) * S.x + t * Dd.x, (1 - t) * S.y + t * Dd.y, (1 - t) * S.z + t * Dd.z};
+        sq = ddot(dsub(c, pp), dsub(c, pp));
+      }
+      if (sqrt(sq) < kEps) {
+        n = en(e);
+        found = true;
+      }
+    }
+    if (!found) n = fn(f);
+  }
+  s = ddot(dsub(q, c), n) >= 0 ? 1.0 : -1.0;
+}
+
+__global__ void pseudonormal_kernel(const double* __restrict__ P, int64_t nP,
+                                    const double* __restrict__ V, const int32_t* __restrict__ F,
+                                    int64_t nF, const double* __restrict__ FN,
+                                    const double* __restrict__ VN, const double* __restrict__ EN,
+                                    const int32_t* __restrict__ edge_of,
+                                    const double* __restrict__ sqrD, const int32_t* __restrict__ I,
+                                    const double* __restrict__ C, double* __restrict__ sgn,
+                                    double* __restrict__ N) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= nP) return;
+  const int32_t f = I[p];
+  if (f < 0 || f >= nF) {
+    sgn[p] = 1.0;
+    if (N) N[p * 3] = N[p * 3 + 1] = N[p * 3 + 2] = 0.0;
+    return;
+  }
+  double s;
+  D3 n;
+  pseudonormal_sign(V, F, nF, FN, VN, EN, edge_of, f, {P[p * 3], P[p * 3 + 1], P[p * 3 + 2]},
+                    {C[p * 3], C[p * 3 + 1], C[p * 3 + 2]}, s, n);
+  sgn[p] = s;
+  if (N) {
+    N[p * 3] = n.x;
+    N[p * 3 + 1] = n.y;
+    N[p * 3 + 2] = n.z;
+  }
+}
+
 // signed_distance.cpp:96-137: out-of-bounds distances give NaN, F.rows()+1
 // and a zero closest point; otherwise S = s sqrt(sqrD) with s = 1 (unsigned),
 // 1 - 2 W (winding number) or 1 - 2 |W| (fast winding number).
@@ -345,6 +546,7 @@ __global__ void combine_kernel(const double* __restrict__ sqrD, const double* __
   double s = 1.0;
   if (sign_mode == 1) s = 1.0 - 2.0 * W[p];
   else if (sign_mode == 2) s = 1.0 - 2.0 * fabs(W[p]);
+  else if (sign_mode == 3) s = W[p];  // pseudonormal sign
   S[p] = s * sqrt(d2);
 }
 
@@ -401,10 +603,48 @@ void soup_squared_distance(const gwn_soup_impl& s, const void* Q, int q_dtype, i
   }
 }
 
+// Pseudonormal signs (W = +-1) and normals N (nullable) of every query from
+// its closest face I and point C.
+static void pseudonormal_signs(const double* P, int64_t nP, const double* V, int64_t nV,
+                               const int32_t* F, int64_t nF, const int32_t* I, const double* C,
+                               double* sqrD, double* sgn, double* N, cudaStream_t st) {
+  const int64_t ne = nF * 3;
+  auto grid = [](int64_t n) { return (unsigned)std::max<int64_t>(1, (n + 255) / 256); };
+  DevBuf<double> FN((size_t)nF * 3, st), angle((size_t)ne, st), VN((size_t)std::max<int64_t>(nV, 1) * 3, st),
+      EN((size_t)ne * 3, st);
+  DevBuf<uint32_t> vkey((size_t)ne, st), vkey_t((size_t)ne, st), eflag((size_t)ne, st);
+  DevBuf<int32_t> vent((size_t)ne, st), vent_t((size_t)ne, st), eent((size_t)ne, st),
+      eent_t((size_t)ne, st), edge_of((size_t)ne, st);
+  DevBuf<unsigned long long> ekey((size_t)ne, st), ekey_t((size_t)ne, st);
+  launch_kernel(face_normals_kernel, grid(nF), 256, 0, st, V, F, nF, FN.get());
+  launch_kernel(corner_entries_kernel, grid(ne), 256, 0, st, V, F, nF, angle.get(), vkey.get(),
+                vent.get(), ekey.get(), eent.get());
+  int vbits = 1;
+  while (vbits < 32 && (int64_t(1) << vbits) < nV) ++vbits;
+  radix_sort_pairs<uint32_t>(vkey.get(), vent.get(), vkey_t.get(), vent_t.get(), ne, 0,
+                             (vbits + 7) / 8 * 8, st);
+  VN.zero(st);
+  launch_kernel(segment_normals_kernel<uint32_t>, grid(ne), 256, 0, st, (const uint32_t*)vkey.get(),
+                (const int32_t*)vent.get(), ne, (const double*)angle.get(),
+                (const double*)FN.get(), 0, (const uint32_t*)nullptr, VN.get(), (int32_t*)nullptr);
+  radix_sort_pairs<unsigned long long>(ekey.get(), eent.get(), ekey_t.get(), eent_t.get(), ne, 0,
+                                       64, st);
+  launch_kernel(segment_start_flags_kernel, grid(ne), 256, 0, st,
+                (const unsigned long long*)ekey.get(), ne, eflag.get());
+  exclusive_scan_u32(eflag.get(), eflag.get(), ne, st);
+  launch_kernel(segment_normals_kernel<unsigned long long>, grid(ne), 256, 0, st,
+                (const unsigned long long*)ekey.get(), (const int32_t*)eent.get(), ne,
+                (const double*)angle.get(), (const double*)FN.get(), 1,
+                (const uint32_t*)eflag.get(), EN.get(), edge_of.get());
+  launch_kernel(pseudonormal_kernel, grid(nP), 256, 0, st, P, nP, V, F, nF,
+                (const double*)FN.get(), (const double*)VN.get(), (const double*)EN.get(),
+                (const int32_t*)edge_of.get(), (const double*)sqrD, I, C, sgn, N);
+}
+
 void signed_distance_run(const double* P, int64_t nP, const double* V, int64_t nV,
                          const int32_t* F, int64_t nF, int sign_type, double lower_bound,
-                         double upper_bound, double* S, int32_t* I, double* C, int precision,
-                         cudaStream_t st) {
+                         double upper_bound, double* S, int32_t* I, double* C, double* N,
+                         int precision, cudaStream_t st) {
   if (nP == 0) return;
   const unsigned grid = (unsigned)((nP + 255) / 256);
   if (nF == 0) {  // signed_distance.cpp:395-402
@@ -430,6 +670,10 @@ void signed_distance_run(const double* P, int64_t nP, const double* V, int64_t n
     W.alloc((size_t)nP, st);
     soup_eval(tree, 2.0f, P, GWN_F64, nP, W.get(), GWN_F64, precision, st);
     mode = 2;
+  } else if (sign_type == GWN_SD_PSEUDONORMAL) {
+    W.alloc((size_t)nP, st);
+    pseudonormal_signs(P, nP, V, nV, F, nF, I, C, sqrD.get(), W.get(), N, st);
+    mode = 3;
   }
   launch_kernel(combine_kernel, grid, 256, 0, st, (const double*)sqrD.get(),
                 (const double*)W.get(), mode, low_sqr_d, up_sqr_d, nP, nF, S, I, C);

@@ -678,8 +678,8 @@ int gwn_soup_squared_distance(const gwn_soup* soup, const void* Q, int q_dtype, 
 
 int gwn_signed_distance(const double* P, int64_t nP, const double* V, int64_t nV,
                         const int32_t* F, int64_t nF, int sign_type, double lower_bound,
-                        double upper_bound, double* S, int32_t* I, double* C, int precision,
-                        int mem, void* stream) {
+                        double upper_bound, double* S, int32_t* I, double* C, double* N,
+                        int precision, int mem, void* stream) {
   return guarded("gwn_signed_distance", [&] {
     GWN_REQUIRE(nP >= 0 && nV >= 0 && nF >= 0, "sizes must be non-negative");
     GWN_REQUIRE(nP == 0 || (P && S && I && C), "P, S, I and C must be non-null");
@@ -687,8 +687,6 @@ int gwn_signed_distance(const double* P, int64_t nP, const double* V, int64_t nV
     GWN_REQUIRE(nP < (int64_t(1) << 31), "at most 2^31-1 queries per call");
     GWN_REQUIRE(sign_type >= GWN_SD_PSEUDONORMAL && sign_type <= GWN_SD_FAST_WINDING_NUMBER,
                 "sign_type must be one of GWN_SD_*");
-    GWN_REQUIRE(sign_type != GWN_SD_PSEUDONORMAL,
-                "GWN_SD_PSEUDONORMAL is not implemented (use a winding-number sign)");
     check_precision(precision);
     check_mem(mem);
     ensure_device();
@@ -699,12 +697,16 @@ int gwn_signed_distance(const double* P, int64_t nP, const double* V, int64_t nV
     Staged<double> dS(S, (size_t)nP, mem, st, false);
     Staged<int32_t> dI(I, (size_t)nP, mem, st, false);
     Staged<double> dC(C, (size_t)nP * 3, mem, st, false);
+    const bool want_n = N != nullptr && sign_type == GWN_SD_PSEUDONORMAL;
+    Staged<double> dN(want_n ? N : nullptr, want_n ? (size_t)nP * 3 : 0, mem, st, false);
     signed_distance_run(dP.dev, nP, dV.dev, nV, dF.dev, nF, sign_type, lower_bound, upper_bound,
-                        dS.dev, dI.dev, dC.dev, precision, st);
+                        dS.dev, dI.dev, dC.dev, want_n ? dN.dev : nullptr, precision, st);
     if (mem == GWN_HOST && nP) {
       GWN_CUDA(cudaMemcpyAsync(S, dS.dev, (size_t)nP * 8, cudaMemcpyDeviceToHost, st));
       GWN_CUDA(cudaMemcpyAsync(I, dI.dev, (size_t)nP * 4, cudaMemcpyDeviceToHost, st));
       GWN_CUDA(cudaMemcpyAsync(C, dC.dev, (size_t)nP * 24, cudaMemcpyDeviceToHost, st));
+      if (want_n)
+        GWN_CUDA(cudaMemcpyAsync(N, dN.dev, (size_t)nP * 24, cudaMemcpyDeviceToHost, st));
       GWN_CUDA(cudaStreamSynchronize(st));
     }
   });

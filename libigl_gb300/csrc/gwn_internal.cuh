@@ -37,7 +37,7 @@ void run_exact_noalloc(const double* V, int64_t nV, const int32_t* F, int64_t nF
 // synchronizes `st`.
 void signed_distance_run(const double* P, int64_t nP, const double* V, int64_t nV,
                          const int32_t* F, int64_t nF, int sign_type, double lower_bound,
-                         double upper_bound, double* S, int32_t* I, double* C, int precision,
-                         cudaStream_t st);
+                         double upper_bound, double* S, int32_t* I, double* C, double* N,
+                         int precision, cudaStream_t st);
 
 }  // namespace gwn

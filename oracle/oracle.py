@@ -88,6 +88,8 @@ def lib():
             L.oracle_squared_distance.restype = C.c_int
             L.oracle_point_triangle.argtypes = [p, p, p, p, p]
             L.oracle_point_triangle.restype = C.c_double
+            L.oracle_pseudonormal.argtypes = [p, i64, p, i64, p, i64, p, p, p, p]
+            L.oracle_pseudonormal.restype = C.c_int
         if hasattr(L, "oracle_knn"):
             L.oracle_knn.argtypes = [p, i64, p, i64, i64, p, p, p, p, p, p, C.c_int]
             L.oracle_knn.restype = C.c_int
@@ -330,18 +332,20 @@ def squared_distance(V, F, P, up_sqr_d: float = np.inf, nthreads: int = 0):
     return sqrD, I, Cp
 
 
-def signed_distance(P, V, F, sign_type, lower_bound=None, upper_bound=None):
+def signed_distance(P, V, F, sign_type, lower_bound=None, upper_bound=None,
+                    return_normals: bool = False):
     """igl::signed_distance(P,V,F,sign_type,lower,upper,S,I,C,N) for 3-D
     triangles, restating include/igl/signed_distance.cpp:372-424 (dispatch,
-    empty F) and :83-137 (bounds, per-query sign): (S, I, C).  The default
+    empty F) and :83-137 (bounds, per-query sign): (S, I, C) or, with
+    return_normals, (S, I, C, N) (N set for the pseudonormal type).  The default
     bounds are the reference's (numeric_limits min / max, :426-440)."""
     P, V = _d(P), _d(V)
     F = _d(F, np.int32)
     nP = P.shape[0]
     if F.shape[0] == 0:
-        return np.full(nP, np.nan), np.full(nP, -1, np.int32), np.full((nP, 3), np.nan)
-    if sign_type == SIGNED_DISTANCE_TYPE_PSEUDONORMAL:
-        raise NotImplementedError("pseudonormal sign is not restated")
+        out = np.full(nP, np.nan), np.full(nP, -1, np.int32), np.full((nP, 3), np.nan)
+        return out + (np.full((nP, 3), np.nan),) if return_normals else out
+    Nrm = np.zeros((nP, 3))
     lo = np.finfo(np.float64).tiny if lower_bound is None else float(lower_bound)
     hi = np.finfo(np.float64).max if upper_bound is None else float(upper_bound)
     max_abs = max(abs(lo), abs(hi))
@@ -355,6 +359,10 @@ def signed_distance(P, V, F, sign_type, lower_bound=None, upper_bound=None):
         # fast_winding_number(fwn_bvh, 2, q) on the float copy of V (:64-65, 113-116)
         w = SoupPort(V.astype(np.float32).astype(np.float64), F, order=2).eval(P, 2.0)
         s = 1.0 - 2.0 * np.abs(w)
+    elif sign_type == SIGNED_DISTANCE_TYPE_PSEUDONORMAL:
+        s = np.empty(nP)
+        lib().oracle_pseudonormal(_ptr(V), V.shape[0], _ptr(F), F.shape[0], _ptr(P), nP, _ptr(I),
+                                  _ptr(Cp), _ptr(s), _ptr(Nrm))
     else:
         s = np.ones(nP)
     S = s * np.sqrt(sqrD)
@@ -363,7 +371,7 @@ def signed_distance(P, V, F, sign_type, lower_bound=None, upper_bound=None):
     I = I.copy()
     I[out] = F.shape[0] + 1
     Cp[out] = 0.0
-    return S, I, Cp
+    return (S, I, Cp, Nrm) if return_normals else (S, I, Cp)
 
 
 class AABB:

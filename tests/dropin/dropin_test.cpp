@@ -84,9 +84,10 @@ int main() {
   {
     Eigen::MatrixXd Pq(1, 3);
     Pq.set({0.5, 0.5, 0.5});
-    const igl::SignedDistanceType types[4] = {
-        igl::SIGNED_DISTANCE_TYPE_WINDING_NUMBER, igl::SIGNED_DISTANCE_TYPE_DEFAULT,
-        igl::SIGNED_DISTANCE_TYPE_UNSIGNED, igl::SIGNED_DISTANCE_TYPE_FAST_WINDING_NUMBER};
+    const igl::SignedDistanceType types[5] = {
+        igl::SIGNED_DISTANCE_TYPE_PSEUDONORMAL, igl::SIGNED_DISTANCE_TYPE_WINDING_NUMBER,
+        igl::SIGNED_DISTANCE_TYPE_DEFAULT, igl::SIGNED_DISTANCE_TYPE_UNSIGNED,
+        igl::SIGNED_DISTANCE_TYPE_FAST_WINDING_NUMBER};
     for (const auto type : types) {
       Eigen::VectorXd S;
       Eigen::VectorXi I;

@@ -32,15 +32,26 @@ def test_single_tet_golden(cuda):
     """tests/include/igl/signed_distance.cpp:4-42."""
     V, F = _tet()
     P = np.array([[0.5, 0.5, 0.5]])
-    for t, tol in ((G.SIGNED_DISTANCE_TYPE_WINDING_NUMBER, 1e-15),
+    for t, tol in ((G.SIGNED_DISTANCE_TYPE_PSEUDONORMAL, 1e-15),
+                   (G.SIGNED_DISTANCE_TYPE_WINDING_NUMBER, 1e-15),
                    (G.SIGNED_DISTANCE_TYPE_DEFAULT, 1e-15),
                    (G.SIGNED_DISTANCE_TYPE_UNSIGNED, 1e-15),
                    (G.SIGNED_DISTANCE_TYPE_FAST_WINDING_NUMBER, 1e-7)):
         S, I, Cp = G.signed_distance(P, V, F, t)
         assert abs(S[0] - np.sqrt(1 / 12)) <= tol, (t, S)
         assert I[0] == 3 and np.allclose(Cp[0], 1 / 3, atol=1e-15)
-    with pytest.raises(G.GwnError):
-        G.signed_distance(P, V, F, G.SIGNED_DISTANCE_TYPE_PSEUDONORMAL)
+    # pseudonormal inside / outside / at a vertex region, with its normals
+    Q = np.array([[0.5, 0.5, 0.5], [0.1, 0.1, 0.1], [2, 2, 2], [-1, -1, -1], [0.3, -1, 0.3]])
+    S, I, Cp, Nn = G.signed_distance(Q, V, F, G.SIGNED_DISTANCE_TYPE_PSEUDONORMAL,
+                                     return_normals=True)
+    Sr, Ir, Cr, Nr = O.signed_distance(Q, V, F, G.SIGNED_DISTANCE_TYPE_PSEUDONORMAL,
+                                       return_normals=True)
+    assert np.abs(S - Sr).max() <= 1e-15
+    # (0.1, 0.1, 0.1) is equally close to three faces and (-1, -1, -1) to the
+    # vertex they share: the closest face (and for the first the normal)
+    # follows whichever face each side reached first
+    same = I == Ir
+    assert same.sum() >= 3 and np.abs(Nn[same] - Nr[same]).max() <= 1e-15
 
 
 @pytest.fixture(scope="module")
@@ -97,6 +108,23 @@ def test_signed_distance_against_oracle(mesh, cuda):
         S, I, Cp = G.signed_distance(P, V, F, t)
         Sr, Ir, Cr = O.signed_distance(P, V, F, t)
         assert np.abs(S - Sr).max() <= 1e-9 * (1 + np.abs(Sr).max()), t
+    # pseudonormal: the sign follows the closest feature, so a tie in the
+    # closest triangle may pick another feature's normal; compare where the
+    # closest triangles agree, and the magnitude everywhere
+    S, I, Cp, Nn = G.signed_distance(P, V, F, G.SIGNED_DISTANCE_TYPE_PSEUDONORMAL,
+                                     return_normals=True)
+    Sr, Ir, Cr, Nr = O.signed_distance(P, V, F, G.SIGNED_DISTANCE_TYPE_PSEUDONORMAL,
+                                       return_normals=True)
+    assert np.all(np.abs(np.abs(S) - np.abs(Sr)) <= 1e-12 * (1 + np.abs(Sr)))
+    same = I == Ir
+    assert same.mean() > 0.5
+    assert np.array_equal(np.sign(S[same]), np.sign(Sr[same]))
+    assert np.abs(Nn[same] - Nr[same]).max() <= 1e-9
+    # and the pseudonormal sign agrees with the exact winding number's
+    # away from the surface and the holes' rims
+    Sw, _, _ = G.signed_distance(P, V, F, G.SIGNED_DISTANCE_TYPE_WINDING_NUMBER)
+    clear = np.abs(Sw) > 1e-3
+    assert (np.sign(S[clear]) == np.sign(Sw[clear])).mean() > 0.95
     # fast-winding-number sign
     S, I, Cp = G.signed_distance(P, V, F, G.SIGNED_DISTANCE_TYPE_FAST_WINDING_NUMBER)
     Sr, _, _ = O.signed_distance(P, V, F, G.SIGNED_DISTANCE_TYPE_FAST_WINDING_NUMBER)

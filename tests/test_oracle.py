@@ -175,7 +175,8 @@ def test_signed_distance_oracle_single_tet_golden():
     V = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], float)
     F = np.array([[0, 1, 3], [0, 2, 1], [0, 3, 2], [1, 2, 3]], np.int32)
     P = np.array([[0.5, 0.5, 0.5]])
-    for t, tol in ((O.SIGNED_DISTANCE_TYPE_WINDING_NUMBER, 1e-15),
+    for t, tol in ((O.SIGNED_DISTANCE_TYPE_PSEUDONORMAL, 1e-15),
+                   (O.SIGNED_DISTANCE_TYPE_WINDING_NUMBER, 1e-15),
                    (O.SIGNED_DISTANCE_TYPE_DEFAULT, 1e-15),
                    (O.SIGNED_DISTANCE_TYPE_UNSIGNED, 1e-15),
                    (O.SIGNED_DISTANCE_TYPE_FAST_WINDING_NUMBER, 1e-7)):
