@@ -57,7 +57,7 @@ def parse():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--workload", choices=["soup", "exact", "cloud", "precision", "served",
-                                           "signed_distance", "knn"],
+                                           "signed_distance", "knn", "eytzinger2d"],
                     default="soup",
                     help="soup = the headline line; the others are extra measurement lines")
     ap.add_argument("--served-seconds", type=float, default=4.0,
@@ -646,6 +646,127 @@ def run_knn_line(args):
     print(json.dumps(line), flush=True)
 
 
+def run_eytzinger_line(args):
+    """igl::eytzinger_aabb_winding_number (2-D segments): 16 x 16 cells of
+    wavy closed loops, 1M segments, 10M uniform float64 query points.  value =
+    queries/s of the mixed-precision evaluation on device-resident arrays
+    (tree and pairs built once); e2e = the same call from pinned host arrays
+    (points, mesh and tree copied in, W out, every step); plain FP64 and the
+    build (tree + pairs) timed beside it; CPU baseline = the restated
+    reference walk (oracle/eytzinger.cpp) on all host cores, 2M-query sample."""
+    import torch
+    import libigl_gb300 as G
+    from libigl_gb300 import synth
+    from oracle import oracle as O
+    V, E = synth.loops2d(seed=7, n_segments=1_000_000, n_cells=16)
+    P = synth.loops2d_queries(16, seed=8, nq=10_000_000)
+    PB1, PB2 = O.segment_boxes(V, E)
+    stream = torch.cuda.current_stream()
+    dV, dE, dP, dPB1, dPB2 = (torch.from_numpy(x).cuda() for x in (V, E, P, PB1, PB2))
+    tree = {}
+
+    def build():
+        tree["B1"], tree["B2"], tree["leaf"] = G.eytzinger_aabb(dPB1, dPB2)
+        tree["I"], tree["C"] = G.eytzinger_aabb_winding_number_tree(dE, tree["leaf"])
+    build_ms, _ = timed_steps(build, 3, 2, stream)
+    build_ms /= 3
+    out = {}
+
+    def run(prec):
+        def step():
+            out[prec] = G.eytzinger_aabb_winding_number(dP, dV, dE, tree["B1"], tree["B2"],
+                                                        tree["leaf"], tree["I"], tree["C"],
+                                                        precision=prec)
+        return step
+    sampler = ClockSampler(0)
+    sampler.start()
+    time.sleep(0.3)
+    G.profile_enable(True)
+    walk_ms = []
+    for _ in range(max(args.warmup, 3)):
+        run("mixed")()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    ev[0].record(stream)
+    for k in range(args.steps):
+        run("mixed")()
+        ev[k + 1].record(stream)
+        walk_ms.append(G.profile_read().get("walk", float("nan")))
+    torch.cuda.synchronize()
+    total = ev[0].elapsed_time(ev[-1])
+    clocks = sampler.stop()
+    G.profile_enable(False)
+    launches = G.launch_count_of(run("mixed"))
+    fp64_ms, _ = timed_steps(run("fp64"), 2, 1, stream)
+    fp64_ms /= 2
+    Wm, W64 = out["mixed"].cpu().numpy(), out["fp64"].cpu().numpy()
+    err = np.abs(Wm - W64)
+    away = np.abs(W64 - 0.5) > 1e-3
+    nq = P.shape[0]
+    # e2e through the C ABI from pinned host arrays
+    h = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in
+         (("P", P), ("V", V), ("E", E), ("B1", tree["B1"].cpu().numpy()),
+          ("B2", tree["B2"].cpu().numpy()), ("leaf", tree["leaf"].cpu().numpy()),
+          ("I", tree["I"].cpu().numpy()), ("C", tree["C"].cpu().numpy()))}
+    hn = {k: v.numpy() for k, v in h.items()}
+
+    def host_step():
+        out["host"] = G.eytzinger_aabb_winding_number(hn["P"], hn["V"], hn["E"], hn["B1"],
+                                                      hn["B2"], hn["leaf"], hn["I"], hn["C"],
+                                                      precision="mixed")
+    host_step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        host_step()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    h2d = sum(int(v.nbytes) for v in hn.values())
+    # CPU baseline: the reference's build and walk restated, all host cores
+    t0 = time.perf_counter()
+    rB1, rB2, rleaf = O.eytzinger_aabb(PB1, PB2, median_mode=0)
+    rI, rC = O.eytzinger_wn_tree(E, rleaf, canonical=False)
+    cpu_build_s = time.perf_counter() - t0
+    ns = 2_000_000
+    t0 = time.perf_counter()
+    Wr = O.eytzinger_winding_number(P[:ns], V, E, rB1, rB2, rleaf, rI, rC)
+    cpu_s = time.perf_counter() - t0
+    nodes = int(tree["leaf"].shape[0])
+    npairs = int(tree["I"].shape[0]) // 2
+    walk = float(np.nanmean(walk_ms))
+    alg_bytes = nq * (16 + 4 + 8) + nodes * 48 + npairs * 24
+    peaks, peak_kind = load_peaks()
+    achieved = alg_bytes / (walk / 1e3) / 1e9
+    line = {"metric": "2-D winding queries/s (Eytzinger AABB, |dW| <= 1e-4 vs FP64)",
+            "value": nq * args.steps / (total / 1e3), "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic",
+            "config": {"workload": "eytzinger2d_loops_1Mseg_10Mq", "segments": int(E.shape[0]),
+                       "queries": nq, "tree_slots": nodes, "pairs": npairs,
+                       "l2": "inputs larger than L2 (160 MB of queries)"},
+            "e2e": {"value": nq / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": int(nq * 8), "ms_per_step": 1e3 * e2e_s},
+            "plain_fp64": {"value": nq / (fp64_ms / 1e3), "unit": UNIT,
+                           "ratio_mixed_over_fp64": (nq * args.steps / (total / 1e3))
+                           / (nq / (fp64_ms / 1e3))},
+            "build_ms": build_ms,
+            "accuracy": {"max_abs_dW": float(err.max()), "p99_abs_dW": float(np.quantile(err, .99)),
+                         "label_mismatch_outside_band":
+                             int((np.round(Wm) != np.round(W64))[away].sum()),
+                         "fp64_vs_cpu_reference_max": float(np.abs(W64[:ns] - Wr).max()),
+                         "host_call_identical": bool(np.array_equal(out["host"], Wm))},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
+                         "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
+                         "traffic": ncu_traffic("eytzinger_walk_2d"), "peak_source": peak_kind,
+                         "kernel": "eval_mixed_kernel", "kernel_ms": walk,
+                         "algorithmic_bytes": alg_bytes},
+            "clocks": clocks, "gpu_launches": launches,
+            "cpu_baseline": {"value": ns / cpu_s, "unit": UNIT, "cores": O.num_threads(0),
+                             "kind": "port", "build_s": cpu_build_s,
+                             "sample": f"first {ns} queries, the reference's walk restated "
+                                       "(oracle/eytzinger.cpp) over its own tree"}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -658,7 +779,8 @@ def main():
             torch.cuda.set_device(local)
         {"exact": run_exact_line, "cloud": run_cloud_line, "precision": run_precision_study,
          "served": run_served_line,
-         "signed_distance": run_signed_distance_line, "knn": run_knn_line}[args.workload](args)
+         "signed_distance": run_signed_distance_line, "knn": run_knn_line,
+         "eytzinger2d": run_eytzinger_line}[args.workload](args)
         return
     import torch
     import libigl_gb300 as G

@@ -252,6 +252,51 @@ int gwn_signed_distance(const double* P, int64_t nP, const double* V, int64_t nV
                         int precision, int mem, void* stream);
 
 /* ------------------------------------------------------------------------
+ * 2-D winding numbers over an Eytzinger AABB tree of segments (libigl's
+ * hierarchical 2-D path).
+ *
+ * gwn_eytzinger_slots: the tree's slot count for m primitives,
+ * 2^(ceil(log2 m) + 1) (0 for m = 0).
+ *
+ * gwn_eytzinger_aabb: igl::eytzinger_aabb(PB1,PB2,B1,B2,leaf)
+ * (include/igl/eytzinger_aabb.h:24-34, eytzinger_aabb.cpp:16-100).  PB1 / PB2
+ * are the m primitives' min / max corners (m x dim float64, dim 1..3); B1 /
+ * B2 (slots x dim) receive the node boxes, leaf (slots) the primitive of a
+ * leaf, -1 for an internal node, -2 for an empty slot (whose boxes are NaN;
+ * the reference leaves them uninitialised).  Median of the box centres
+ * along the longest axis as the reference, taken as the order statistics.
+ *
+ * gwn_eytzinger_winding_number_tree: igl::eytzinger_aabb_winding_number_tree
+ * (eytzinger_aabb_winding_number_tree.h:22-35, .cpp:17-118) for segments E
+ * (nE x 2 int32) and a tree's leaf array: C (slots + 1) is always written;
+ * I (C[slots] entries) only when non-NULL, so a caller sizes I from C and
+ * calls again.  Each internal node's pairs list its boundary vertices,
+ * positive ones ascending paired with negative ones ascending (the
+ * reference's pairing order is an unordered_map's; the sum is the same).
+ * Synchronizes `stream`.
+ *
+ * gwn_eytzinger_winding_number: igl::eytzinger_aabb_winding_number(p,V,E,
+ * B1,B2,leaf,I,C,wn) (eytzinger_aabb_winding_number.h:25-44, .cpp:9-125)
+ * for nP points P (nP x 2 float64) over V (nV x 2), E, the tree (B1, B2:
+ * slots x 2) and its pairs (I: nI entries, C: slots + 1).  GWN_PLAIN_FP64
+ * follows the reference's walk and arithmetic; GWN_MIXED walks FP32 boxes
+ * with FP32 angles, FP64 for terms within 1e-3 x the root box diagonal and
+ * for results within 1e-3 of 0.5.  Indices out of range set
+ * GWN_STATUS_BAD_INPUT and are skipped.
+ * ---------------------------------------------------------------------- */
+int64_t gwn_eytzinger_slots(int64_t m);
+int gwn_eytzinger_aabb(const double* PB1, const double* PB2, int64_t m, int dim, double* B1,
+                       double* B2, int32_t* leaf, int mem, void* stream);
+int gwn_eytzinger_winding_number_tree(const int32_t* E, int64_t nE, const int32_t* leaf,
+                                      int64_t slots, int32_t* C, int32_t* I, int mem,
+                                      void* stream);
+int gwn_eytzinger_winding_number(const double* P, int64_t nP, const double* V, int64_t nV,
+                                 const int32_t* E, int64_t nE, const double* B1,
+                                 const double* B2, const int32_t* leaf, int64_t slots,
+                                 const int32_t* I, int64_t nI, const int32_t* C, double* W,
+                                 int precision, int mem, void* stream);
+
+/* ------------------------------------------------------------------------
  * Served evaluation (no counterpart in the reference: libigl evaluates one
  * mesh per call).  A server keeps triangle meshes resident on the device as
  * built soup trees and evaluates requests against them, each request being

@@ -33,7 +33,8 @@ __all__ = [
     "fast_winding_number_soup_precompute", "fast_winding_number_soup",
     "Octree", "octree", "CloudExpansion", "fast_winding_number_cloud_precompute",
     "fast_winding_number_cloud", "fast_winding_number_cloud_oneshot", "device_status",
-    "Server", "signed_distance", "knn",
+    "Server", "signed_distance", "knn", "eytzinger_aabb", "eytzinger_aabb_winding_number_tree",
+    "eytzinger_aabb_winding_number",
 ]
 
 _PREC = {"fp64": N.GWN_PLAIN_FP64, "plain": N.GWN_PLAIN_FP64, "mixed": N.GWN_MIXED}
@@ -465,6 +466,69 @@ def knn(P, V, k: int):
     N.check(N.load().gwn_knn(Pa.ptr, Pa.shape[0], Va.ptr, Va.shape[0], int(k), _ptr_of(I),
                              Pa.mem, stream))
     return I
+
+
+# ------------------------------------------- 2-D Eytzinger AABB winding --
+def eytzinger_aabb(PB1, PB2):
+    """igl::eytzinger_aabb(PB1,PB2,B1,B2,leaf) (include/igl/eytzinger_aabb.h):
+    (B1, B2, leaf) of the tree over the m primitive boxes (m x dim corners);
+    empty slots have leaf -2 and NaN boxes.  Host arrays or CUDA tensors."""
+    A1, A2 = _Arg(PB1, np.float64), _Arg(PB2, np.float64)
+    _same_mem(A1, A2)
+    if len(A1.shape) != 2 or A1.shape != A2.shape:
+        raise ValueError("PB1 and PB2 must both be m x dim")
+    m, dim = A1.shape
+    L = N.load()
+    nb = int(L.gwn_eytzinger_slots(m))
+    B1 = _empty_like_mem(A1.mem, (nb, dim), np.float64, like=A1)
+    B2 = _empty_like_mem(A1.mem, (nb, dim), np.float64, like=A1)
+    leaf = _empty_like_mem(A1.mem, (nb,), np.int32, like=A1)
+    stream = _stream_ptr() if A1.mem == N.GWN_DEVICE else None
+    N.check(L.gwn_eytzinger_aabb(A1.ptr, A2.ptr, m, dim, _ptr_of(B1), _ptr_of(B2), _ptr_of(leaf),
+                                 A1.mem, stream))
+    return B1, B2, leaf
+
+
+def eytzinger_aabb_winding_number_tree(E, leaf):
+    """igl::eytzinger_aabb_winding_number_tree(E,leaf,I,C): (I, C), each
+    internal node's boundary-vertex pairs (positive vertices ascending paired
+    with negative vertices ascending)."""
+    Ea = _Arg(E, np.int32, allowed=(np.int32,))
+    La = _Arg(leaf, np.int32, allowed=(np.int32,))
+    _same_mem(Ea, La)
+    nb = La.shape[0]
+    L = N.load()
+    Cc = _empty_like_mem(La.mem, (nb + 1,), np.int32, like=La)
+    stream = _stream_ptr() if La.mem == N.GWN_DEVICE else None
+    nE = Ea.shape[0] if len(Ea.shape) == 2 else 0
+    N.check(L.gwn_eytzinger_winding_number_tree(Ea.ptr, nE, La.ptr, nb, _ptr_of(Cc), None,
+                                                La.mem, stream))
+    total = int(Cc[-1])
+    I = _empty_like_mem(La.mem, (total,), np.int32, like=La)
+    if total:
+        N.check(L.gwn_eytzinger_winding_number_tree(Ea.ptr, nE, La.ptr, nb, _ptr_of(Cc),
+                                                    _ptr_of(I), La.mem, stream))
+    return I, Cc
+
+
+def eytzinger_aabb_winding_number(P, V, E, B1, B2, leaf, I, Cc, precision="mixed"):
+    """igl::eytzinger_aabb_winding_number(p,V,E,B1,B2,leaf,I,C,wn) for every
+    row of P (#P x 2): the winding number of each point with respect to the
+    segments E of V (2-D).  ``precision`` "fp64" follows the reference's
+    arithmetic; "mixed" is FP32 with FP64 where it matters."""
+    Pa, Va, B1a, B2a = (_Arg(x, np.float64) for x in (P, V, B1, B2))
+    Ea, La, Ia, Ca = (_Arg(x, np.int32, allowed=(np.int32,)) for x in (E, leaf, I, Cc))
+    _same_mem(Pa, Va, B1a, B2a, Ea, La, Ia, Ca)
+    if len(Pa.shape) != 2 or Pa.shape[1] != 2 or (Va.shape[0] and Va.shape[1:] != (2,)):
+        raise ValueError("P and V must be #P x 2 / #V x 2")
+    n = Pa.shape[0]
+    W = _empty_like_mem(Pa.mem, (n,), np.float64, like=Pa)
+    stream = _stream_ptr() if Pa.mem == N.GWN_DEVICE else None
+    nE = Ea.shape[0] if len(Ea.shape) == 2 else 0
+    N.check(N.load().gwn_eytzinger_winding_number(
+        Pa.ptr, n, Va.ptr, Va.shape[0], Ea.ptr, nE, B1a.ptr, B2a.ptr, La.ptr, La.shape[0],
+        Ia.ptr, Ia.shape[0], Ca.ptr, _ptr_of(W), _prec(precision), Pa.mem, stream))
+    return W
 
 
 # ------------------------------------------------------- signed distance --

@@ -56,6 +56,11 @@ SIGNATURES = {
     "gwn_soup_squared_distance": ([_p, _p, _i, _i64, _d, _p, _p, _p, _i, _p], _i),
     "gwn_octree_knn": ([_p, _p, _i, _i64, _i64, _p, _i, _p], _i),
     "gwn_knn": ([_p, _i64, _p, _i64, _i64, _p, _i, _p], _i),
+    "gwn_eytzinger_slots": ([_i64], _i64),
+    "gwn_eytzinger_aabb": ([_p, _p, _i64, _i, _p, _p, _p, _i, _p], _i),
+    "gwn_eytzinger_winding_number_tree": ([_p, _i64, _p, _i64, _p, _p, _i, _p], _i),
+    "gwn_eytzinger_winding_number": ([_p, _i64, _p, _i64, _p, _i64, _p, _p, _p, _i64, _p, _i64,
+                                      _p, _p, _i, _i, _p], _i),
     "gwn_signed_distance": ([_p, _i64, _p, _i64, _p, _i64, _i, _d, _d, _p, _p, _p, _p, _i, _i,
                              _p], _i),
     "gwn_server_create": ([_i64, _i64, C.c_int32, _p], _i),

@@ -729,4 +729,100 @@ int gwn_winding_number_noalloc(const double* V, int64_t nV, const int32_t* F, in
   });
 }
 
+int64_t gwn_eytzinger_slots(int64_t m) { return eytzinger_slots(m); }
+
+int gwn_eytzinger_aabb(const double* PB1, const double* PB2, int64_t m, int dim, double* B1,
+                       double* B2, int32_t* leaf, int mem, void* stream) {
+  return guarded("gwn_eytzinger_aabb", [&] {
+    GWN_REQUIRE(m >= 0, "m must be non-negative");
+    GWN_REQUIRE(dim >= 1 && dim <= 3, "dim must be 1, 2 or 3");
+    GWN_REQUIRE(m < (int64_t(1) << 30), "at most 2^30-1 primitives");
+    GWN_REQUIRE(m == 0 || (PB1 && PB2 && B1 && B2 && leaf), "PB1, PB2, B1, B2 and leaf must be non-null");
+    check_mem(mem);
+    ensure_device();
+    if (m == 0) return;
+    cudaStream_t st = as_stream(stream);
+    const int64_t nb = eytzinger_slots(m);
+    Staged<double> dP1(PB1, (size_t)(m * dim), mem, st), dP2(PB2, (size_t)(m * dim), mem, st);
+    Staged<double> dB1(B1, (size_t)(nb * dim), mem, st, false), dB2(B2, (size_t)(nb * dim), mem, st, false);
+    Staged<int32_t> dL(leaf, (size_t)nb, mem, st, false);
+    eytzinger_build(dP1.dev, dP2.dev, m, dim, dB1.dev, dB2.dev, dL.dev, st);
+    if (mem == GWN_HOST) {
+      GWN_CUDA(cudaMemcpyAsync(B1, dB1.dev, (size_t)(nb * dim) * 8, cudaMemcpyDeviceToHost, st));
+      GWN_CUDA(cudaMemcpyAsync(B2, dB2.dev, (size_t)(nb * dim) * 8, cudaMemcpyDeviceToHost, st));
+      GWN_CUDA(cudaMemcpyAsync(leaf, dL.dev, (size_t)nb * 4, cudaMemcpyDeviceToHost, st));
+      GWN_CUDA(cudaStreamSynchronize(st));
+    }
+  });
+}
+
+int gwn_eytzinger_winding_number_tree(const int32_t* E, int64_t nE, const int32_t* leaf,
+                                      int64_t slots, int32_t* C, int32_t* I, int mem,
+                                      void* stream) {
+  return guarded("gwn_eytzinger_winding_number_tree", [&] {
+    GWN_REQUIRE(nE >= 0 && slots >= 0, "sizes must be non-negative");
+    GWN_REQUIRE(C != nullptr, "C must be non-null");
+    GWN_REQUIRE(slots == 0 || leaf, "leaf must be non-null");
+    GWN_REQUIRE(nE == 0 || E, "E must be non-null");
+    GWN_REQUIRE(nE < (int64_t(1) << 30) && slots <= (int64_t(1) << 31),
+                "at most 2^30-1 segments and 2^31 slots");
+    check_mem(mem);
+    ensure_device();
+    cudaStream_t st = as_stream(stream);
+    DeviceStatus status(st, true);
+    Staged<int32_t> dE(E, (size_t)nE * 2, mem, st), dL(leaf, (size_t)slots, mem, st);
+    Staged<int32_t> dC(C, (size_t)slots + 1, mem, st, false);
+    // the pair count is known only after the first pass: host-mode I is
+    // staged after it
+    int64_t total = eytzinger_pairs(dE.dev, nE, dL.dev, slots, dC.dev, nullptr, status.ptr(), st);
+    if (I && total > 0) {
+      Staged<int32_t> dI(I, (size_t)total, mem, st, false);
+      eytzinger_pairs(dE.dev, nE, dL.dev, slots, dC.dev, dI.dev, status.ptr(), st);
+      if (mem == GWN_HOST)
+        GWN_CUDA(cudaMemcpyAsync(I, dI.dev, (size_t)total * 4, cudaMemcpyDeviceToHost, st));
+    }
+    if (mem == GWN_HOST)
+      GWN_CUDA(cudaMemcpyAsync(C, dC.dev, (size_t)(slots + 1) * 4, cudaMemcpyDeviceToHost, st));
+    status.check(st, "eytzinger_winding_number_tree");
+  });
+}
+
+int gwn_eytzinger_winding_number(const double* P, int64_t nP, const double* V, int64_t nV,
+                                 const int32_t* E, int64_t nE, const double* B1,
+                                 const double* B2, const int32_t* leaf, int64_t slots,
+                                 const int32_t* I, int64_t nI, const int32_t* C, double* W,
+                                 int precision, int mem, void* stream) {
+  return guarded("gwn_eytzinger_winding_number", [&] {
+    profile_begin_call();
+    GWN_REQUIRE(nP >= 0 && nV >= 0 && nE >= 0 && slots >= 0 && nI >= 0,
+                "sizes must be non-negative");
+    GWN_REQUIRE(nP == 0 || (P && W), "P and W must be non-null");
+    GWN_REQUIRE(slots == 0 || (B1 && B2 && leaf && C), "B1, B2, leaf and C must be non-null");
+    GWN_REQUIRE(nE == 0 || E, "E must be non-null");
+    GWN_REQUIRE(nV == 0 || V, "V must be non-null");
+    GWN_REQUIRE(nI == 0 || I, "I must be non-null");
+    GWN_REQUIRE(slots == 0 || (slots >= 2 && (slots & (slots - 1)) == 0),
+                "slots must be 0 or a power of two");
+    GWN_REQUIRE(nP < (int64_t(1) << 31), "at most 2^31-1 queries per call");
+    check_precision(precision);
+    check_mem(mem);
+    ensure_device();
+    if (nP == 0) return;
+    cudaStream_t st = as_stream(stream);
+    DeviceStatus status(st, mem == GWN_HOST);
+    Staged<double> dP(P, (size_t)nP * 2, mem, st), dV(V, (size_t)nV * 2, mem, st);
+    Staged<int32_t> dE(E, (size_t)nE * 2, mem, st);
+    Staged<double> dB1(B1, (size_t)slots * 2, mem, st), dB2(B2, (size_t)slots * 2, mem, st);
+    Staged<int32_t> dL(leaf, (size_t)slots, mem, st), dI(I, (size_t)nI, mem, st);
+    Staged<int32_t> dC(C, slots ? (size_t)slots + 1 : 0, mem, st);
+    Staged<double> dW(W, (size_t)nP, mem, st, false);
+    eytzinger_eval(dP.dev, nP, dV.dev, nV, dE.dev, nE, dB1.dev, dB2.dev, dL.dev, slots, dI.dev,
+                   dC.dev, nI, dW.dev, precision, status.ptr(), st);
+    if (mem == GWN_HOST) {
+      GWN_CUDA(cudaMemcpyAsync(W, dW.dev, (size_t)nP * 8, cudaMemcpyDeviceToHost, st));
+      status.check(st, "eytzinger_winding_number");
+    }
+  });
+}
+
 }  // extern "C"

@@ -40,4 +40,17 @@ void signed_distance_run(const double* P, int64_t nP, const double* V, int64_t n
                          double upper_bound, double* S, int32_t* I, double* C, double* N,
                          int precision, cudaStream_t st);
 
+// Eytzinger AABB tree of segments (eytzinger.cu); device pointers.
+int64_t eytzinger_slots(int64_t m);
+void eytzinger_build(const double* PB1, const double* PB2, int64_t m, int dim, double* B1,
+                     double* B2, int32_t* leaf, cudaStream_t st);
+// Writes C (slots + 1) and, when I is non-null, I; returns C[slots].
+// Synchronizes `st`.
+int64_t eytzinger_pairs(const int32_t* E, int64_t nE, const int32_t* leaf, int64_t nb, int32_t* C,
+                        int32_t* I, unsigned* status, cudaStream_t st);
+void eytzinger_eval(const double* P, int64_t nP, const double* V, int64_t nV, const int32_t* E,
+                    int64_t nE, const double* B1, const double* B2, const int32_t* leaf,
+                    int64_t nb, const int32_t* I, const int32_t* C, int64_t nI, double* W,
+                    int precision, unsigned* status, cudaStream_t st);
+
 }  // namespace gwn

@@ -11,6 +11,8 @@ input specification):
 * torus_cloud: area-uniform torus samples with jittered normals and areas.
 * exact_workload / soup_workload / cloud_workload / precision_workload /
   served_meshes: the five benchmark configurations.
+* loops2d / loops2d_queries: closed wavy 2-D polygons (outer loops, holes
+  and doubled loops) for the 2-D segment winding number.
 """
 from __future__ import annotations
 
@@ -323,3 +325,43 @@ def served_mesh(spec):
     if spec["hole"]:
         F = delete_patch(F, rng, max(1, F.shape[0] // 100))
     return V, F
+
+
+def loops2d(seed: int = 7, n_segments: int = 1_000_000, n_cells: int = 16):
+    """Closed 2-D polylines on an n_cells x n_cells grid of unit cells.  Cell k
+    holds an outer counter-clockwise loop (radius 0.4) and, for k % 3 == 1, a
+    clockwise hole (radius 0.18), for k % 3 == 2 a second counter-clockwise
+    loop (radius 0.18, winding number 2 inside).  Radii carry a wave
+    r(t) = r0 (1 + 0.15 sin(5t + phase) + 0.04 sin(23t)).  Segments are split
+    between loops in proportion to their radius.  Returns V (#V x 2 float64)
+    and E (#E x 2 int32), each loop's vertices consecutive."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for k in range(n_cells * n_cells):
+        cx, cy = k % n_cells + 0.5, k // n_cells + 0.5
+        specs.append((cx, cy, 0.4, 1.0))
+        if k % 3 == 1:
+            specs.append((cx, cy, 0.18, -1.0))
+        elif k % 3 == 2:
+            specs.append((cx, cy, 0.18, 1.0))
+    radii = np.array([sp[2] for sp in specs])
+    counts = np.maximum(8, np.floor(n_segments * radii / radii.sum())).astype(np.int64)
+    counts[0] += max(0, n_segments - int(counts.sum()))
+    Vs, Es, base = [], [], 0
+    for (cx, cy, r0, orient), n in zip(specs, counts):
+        t = np.arange(n) * (2 * np.pi / n)
+        ph = rng.uniform(0, 2 * np.pi)
+        r = r0 * (1 + 0.15 * np.sin(5 * t + ph) + 0.04 * np.sin(23 * t))
+        V = np.stack([cx + r * np.cos(t), cy + orient * r * np.sin(t)], axis=1)
+        idx = np.arange(n)
+        Es.append(np.stack([base + idx, base + (idx + 1) % n], axis=1))
+        Vs.append(V)
+        base += n
+    return np.concatenate(Vs), np.concatenate(Es).astype(np.int32)
+
+
+def loops2d_queries(n_cells: int = 16, seed: int = 8, nq: int = 10_000_000):
+    """Uniform query points over the cells' square, grown by 5% per side."""
+    rng = np.random.default_rng(seed)
+    lo, hi = -0.05 * n_cells, 1.05 * n_cells
+    return rng.uniform(lo, hi, (nq, 2))

@@ -20,7 +20,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "liboracle.so")
 REF_SOUP_PATH = os.path.join(HERE, "_ref", "libref_soup.so")
 
-_SOURCES = ["gwn_oracle.cpp", "soup_port.cpp", "soup_hdk.cpp", "wn_hier.cpp", "distance.cpp", "aabb.cpp", "knn.cpp"]
+_SOURCES = ["gwn_oracle.cpp", "soup_port.cpp", "soup_hdk.cpp", "wn_hier.cpp", "distance.cpp", "aabb.cpp", "knn.cpp", "eytzinger.cpp"]
 
 
 def build(force: bool = False) -> str:
@@ -98,6 +98,13 @@ def lib():
             L.oracle_aabb_build.restype = p
             L.oracle_aabb_free.argtypes = [p]
             L.oracle_aabb_squared_distance.argtypes = [p, p, i64, C.c_double, p, p, p, C.c_int]
+        if hasattr(L, "oracle_eytzinger_aabb"):
+            L.oracle_eytzinger_slots.argtypes = [i64]
+            L.oracle_eytzinger_slots.restype = i64
+            L.oracle_eytzinger_aabb.argtypes = [p, p, i64, C.c_int, C.c_int, p, p, p]
+            L.oracle_eytzinger_wn_tree.argtypes = [p, p, i64, C.c_int, p, p]
+            L.oracle_eytzinger_wn.argtypes = [p, i64, p, p, p, p, p, i64, p, p, p, C.c_int]
+            L.oracle_segments_wn.argtypes = [p, i64, p, p, i64, p]
         if hasattr(L, "oracle_winding_number_hier"):
             L.oracle_winding_number_hier.argtypes = [p, i64, p, i64, p, i64, p, C.c_int]
             L.oracle_winding_number_hier.restype = C.c_int
@@ -410,3 +417,60 @@ def knn(P, V, k: int, tree: Octree | None = None, nthreads: int = 0):
                      _ptr(tree.pi_idx), _ptr(tree.CH), _ptr(tree.CN), _ptr(tree.W), _ptr(I),
                      nthreads)
     return I
+
+
+def _i(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def eytzinger_aabb(PB1, PB2, median_mode: int = 0):
+    """igl::eytzinger_aabb(PB1,PB2,B1,B2,leaf) restated (eytzinger_aabb.cpp);
+    median_mode 0 = the reference's igl::median, 1 = exact order statistics.
+    Empty slots hold NaN boxes."""
+    PB1, PB2 = _d(PB1), _d(PB2)
+    m, dim = PB1.shape
+    nb = int(lib().oracle_eytzinger_slots(m))
+    B1 = np.empty((nb, dim)); B2 = np.empty((nb, dim)); leaf = np.empty(nb, np.int32)
+    lib().oracle_eytzinger_aabb(_ptr(PB1), _ptr(PB2), m, dim, median_mode, _ptr(B1), _ptr(B2),
+                                _ptr(leaf))
+    return B1, B2, leaf
+
+
+def eytzinger_wn_tree(E, leaf, canonical: bool = True):
+    """igl::eytzinger_aabb_winding_number_tree(E,leaf,I,C) restated; canonical
+    sorts each node's positive and negative vertex lists (the reference's
+    order is that of an unordered_map)."""
+    E, leaf = _i(E), _i(leaf)
+    nb = leaf.shape[0]
+    Cc = np.empty(nb + 1, np.int32)
+    lib().oracle_eytzinger_wn_tree(_ptr(E), _ptr(leaf), nb, int(canonical), _ptr(Cc), None)
+    I = np.empty(int(Cc[-1]), np.int32)
+    lib().oracle_eytzinger_wn_tree(_ptr(E), _ptr(leaf), nb, int(canonical), _ptr(Cc), _ptr(I))
+    return I, Cc
+
+
+def eytzinger_winding_number(P, V, E, B1, B2, leaf, I, Cc, nthreads: int = 0):
+    """igl::eytzinger_aabb_winding_number(p,V,E,B1,B2,leaf,I,C,wn) restated,
+    for every row of P."""
+    P, V, B1, B2 = _d(P), _d(V), _d(B1), _d(B2)
+    E, leaf, I, Cc = _i(E), _i(leaf), _i(I), _i(Cc)
+    W = np.empty(P.shape[0])
+    lib().oracle_eytzinger_wn(_ptr(P), P.shape[0], _ptr(V), _ptr(E), _ptr(B1), _ptr(B2),
+                              _ptr(leaf), leaf.shape[0], _ptr(I), _ptr(Cc), _ptr(W), nthreads)
+    return W
+
+
+def segments_winding_number(P, V, E):
+    """Direct sum of atan2(cross, dot)/(2 pi) over every segment."""
+    P, V, E = _d(P), _d(V), _i(E)
+    W = np.empty(P.shape[0])
+    lib().oracle_segments_wn(_ptr(P), P.shape[0], _ptr(V), _ptr(E), E.shape[0], _ptr(W))
+    return W
+
+
+def segment_boxes(V, E):
+    """Per-segment min / max corners (the PB1, PB2 a caller passes to
+    eytzinger_aabb)."""
+    V, E = _d(V), _i(E)
+    A, B = V[E[:, 0]], V[E[:, 1]]
+    return np.minimum(A, B), np.maximum(A, B)

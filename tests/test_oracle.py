@@ -135,12 +135,12 @@ def test_soup_port_reproduces_reference_fixtures_bit_for_bit():
 
 
 def test_pair_atan2_polynomial_in_fp32():
-    """The FP32 atan2 of the exact kernel's pair terms (exact.cu,
-    atan2_pairs): its coefficients, evaluated in float32 with the kernel's
+    """The FP32 atan2 of the FP32 angle terms (atan2f.cuh, atan2_pairs, used
+    by the exact 3-D sum and the 2-D tree walk): its coefficients, evaluated in float32 with the kernel's
     octant reduction, stay within a few ulp of atan2 everywhere."""
     import re
     src = open(os.path.join(os.path.dirname(__file__), "..", "libigl_gb300", "csrc",
-                            "exact.cu")).read()
+                            "atan2f.cuh")).read()
     body = src[src.index("float atan2_pairs("):]
     body = body[:body.index("\n}\n")]
     coef = [np.float32(float(x)) for x in
@@ -226,3 +226,72 @@ def test_knn_oracle_golden():
     V2 = np.array([[0, 0, 0], [1, 1, 1]], float)
     P2 = np.array([[0, 0, 0], [-1, -1, -1], [2, 2, 2]], float)
     assert np.array_equal(O.knn(P2, V2, 10), [[0, 1], [0, 1], [1, 0]])
+
+
+# ------------------------------------------------- 2-D Eytzinger AABB tree --
+def _eytz_cases():
+    from libigl_gb300 import synth
+    rng = np.random.default_rng(11)
+    cases = {}
+    cases["loops"] = synth.loops2d(n_segments=3000, n_cells=3)
+    n = 1500  # random grid polygon: repeated coordinates, self-intersections
+    g = rng.integers(0, 40, (n, 2)).astype(float)
+    cases["grid"] = (g, np.c_[np.arange(n), (np.arange(n) + 1) % n].astype(np.int32))
+    t = np.linspace(0, 3 * np.pi, 400)  # open spiral
+    cases["open"] = (np.c_[t * np.cos(t), t * np.sin(t)] / 10,
+                     np.c_[np.arange(399), np.arange(1, 400)].astype(np.int32))
+    # a vertex shared by six segments (two triangles and a bow-tie through 0),
+    # a zero-length segment and a duplicated segment
+    V = np.array([[0, 0], [1, 0], [1, 1], [-1, 0], [-1, -1], [0, 1], [0, -1], [.5, .5]], float)
+    E = np.array([[0, 1], [1, 2], [2, 0], [0, 3], [3, 4], [4, 0], [0, 5], [5, 6], [6, 0],
+                  [7, 7], [1, 2]], np.int32)
+    cases["nonmanifold"] = (V, E)
+    return cases
+
+
+def test_eytzinger_oracle_equals_direct_sum():
+    """The hierarchy (eytzinger_aabb_winding_number.cpp:66-110) returns the
+    direct sum over every segment (the same per-term formula) for closed,
+    open, self-intersecting and non-manifold inputs, with the reference's
+    pairing order and with the canonical one."""
+    rng = np.random.default_rng(12)
+    for name, (V, E) in _eytz_cases().items():
+        lo, hi = V.min(0), V.max(0)
+        P = rng.uniform(lo - 0.1 * (hi - lo), hi + 0.1 * (hi - lo), (800, 2))
+        Wd = O.segments_winding_number(P, V, E)
+        B1, B2, leaf = O.eytzinger_aabb(*O.segment_boxes(V, E), median_mode=0)
+        for canonical in (False, True):
+            I, Cc = O.eytzinger_wn_tree(E, leaf, canonical=canonical)
+            assert Cc[0] == 0 and np.all(np.diff(Cc) % 2 == 0)
+            W = O.eytzinger_winding_number(P, V, E, B1, B2, leaf, I, Cc)
+            np.testing.assert_allclose(W, Wd, rtol=0, atol=1e-12, err_msg=name)
+
+
+def test_eytzinger_oracle_known_answers():
+    """Unit square: 1 inside counter-clockwise, -1 clockwise, 0 outside; a
+    point on a vertex adds atan2(0, 0) = 0 for its two segments."""
+    V = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], float)
+    E = np.array([[0, 1], [1, 2], [2, 3], [3, 0]], np.int32)
+    P = np.array([[.5, .5], [2, .5], [-.1, -.1], [.25, .75]])
+    for orient, want in ((E, [1, 0, 0, 1]), (E[:, ::-1].copy(), [-1, 0, 0, -1])):
+        B1, B2, leaf = O.eytzinger_aabb(*O.segment_boxes(V, orient))
+        assert leaf.shape == (8,) and list(leaf[:3]) == [-1, -1, -1]
+        I, Cc = O.eytzinger_wn_tree(orient, leaf)
+        W = O.eytzinger_winding_number(P, V, orient, B1, B2, leaf, I, Cc)
+        np.testing.assert_allclose(W, want, atol=1e-15)
+
+
+def test_eytzinger_median_forms_agree():
+    """igl::median's two nth_element calls (median.cpp:14-35) against the
+    order statistics: the same tree on distinct centre coordinates; with
+    repeated coordinates any difference leaves the winding numbers equal."""
+    for name, (V, E) in _eytz_cases().items():
+        PB1, PB2 = O.segment_boxes(V, E)
+        a = O.eytzinger_aabb(PB1, PB2, median_mode=0)
+        b = O.eytzinger_aabb(PB1, PB2, median_mode=1)
+        if name in ("loops", "open"):
+            assert np.array_equal(a[2], b[2]), name
+        P = np.random.default_rng(13).uniform(V.min(0) - .1, V.max(0) + .1, (300, 2))
+        Wa = O.eytzinger_winding_number(P, V, E, a[0], a[1], a[2], *O.eytzinger_wn_tree(E, a[2]))
+        Wb = O.eytzinger_winding_number(P, V, E, b[0], b[1], b[2], *O.eytzinger_wn_tree(E, b[2]))
+        np.testing.assert_allclose(Wa, Wb, atol=1e-12, err_msg=name)
