@@ -688,10 +688,12 @@ def run_eytzinger_line(args):
     torch.cuda.synchronize()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     ev[0].record(stream)
+    phases = {}
     for k in range(args.steps):
         run("mixed")()
         ev[k + 1].record(stream)
-        walk_ms.append(G.profile_read().get("walk", float("nan")))
+        phases = G.profile_read()
+        walk_ms.append(phases.get("walk", float("nan")))
     torch.cuda.synchronize()
     total = ev[0].elapsed_time(ev[-1])
     clocks = sampler.stop()
@@ -748,7 +750,7 @@ def run_eytzinger_line(args):
             "plain_fp64": {"value": nq / (fp64_ms / 1e3), "unit": UNIT,
                            "ratio_mixed_over_fp64": (nq * args.steps / (total / 1e3))
                            / (nq / (fp64_ms / 1e3))},
-            "build_ms": build_ms,
+            "build_ms": build_ms, "phases_ms_last_step": phases,
             "accuracy": {"max_abs_dW": float(err.max()), "p99_abs_dW": float(np.quantile(err, .99)),
                          "label_mismatch_outside_band":
                              int((np.round(Wm) != np.round(W64))[away].sum()),

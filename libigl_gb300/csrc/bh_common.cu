@@ -1,5 +1,6 @@
-// Query ordering for the Barnes-Hut walks: 30-bit Morton keys inside the
-// tree's bounding box, stable radix sort, permutation handed to the walk.
+// Query ordering for the Barnes-Hut walks: queries grouped by their cell of a
+// 256^3 Morton grid over the tree's bounding box (one counting pass), the
+// permutation handed to the walk.
 #include <cuda_runtime.h>
 
 #include "bh_common.cuh"
@@ -12,7 +13,7 @@ constexpr int64_t kMinOrdered = 8192;  // smaller batches are walked in input or
 
 template <typename QT>
 __global__ void query_keys_kernel(const QT* __restrict__ Q, int64_t n, float3 lo, float3 inv,
-                                  uint32_t* __restrict__ keys, int32_t* __restrict__ idx) {
+                                  uint32_t* __restrict__ keys) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float x = (float)Q[i * 3 + 0], y = (float)Q[i * 3 + 1], z = (float)Q[i * 3 + 2];
@@ -21,9 +22,9 @@ __global__ void query_keys_kernel(const QT* __restrict__ Q, int64_t n, float3 lo
     t = fminf(fmaxf(t, 0.f), 1023.f);  // NaN -> 0 via fmaxf
     return (uint32_t)t;
   };
-  keys[i] = (spread10(q(x, lo.x, inv.x)) << 2) | (spread10(q(y, lo.y, inv.y)) << 1) |
-            spread10(q(z, lo.z, inv.z));
-  idx[i] = (int32_t)i;
+  // the cell of 256^3 over the box: the top 24 bits of the 30-bit Morton code
+  keys[i] = ((spread10(q(x, lo.x, inv.x)) << 2) | (spread10(q(y, lo.y, inv.y)) << 1) |
+             spread10(q(z, lo.z, inv.z))) >> 6;
 }
 
 }  // namespace
@@ -43,18 +44,16 @@ void order_queries(const void* Q, int q_dtype, int64_t nQ, const double lo[3], c
   l = make_float3((float)(c[0] - h[0]), (float)(c[1] - h[1]), (float)(c[2] - h[2]));
   inv = make_float3((float)(1024.0 / (2 * h[0])), (float)(1024.0 / (2 * h[1])),
                     (float)(1024.0 / (2 * h[2])));
-  DevBuf<uint32_t> keys((size_t)nQ, st), keys_tmp((size_t)nQ, st);
-  DevBuf<int32_t> tmp((size_t)nQ, st);
+  DevBuf<uint32_t> keys((size_t)nQ, st);
   out.perm.alloc((size_t)nQ, st);
   const unsigned grid = (unsigned)((nQ + 255) / 256);
   if (q_dtype == GWN_F64)
-    launch_kernel(query_keys_kernel<double>, grid, 256, 0, st, static_cast<const double*>(Q), nQ, l, inv,
-                                                   keys.get(), out.perm.get());
+    launch_kernel(query_keys_kernel<double>, grid, 256, 0, st, static_cast<const double*>(Q), nQ,
+                  l, inv, keys.get());
   else
-    launch_kernel(query_keys_kernel<float>, grid, 256, 0, st, static_cast<const float*>(Q), nQ, l, inv,
-                                                  keys.get(), out.perm.get());
-  GWN_CUDA(cudaGetLastError());
-  radix_sort_pairs<uint32_t>(keys.get(), out.perm.get(), keys_tmp.get(), tmp.get(), nQ, 0, 30, st);
+    launch_kernel(query_keys_kernel<float>, grid, 256, 0, st, static_cast<const float*>(Q), nQ,
+                  l, inv, keys.get());
+  bucket_order(keys.get(), nQ, 1u << 24, out.perm.get(), st);
   out.active = true;
 }
 

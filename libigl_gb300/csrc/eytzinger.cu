@@ -23,14 +23,16 @@
 // vertices ascending, paired in order with negative vertices ascending (the
 // reference pairs in unordered_map order; any pairing gives the same sum).
 //
-// Evaluation.  One thread per query (Morton-ordered), a stackless walk of the
-// implicit tree in the reference's visiting order (right child first).  FP64
-// form: the reference's arithmetic on the caller's arrays.  Mixed form: FP32
+// Evaluation.  One thread per query (grouped by Morton cell), a stackless
+// walk of the implicit tree in the reference's visiting order (right child
+// first); the mixed walk moves warp by warp.  FP64 form: the reference's
+// arithmetic on the caller's arrays.  Mixed form: FP32
 // boxes rounded outward (a box test may only say "outside" when the query is
-// outside), FP32 segment / pair endpoints relative to the root box centre,
-// FP32 angle summed with compensation; a term whose segment passes within
-// 1e-3 x the root box diagonal of the query is evaluated in FP64, and a
-// result within 1e-3 of 0.5 is evaluated again in FP64.
+// outside), segment / pair endpoints and the query as hi + lo FP32 pairs in a
+// frame centred on the root box, FP32 angle summed with compensation; FP64
+// only for a term whose FP32 angle may be off by 2 pi (query almost on the
+// segment) or whose query sits on an endpoint, and again for a result within
+// 1e-3 of 0.5.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -553,23 +555,52 @@ __global__ void eval64_kernel(EvalTree T, const double* __restrict__ P, int64_t 
   W[q] = eval64(T, P[2 * q], P[2 * q + 1], status);
 }
 
-// Mixed-precision node: box relative to the centre (rounded outward), and
-// for a leaf its segment's endpoints; meta = (leaf, a | c0, b | c1, 0).
+// Mixed-precision frame: coordinates relative to the root box centre c,
+// scaled by a power of two so the root box diagonal is in [0.5, 1] (exact,
+// and FP32 stays far from overflow and underflow for any input scale).
+// Vertices and queries are held as hi + lo FP32 pairs (x = hi + lo to ~2^-48
+// relative), so a difference V - p is accurate to FP32 rounding of the
+// difference itself however close V and p are.
+struct Frame {
+  double cx, cy, scale;
+};
+__device__ __forceinline__ void split_coord(double x, float& hi, float& lo) {
+  hi = (float)x;
+  lo = (float)(x - (double)hi);
+}
+
+// Node: box in the frame (rounded outward), for a leaf its segment's
+// endpoints (hi, lo); meta = (leaf, a | c0, b | c1, 0).
 struct NodeF {
   float4 box;
-  float4 seg;
+  float4 shi;
+  float4 slo;
   int4 meta;
 };
+struct PairF {
+  float4 hi;
+  float4 lo;
+};
 
-__global__ void prep_nodes_kernel(EvalTree T, double cx, double cy, NodeF* __restrict__ nodes,
+__device__ __forceinline__ void seg_hilo(const double* V, int64_t a, int64_t b, const Frame& f,
+                                         float4& hi, float4& lo) {
+  split_coord((V[2 * a] - f.cx) * f.scale, hi.x, lo.x);
+  split_coord((V[2 * a + 1] - f.cy) * f.scale, hi.y, lo.y);
+  split_coord((V[2 * b] - f.cx) * f.scale, hi.z, lo.z);
+  split_coord((V[2 * b + 1] - f.cy) * f.scale, hi.w, lo.w);
+}
+
+__global__ void prep_nodes_kernel(EvalTree T, Frame f, NodeF* __restrict__ nodes,
                                   unsigned* status) {
   const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r >= T.nb) return;
   NodeF nd;
   const int32_t lf = T.leaf[r];
-  nd.box = make_float4(__double2float_rd(T.B1[2 * r] - cx), __double2float_rd(T.B1[2 * r + 1] - cy),
-                       __double2float_ru(T.B2[2 * r] - cx), __double2float_ru(T.B2[2 * r + 1] - cy));
-  nd.seg = make_float4(0.f, 0.f, 0.f, 0.f);
+  nd.box = make_float4(__double2float_rd((T.B1[2 * r] - f.cx) * f.scale),
+                       __double2float_rd((T.B1[2 * r + 1] - f.cy) * f.scale),
+                       __double2float_ru((T.B2[2 * r] - f.cx) * f.scale),
+                       __double2float_ru((T.B2[2 * r + 1] - f.cy) * f.scale));
+  nd.shi = nd.slo = make_float4(0.f, 0.f, 0.f, 0.f);
   nd.meta = make_int4(lf, 0, 0, 0);
   if (lf >= 0) {
     int64_t a = -1, b = -1;
@@ -581,8 +612,7 @@ __global__ void prep_nodes_kernel(EvalTree T, double cx, double cy, NodeF* __res
       atomicOr(status, kStatusBadInput);
       nd.meta = make_int4(-3, 0, 0, 0);  // skipped by the walk
     } else {
-      nd.seg = make_float4((float)(T.V[2 * a] - cx), (float)(T.V[2 * a + 1] - cy),
-                           (float)(T.V[2 * b] - cx), (float)(T.V[2 * b + 1] - cy));
+      seg_hilo(T.V, a, b, f, nd.shi, nd.slo);
       nd.meta = make_int4(lf, (int)a, (int)b, 0);
     }
   } else if (lf == -1) {
@@ -597,8 +627,8 @@ __global__ void prep_nodes_kernel(EvalTree T, double cx, double cy, NodeF* __res
   nodes[r] = nd;
 }
 
-// Pair i: both endpoints relative to the centre; (ida, idb) for FP64 terms.
-__global__ void prep_pairs_kernel(EvalTree T, double cx, double cy, float4* __restrict__ pf,
+// Pair i: both endpoints in the frame (hi, lo); (ida, idb) for FP64 terms.
+__global__ void prep_pairs_kernel(EvalTree T, Frame f, PairF* __restrict__ pf,
                                   int2* __restrict__ pid, int64_t npairs, unsigned* status) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= npairs) return;
@@ -607,30 +637,30 @@ __global__ void prep_pairs_kernel(EvalTree T, double cx, double cy, float4* __re
     atomicOr(status, kStatusBadInput);
     a = b = 0;  // a zero-length pair adds nothing
   }
-  pf[i] = make_float4((float)(T.V[2 * a] - cx), (float)(T.V[2 * a + 1] - cy),
-                      (float)(T.V[2 * b] - cx), (float)(T.V[2 * b + 1] - cy));
+  PairF pr;
+  seg_hilo(T.V, a, b, f, pr.hi, pr.lo);
+  pf[i] = pr;
   pid[i] = make_int2((int)a, (int)b);
 }
 
 struct MixedTree {
   const NodeF* nodes;
-  const float4* pf;
+  const PairF* pf;
   const int2* pid;
   const double* V;
   int64_t nb;
-  double cx, cy;
-  float e2;  // (near distance)^2
+  Frame f;
 };
 
-// True when the segment (a, b), given relative to the query, passes within
-// sqrt(e2) of it.
-__device__ __forceinline__ bool near_seg(float x0, float y0, float x1, float y1, float cr, float dt,
-                                         float e2) {
-  const float l0 = fmaf(x0, x0, y0 * y0), l1 = fmaf(x1, x1, y1 * y1);
-  if (l0 < e2 || l1 < e2) return true;
-  const float len2 = l0 + l1 - 2.f * dt;
-  return dt < fminf(l0, l1) && cr * cr < e2 * len2;
-}
+// An FP32 angle term is trusted unless (a) the query is within 1e-9 of the
+// frame's scale of an endpoint, or (b) the angle is near +-pi (dot < 0) with
+// |cross| <= 8 u |v0||v1| (u = 2^-24): there rounding may flip the sign of
+// the cross product and the angle by 2 pi.  Elsewhere the error of the
+// computed angle is a few u (the differences are accurate to u, the cross
+// and dot products to 2u |v0||v1|), independent of the distance to the
+// segment.
+constexpr float kTiny2 = 1e-18f;
+constexpr float kTau2 = 64.f * 5.9604645e-8f * 5.9604645e-8f;
 
 // Compensated FP32 sum (Neumaier): a walk can add thousands of angles of up
 // to pi each (dense self-intersecting curves), which a plain FP32 sum rounds
@@ -646,16 +676,26 @@ struct Sum32 {
   __device__ __forceinline__ double value() const { return (double)s + (double)c; }
 };
 
-__device__ __forceinline__ void term_mixed(const MixedTree& T, float4 s, int a, int b, float qx,
-                                           float qy, double px, double py, Sum32& acc,
-                                           double& acc64) {
-  const float x0 = s.x - qx, y0 = s.y - qy, x1 = s.z - qx, y1 = s.w - qy;
+__device__ __forceinline__ void term_mixed(const MixedTree& T, float4 h, float4 l, int a, int b,
+                                           float2 qh, float2 ql, double px, double py,
+                                           Sum32& acc, double& acc64) {
+  const float x0 = (h.x - qh.x) + (l.x - ql.x), y0 = (h.y - qh.y) + (l.y - ql.y);
+  const float x1 = (h.z - qh.x) + (l.z - ql.x), y1 = (h.w - qh.y) + (l.w - ql.y);
   const float cr = x0 * y1 - y0 * x1;
   const float dt = fmaf(x0, x1, y0 * y1);
-  if (near_seg(x0, y0, x1, y1, cr, dt, T.e2)) acc64 += seg_angle64(T.V, a, b, px, py);
-  else acc.add(atan2_pairs(cr, dt));
+  const float l0 = fmaf(x0, x0, y0 * y0), l1 = fmaf(x1, x1, y1 * y1);
+  if (fminf(l0, l1) < kTiny2 || (dt < 0.f && cr * cr <= kTau2 * (l0 * l1)))
+    acc64 += seg_angle64(T.V, a, b, px, py);
+  else
+    acc.add(atan2_pairs(cr, dt));
 }
 
+// Warp-coherent walk: the lanes of a warp (Morton-ordered queries) share the
+// walk position r.  At an internal node each active lane outside the box adds
+// the node's pairs (all such lanes read the same pairs) and waits for the
+// walk to come back out of the subtree (at walk_next(r)); the warp descends
+// if any active lane is inside.  Every lane adds exactly the terms, in the
+// same order, of its own walk.
 __global__ void __launch_bounds__(kT) eval_mixed_kernel(MixedTree T, const double* __restrict__ P,
                                                         int64_t nP,
                                                         const int32_t* __restrict__ perm,
@@ -663,31 +703,48 @@ __global__ void __launch_bounds__(kT) eval_mixed_kernel(MixedTree T, const doubl
                                                         int32_t* __restrict__ redo,
                                                         uint32_t* __restrict__ nredo) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= nP) return;
-  const int64_t q = perm ? perm[i] : i;
-  const double px = P[2 * q], py = P[2 * q + 1];
-  const float qx = (float)(px - T.cx), qy = (float)(py - T.cy);
+  const bool valid = i < nP;
+  const int64_t q = valid ? (perm ? perm[i] : i) : 0;
+  const double px = valid ? P[2 * q] : 0.0, py = valid ? P[2 * q + 1] : 0.0;
+  float2 qh, ql;
+  split_coord((px - T.f.cx) * T.f.scale, qh.x, ql.x);
+  split_coord((py - T.f.cy) * T.f.scale, qh.y, ql.y);
   Sum32 acc;
   double acc64 = 0.0;
+  bool active = valid;
+  int64_t resume = -1;
   int64_t r = T.nb > 0 ? 0 : -1;
   while (r >= 0) {
-    const float4 box = __ldg(&T.nodes[r].box);
-    const int4 meta = __ldg(&T.nodes[r].meta);
+    if (resume == r) active = true;
+    const NodeF* nd = T.nodes + r;
+    const int4 meta = __ldg(&nd->meta);
     if (meta.x >= 0) {
-      term_mixed(T, __ldg(&T.nodes[r].seg), meta.y, meta.z, qx, qy, px, py, acc, acc64);
+      if (active)
+        term_mixed(T, __ldg(&nd->shi), __ldg(&nd->slo), meta.y, meta.z, qh, ql, px, py, acc,
+                   acc64);
       r = walk_next(r);
-    } else if (meta.x != -1) {
-      r = walk_next(r);
-    } else if (qx < box.x || qx > box.z || qy < box.y || qy > box.w) {
-      for (int k = meta.y; k < meta.z; k += 2) {
-        const int2 id = __ldg(&T.pid[k >> 1]);
-        term_mixed(T, __ldg(&T.pf[k >> 1]), id.x, id.y, qx, qy, px, py, acc, acc64);
-      }
-      r = walk_next(r);
-    } else {
-      r = 2 * r + 2;
+      continue;
     }
+    if (meta.x != -1) {
+      r = walk_next(r);
+      continue;
+    }
+    const float4 box = __ldg(&nd->box);
+    const bool outside =
+        active && (qh.x < box.x || qh.x > box.z || qh.y < box.y || qh.y > box.w);
+    const int64_t after = walk_next(r);
+    if (outside) {
+      for (int k = meta.y; k < meta.z; k += 2) {
+        const PairF* pr = T.pf + (k >> 1);
+        const int2 id = __ldg(&T.pid[k >> 1]);
+        term_mixed(T, __ldg(&pr->hi), __ldg(&pr->lo), id.x, id.y, qh, ql, px, py, acc, acc64);
+      }
+      active = false;
+      resume = after;
+    }
+    r = __any_sync(0xffffffffu, active) ? 2 * r + 2 : after;
   }
+  if (!valid) return;
   const double w = (acc.value() + acc64) / kTwoPi;
   W[q] = w;
   if (fabs(w - 0.5) < 1e-3) redo[atomicAdd(nredo, 1u)] = (int32_t)q;
@@ -703,8 +760,8 @@ __global__ void redo64_kernel(EvalTree T, const double* __restrict__ P,
   }
 }
 
-__device__ __forceinline__ uint32_t spread16(uint32_t x) {
-  x &= 0xffffu;
+__device__ __forceinline__ uint32_t spread10(uint32_t x) {
+  x &= 0x3ffu;
   x = (x | (x << 8)) & 0x00ff00ffu;
   x = (x | (x << 4)) & 0x0f0f0f0fu;
   x = (x | (x << 2)) & 0x33333333u;
@@ -713,17 +770,15 @@ __device__ __forceinline__ uint32_t spread16(uint32_t x) {
 }
 
 __global__ void keys2_kernel(const double* __restrict__ P, int64_t n, double lx, double ly,
-                             double sx, double sy, uint32_t* __restrict__ key,
-                             int32_t* __restrict__ idx) {
+                             double sx, double sy, uint32_t* __restrict__ key) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
   auto qz = [](double v, double l, double s) -> uint32_t {
     double t = (v - l) * s;
-    t = fmin(fmax(t, 0.0), 65535.0);  // NaN -> 0
+    t = fmin(fmax(t, 0.0), 1023.0);  // NaN -> 0
     return (uint32_t)t;
   };
-  key[i] = (spread16(qz(P[2 * i + 1], ly, sy)) << 1) | spread16(qz(P[2 * i], lx, sx));
-  idx[i] = (int32_t)i;
+  key[i] = (spread10(qz(P[2 * i + 1], ly, sy)) << 1) | spread10(qz(P[2 * i], lx, sx));
 }
 
 void scan_into(const uint32_t* in, uint32_t* out, int64_t n, cudaStream_t st) {
@@ -891,12 +946,12 @@ void eytzinger_eval(const double* P, int64_t nP, const double* V, int64_t nV, co
     PhaseTimer ph("order_queries", st);
     GWN_REQUIRE(nP < (int64_t(1) << 31), "at most 2^31-1 queries per call");
     const double hx = 0.625 * ex + 1e-300, hy = 0.625 * ey + 1e-300;
-    DevBuf<uint32_t> key((size_t)nP, st), key_tmp((size_t)nP, st);
-    DevBuf<int32_t> tmp((size_t)nP, st);
+    DevBuf<uint32_t> key((size_t)nP, st);
     perm.alloc((size_t)nP, st);
-    launch_kernel(keys2_kernel, nblk(nP), kT, 0, st, P, nP, cx - hx, cy - hy, 65536.0 / (2 * hx),
-                  65536.0 / (2 * hy), key.get(), perm.get());
-    radix_sort_pairs<uint32_t>(key.get(), perm.get(), key_tmp.get(), tmp.get(), nP, 0, 32, st);
+    // 1024 x 1024 Morton cells over the root box (grown 25%)
+    launch_kernel(keys2_kernel, nblk(nP), kT, 0, st, P, nP, cx - hx, cy - hy, 1024.0 / (2 * hx),
+                  1024.0 / (2 * hy), key.get());
+    bucket_order(key.get(), nP, 1u << 20, perm.get(), st);
   }
   if (precision == GWN_PLAIN_FP64) {
     PhaseTimer ph("walk", st);
@@ -905,17 +960,20 @@ void eytzinger_eval(const double* P, int64_t nP, const double* V, int64_t nV, co
   }
   const int64_t npairs = nI / 2;
   DevBuf<NodeF> nodes((size_t)nb, st);
-  DevBuf<float4> pf((size_t)std::max<int64_t>(npairs, 1), st);
+  DevBuf<PairF> pf((size_t)std::max<int64_t>(npairs, 1), st);
   DevBuf<int2> pid((size_t)std::max<int64_t>(npairs, 1), st);
+  const double diag = std::sqrt(ex * ex + ey * ey);
+  int e2 = 0;
+  if (diag > 0 && std::isfinite(diag)) std::frexp(diag, &e2);  // diag = f * 2^e2, f in [0.5, 1)
+  const Frame frame{cx, cy, std::ldexp(1.0, -e2)};
   {
     PhaseTimer ph("prep", st);
-    launch_kernel(prep_nodes_kernel, nblk(nb), kT, 0, st, T, cx, cy, nodes.get(), status);
+    launch_kernel(prep_nodes_kernel, nblk(nb), kT, 0, st, T, frame, nodes.get(), status);
     if (npairs)
-      launch_kernel(prep_pairs_kernel, nblk(npairs), kT, 0, st, T, cx, cy, pf.get(), pid.get(),
+      launch_kernel(prep_pairs_kernel, nblk(npairs), kT, 0, st, T, frame, pf.get(), pid.get(),
                     npairs, status);
   }
-  const double diag = std::sqrt(ex * ex + ey * ey);
-  MixedTree M{nodes.get(), pf.get(), pid.get(), V, nb, cx, cy, (float)(1e-6 * diag * diag)};
+  MixedTree M{nodes.get(), pf.get(), pid.get(), V, nb, frame};
   DevBuf<int32_t> redo((size_t)nP, st);
   DevBuf<uint32_t> nredo(1, st);
   nredo.zero(st);

@@ -162,7 +162,32 @@ __global__ void __launch_bounds__(kRsThreads) rs_scatter_kernel(
   }
 }
 
+__global__ void bucket_rank_kernel(const uint32_t* __restrict__ keys, int64_t n,
+                                   uint32_t* __restrict__ cnt, uint32_t* __restrict__ rank) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) rank[i] = atomicAdd(&cnt[keys[i]], 1u);
+}
+
+__global__ void bucket_place_kernel(const uint32_t* __restrict__ keys, int64_t n,
+                                    const uint32_t* __restrict__ off,
+                                    const uint32_t* __restrict__ rank, int32_t* __restrict__ perm) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) perm[off[keys[i]] + rank[i]] = (int32_t)i;
+}
+
 }  // namespace
+
+void bucket_order(const uint32_t* keys, int64_t n, uint32_t nbuckets, int32_t* perm,
+                  cudaStream_t st) {
+  if (n <= 0) return;
+  GWN_REQUIRE(n < (int64_t(1) << 31), "bucket order: at most 2^31-1 elements");
+  DevBuf<uint32_t> cnt((size_t)nbuckets, st), rank((size_t)n, st);
+  cnt.zero(st);
+  const unsigned grid = (unsigned)((n + 255) / 256);
+  launch_kernel(bucket_rank_kernel, grid, 256, 0, st, keys, n, cnt.get(), rank.get());
+  exclusive_scan_u32(cnt.get(), cnt.get(), nbuckets, st);
+  launch_kernel(bucket_place_kernel, grid, 256, 0, st, keys, n, cnt.get(), rank.get(), perm);
+}
 
 int64_t scan_scratch_elems(int64_t n) {
   int64_t total = 0;

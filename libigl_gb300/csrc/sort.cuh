@@ -24,6 +24,14 @@ template <typename K>
 void radix_sort_pairs(K* keys, int32_t* vals, K* keys_tmp, int32_t* vals_tmp, int64_t n,
                       int begin_bit, int end_bit, cudaStream_t st);
 
+// Groups n keys (each < nbuckets) by value, ascending, in one counting pass:
+// perm[k] is the input index of the k-th element.  The order inside a bucket
+// is whatever order the atomics were served in (not stable), which suits
+// query ordering for coherence: every walk here gives each query the same
+// result whatever its neighbours in the warp.
+void bucket_order(const uint32_t* keys, int64_t n, uint32_t nbuckets, int32_t* perm,
+                  cudaStream_t st);
+
 // Graph-capturable variant for 32-bit keys: sorts the first min(cap, *n_dev)
 // elements (n_dev is device memory, read when the kernels run) with caller
 // scratch (radix_sort_scratch_elems(cap)); an even number of 8-bit passes,

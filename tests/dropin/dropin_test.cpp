@@ -10,6 +10,9 @@
 
 #include <Eigen/Core>
 #include <igl/fast_winding_number.h>
+#include <igl/eytzinger_aabb.h>
+#include <igl/eytzinger_aabb_winding_number.h>
+#include <igl/eytzinger_aabb_winding_number_tree.h>
 #include <igl/knn.h>
 #include <igl/octree.h>
 #include <igl/signed_distance.h>
@@ -113,6 +116,38 @@ int main() {
     const int answer[9] = {0, 3, 2, 3, 4, 0, 5, 4, 1};
     for (int r = 0; r < 3; ++r)
       for (int c = 0; c < 3; ++c) check_near("knn_unit_cube", I(r, c), answer[r * 3 + c], 0.0);
+  }
+  // 2-D Eytzinger AABB winding number: unit square, counter-clockwise
+  {
+    Eigen::MatrixXd V2(4, 2);
+    V2.set({0, 0, 1, 0, 1, 1, 0, 1});
+    Eigen::MatrixXi E2(4, 2);
+    E2.set({0, 1, 1, 2, 2, 3, 3, 0});
+    Eigen::MatrixXd PB1(4, 2), PB2(4, 2);
+    for (int e = 0; e < 4; ++e)
+      for (int d = 0; d < 2; ++d) {
+        const double a = V2(E2(e, 0), d), b = V2(E2(e, 1), d);
+        PB1(e, d) = a < b ? a : b;
+        PB2(e, d) = a < b ? b : a;
+      }
+    Eigen::MatrixXd B1, B2;
+    Eigen::VectorXi leaf, I, C;
+    igl::eytzinger_aabb(PB1, PB2, B1, B2, leaf);
+    check_near("eytzinger_slots", (double)leaf.rows(), 8, 0);
+    igl::eytzinger_aabb_winding_number_tree(E2, leaf, I, C);
+    check_near("eytzinger_C_rows", (double)C.rows(), 9, 0);
+    Eigen::MatrixXd p(1, 2);
+    p.set({0.5, 0.5});
+    double wn = 0;
+    igl::eytzinger_aabb_winding_number(p, V2, E2, B1, B2, leaf, I, C, wn);
+    check_near("eytzinger_wn_inside", wn, 1.0, 1e-15);
+    Eigen::MatrixXd Pq(3, 2);
+    Pq.set({0.5, 0.5, 2, 0.5, 0.25, 0.75});
+    Eigen::VectorXd Wq;
+    igl::eytzinger_aabb_winding_number(Pq, V2, E2, B1, B2, leaf, I, C, Wq);
+    check_near("eytzinger_wn_batch0", Wq(0), 1.0, 1e-6);
+    check_near("eytzinger_wn_batch1", Wq(1), 0.0, 1e-6);
+    check_near("eytzinger_wn_batch2", Wq(2), 1.0, 1e-6);
   }
   std::printf("failures %d\n", failures);
   return failures ? 1 : 0;
