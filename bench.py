@@ -57,7 +57,7 @@ def parse():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--workload", choices=["soup", "exact", "cloud", "precision", "served",
-                                           "signed_distance", "knn", "eytzinger2d"],
+                                           "signed_distance", "knn", "eytzinger2d", "swept"],
                     default="soup",
                     help="soup = the headline line; the others are extra measurement lines")
     ap.add_argument("--served-seconds", type=float, default=4.0,
@@ -681,22 +681,20 @@ def run_eytzinger_line(args):
     sampler = ClockSampler(0)
     sampler.start()
     time.sleep(0.3)
-    G.profile_enable(True)
-    walk_ms = []
     for _ in range(max(args.warmup, 3)):
         run("mixed")()
     torch.cuda.synchronize()
+    G.profile_enable(True, accumulate=True)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     ev[0].record(stream)
-    phases = {}
     for k in range(args.steps):
         run("mixed")()
         ev[k + 1].record(stream)
-        phases = G.profile_read()
-        walk_ms.append(phases.get("walk", float("nan")))
     torch.cuda.synchronize()
     total = ev[0].elapsed_time(ev[-1])
     clocks = sampler.stop()
+    phases = {k: v / args.steps for k, v in G.profile_read().items()}
+    walk_ms = [phases.get("walk", float("nan"))]
     G.profile_enable(False)
     launches = G.launch_count_of(run("mixed"))
     fp64_ms, _ = timed_steps(run("fp64"), 2, 1, stream)
@@ -750,7 +748,7 @@ def run_eytzinger_line(args):
             "plain_fp64": {"value": nq / (fp64_ms / 1e3), "unit": UNIT,
                            "ratio_mixed_over_fp64": (nq * args.steps / (total / 1e3))
                            / (nq / (fp64_ms / 1e3))},
-            "build_ms": build_ms, "phases_ms_last_step": phases,
+            "build_ms": build_ms, "phases_ms_per_step": phases,
             "accuracy": {"max_abs_dW": float(err.max()), "p99_abs_dW": float(np.quantile(err, .99)),
                          "label_mismatch_outside_band":
                              int((np.round(Wm) != np.round(W64))[away].sum()),
@@ -769,6 +767,82 @@ def run_eytzinger_line(args):
     print(json.dumps(line), flush=True)
 
 
+def run_swept_line(args):
+    """igl::swept_volume_signed_distance: a 20,480-triangle deformed ellipsoid
+    under 64 rigid motions of a screw, a 128 x 69 x 60 grid (529,920 points)
+    around the sweep, isolevel 0, sign SIGNED_DISTANCE_TYPE_DEFAULT (exact
+    winding number).  value = grid-point evaluations per second (#GV x
+    #transforms / s) of the device call on device arrays (tree built inside,
+    as the reference does; the sign's exact winding number in mixed
+    precision, plain FP64 timed beside it); e2e = the same call from host
+    arrays; CPU
+    baseline = the restated reference loop (oracle.swept_volume_signed_
+    distance: AABB, exact winding number, flood fill) on the first 4
+    transforms, all host cores; accuracy = GPU vs that restatement on the
+    same 4 transforms."""
+    import torch
+    import libigl_gb300 as G
+    from libigl_gb300 import synth
+    from oracle import oracle as O
+    V, F, T, GV, res, h = synth.swept_workload()
+    sign = G.SIGNED_DISTANCE_TYPE_DEFAULT
+    dV, dF, dGV = (torch.from_numpy(x).cuda() for x in (V, F, GV))
+    stream = torch.cuda.current_stream()
+    out = {}
+
+    def step():
+        out["S"] = G.swept_volume_signed_distance(dV, dF, T, sign, dGV, res, h, 0.0)
+    steps = min(args.steps, 5)
+    G.profile_enable(True)
+    total, per = timed_steps(step, steps, max(args.warmup, 1), stream)
+    phases = G.profile_read()  # the last sweep's phases
+    G.profile_enable(False)
+    launches = G.launch_count_of(step)
+    nG, nT = GV.shape[0], T.shape[0]
+    t0 = time.perf_counter()
+    Sh = G.swept_volume_signed_distance(V, F, T, sign, GV, res, h, 0.0)
+    e2e_s = time.perf_counter() - t0
+    k = 4
+    S4 = G.swept_volume_signed_distance(V, F, T[:k], sign, GV, res, h, 0.0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    S4_64 = G.swept_volume_signed_distance(dV, dF, T[:k], sign, dGV, res, h, 0.0,
+                                           precision="fp64").cpu().numpy()
+    fp64_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    Sr = O.swept_volume_signed_distance(V, F, T[:k], sign, GV, res, h, 0.0)
+    cpu_s = time.perf_counter() - t0
+    rel = np.abs(S4 - Sr) / np.maximum(np.abs(Sr), 1e-12)
+    rel64 = np.abs(S4_64 - Sr) / np.maximum(np.abs(Sr), 1e-12)
+    line = {"metric": "swept-volume grid-point evaluations/s (#GV x #transforms / s)",
+            "value": nG * nT * steps / (total / 1e3), "unit": "evaluations/s", "n_gpus": 1,
+            "steps": steps, "warmup": max(args.warmup, 1), "ms_per_step": total / steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": "swept_ellipsoid20k_64T_grid128", "triangles": int(F.shape[0]),
+                       "transforms": int(nT), "grid": [int(x) for x in res],
+                       "grid_points": int(nG), "h": h, "isolevel": 0.0,
+                       "sign_type": "DEFAULT (exact winding number)"},
+            "e2e": {"value": nG * nT / e2e_s, "unit": "evaluations/s",
+                    "h2d_bytes_per_step": int(V.nbytes + F.nbytes + GV.nbytes + T.nbytes),
+                    "d2h_bytes_per_step": int(nG * 8), "ms_per_step": 1e3 * e2e_s},
+            "phases_ms_last_sweep": phases,
+            "plain_fp64": {"value": nG * k / fp64_s, "unit": "evaluations/s",
+                           "sample": f"first {k} transforms, device arrays"},
+            "accuracy": {"nan_pattern_identical": bool(np.array_equal(np.isnan(S4), np.isnan(Sr))),
+                         "max_rel_dS_mixed": float(np.nanmax(rel)),
+                         "max_rel_dS_fp64": float(np.nanmax(rel64)),
+                         "host_call_identical": bool(np.array_equal(Sh, out["S"].cpu().numpy(),
+                                                                    equal_nan=True)),
+                         "transforms_compared": k},
+            "gpu_launches": launches,
+            "cpu_baseline": {"value": nG * k / cpu_s, "unit": "evaluations/s",
+                             "cores": O.num_threads(0), "kind": "port",
+                             "sample": f"first {k} of {nT} transforms, the reference's loop "
+                                       "restated over the oracle AABB / exact winding number"}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -782,7 +856,7 @@ def main():
         {"exact": run_exact_line, "cloud": run_cloud_line, "precision": run_precision_study,
          "served": run_served_line,
          "signed_distance": run_signed_distance_line, "knn": run_knn_line,
-         "eytzinger2d": run_eytzinger_line}[args.workload](args)
+         "eytzinger2d": run_eytzinger_line, "swept": run_swept_line}[args.workload](args)
         return
     import torch
     import libigl_gb300 as G
@@ -824,8 +898,9 @@ def main():
         step()
     torch.cuda.synchronize()
 
-    # timed region: per-step CUDA events on the launch stream + live phase events
-    G.profile_enable(True)
+    # timed region: per-step CUDA events on the launch stream + live phase
+    # events (recorded by the library on its stream, read after the loop)
+    G.profile_enable(True, accumulate=True)
     sampler = ClockSampler(local)
     sampler.start()
     time.sleep(0.3)
@@ -833,17 +908,16 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
-    walk_ms = []
     evs[0].record(stream)
     for k in range(args.steps):
         step()
         evs[k + 1].record(stream)
-        ph = G.profile_read()  # waits for this step's phase events
-        walk_ms.append(ph.get("walk", float("nan")))
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
     clocks = sampler.stop()
+    ph = G.profile_read()
+    walk_ms = [ph.get("walk", float("nan")) / args.steps]
     G.profile_enable(False)
     step_ms = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
     total_ms = evs[0].elapsed_time(evs[-1])

@@ -252,6 +252,34 @@ int gwn_signed_distance(const double* P, int64_t nP, const double* V, int64_t nV
                         int precision, int mem, void* stream);
 
 /* ------------------------------------------------------------------------
+ * Swept volumes (the batched caller of the winding number and the signed
+ * distance on grids).
+ *
+ * gwn_swept_volume_signed_distance: igl::swept_volume_signed_distance(V,F,
+ * transforms,sign_type,GV,res,h,isolevel,S0,S)
+ * (include/igl/swept_volume_signed_distance.h:28-51, .cpp:21-160) for a
+ * triangle mesh V (#V x 3), F (#F x 3) under nT rigid motions
+ * (transforms: nT x 12 float64, each the row-major 3 x 4 [linear |
+ * translation] of the affine transform), over grid points GV (#GV x 3) of a
+ * res[0] x res[1] x res[2] grid (x fastest) with spacing h.  S0 (#GV,
+ * nullable: all NaN, the reference's second overload) seeds the running
+ * minimum; S (#GV) receives it (S may equal S0).  sign_type as for
+ * gwn_signed_distance.  A finite isolevel enables the reference's skipping
+ * of far and deep points and its final flood fill (#GV must then be
+ * res[0] res[1] res[2]).  Synchronizes `stream`.
+ *
+ * gwn_flood_fill: igl::flood_fill(res,S) (include/igl/flood_fill.h:20-25,
+ * .cpp:11-80): NaN entries of S (res[0] x res[1] x res[2], x fastest) take
+ * the values of the reference's scan.
+ * ---------------------------------------------------------------------- */
+int gwn_swept_volume_signed_distance(const double* V, int64_t nV, const int32_t* F, int64_t nF,
+                                     const double* transforms, int64_t nT, int sign_type,
+                                     const double* GV, int64_t nGV, const int32_t* res, double h,
+                                     double isolevel, const double* S0, double* S, int precision,
+                                     int mem, void* stream);
+int gwn_flood_fill(const int32_t* res, double* S, int mem, void* stream);
+
+/* ------------------------------------------------------------------------
  * 2-D winding numbers over an Eytzinger AABB tree of segments (libigl's
  * hierarchical 2-D path).
  *
@@ -363,6 +391,9 @@ int gwn_server_destroy(gwn_server* server);
  * CUDA events around its phases on its stream (e.g. "order_queries", "walk",
  * "refine"); gwn_profile_read waits for the last call's events and returns
  * the phase names ';'-separated and their durations in milliseconds.
+ * gwn_profile_enable(2) keeps the phases of every call until the next
+ * gwn_profile_enable (so a timed loop can read them once, after it ends);
+ * 0 turns recording off.  Each gwn_profile_enable clears what was kept.
  * ---------------------------------------------------------------------- */
 int gwn_profile_enable(int on);
 int gwn_profile_read(char* names, int names_cap, float* ms, int max_phases, int* num_phases);

@@ -34,7 +34,7 @@ __all__ = [
     "Octree", "octree", "CloudExpansion", "fast_winding_number_cloud_precompute",
     "fast_winding_number_cloud", "fast_winding_number_cloud_oneshot", "device_status",
     "Server", "signed_distance", "knn", "eytzinger_aabb", "eytzinger_aabb_winding_number_tree",
-    "eytzinger_aabb_winding_number",
+    "eytzinger_aabb_winding_number", "swept_volume_signed_distance", "flood_fill",
 ]
 
 _PREC = {"fp64": N.GWN_PLAIN_FP64, "plain": N.GWN_PLAIN_FP64, "mixed": N.GWN_MIXED}
@@ -577,17 +577,79 @@ def signed_distance(P, V, F, sign_type=SIGNED_DISTANCE_TYPE_DEFAULT, lower_bound
 
 
 # ------------------------------------------------------------- profiling --
-def profile_enable(on: bool = True) -> None:
-    """Record CUDA events around each phase of this thread's calls."""
-    N.check(N.load().gwn_profile_enable(int(on)))
+def _affine_rows(transforms):
+    T = np.asarray(transforms, dtype=np.float64)
+    if T.ndim == 2 and T.shape[1] == 12:
+        return np.ascontiguousarray(T)
+    if T.ndim == 3 and T.shape[1:] in ((3, 4), (4, 4)):
+        return np.ascontiguousarray(T[:, :3, :4].reshape(-1, 12))
+    raise ValueError("transforms must be nT x 3 x 4, nT x 4 x 4 or nT x 12")
+
+
+def swept_volume_signed_distance(V, F, transforms, sign_type, GV, res, h, isolevel, S0=None,
+                                 precision=None):
+    """igl::swept_volume_signed_distance(V,F,transforms,sign_type,GV,res,h,
+    isolevel,S0,S) (include/igl/swept_volume_signed_distance.h): the signed
+    distance at grid points GV (#GV x 3, a res[0] x res[1] x res[2] grid, x
+    fastest, spacing h) to the volume swept by the mesh under the rigid
+    motions ``transforms`` (nT x 3 x 4 or 4 x 4 affine matrices, applied as
+    x -> L x + t).  ``S0`` seeds the running minimum (default all NaN).  Host
+    arrays or CUDA tensors for V, F, GV, S0 (all of one kind); transforms on
+    the host.  ``precision``: how the sign's winding number is computed,
+    mixed by default (FP32 with FP64 near the mesh and for results within
+    1e-3 of 0.5); "fp64" is the reference's arithmetic."""
+    Va, Ga = _Arg(V, np.float64), _Arg(GV, np.float64)
+    Fa = _Arg(F, np.int32, allowed=(np.int32,))
+    _same_mem(Va, Fa, Ga)
+    if Ga.shape[1:] != (3,) or Va.shape[1:] != (3,) or Fa.shape[1:] != (3,):
+        raise ValueError("V, GV must be #x3 float and F #F x 3 int32")
+    T = _affine_rows(transforms)
+    r = np.ascontiguousarray(res, dtype=np.int32).reshape(3)
+    if precision is None:
+        precision = "mixed"
+    n = Ga.shape[0]
+    S = _empty_like_mem(Ga.mem, (n,), np.float64, like=Ga)
+    S0p = None
+    if S0 is not None:
+        S0a = _Arg(S0, np.float64)
+        _same_mem(Ga, S0a)
+        S0p = S0a.ptr
+    stream = _stream_ptr() if Ga.mem == N.GWN_DEVICE else None
+    N.check(N.load().gwn_swept_volume_signed_distance(
+        Va.ptr, Va.shape[0], Fa.ptr, Fa.shape[0], T.ctypes.data_as(C.c_void_p), T.shape[0],
+        int(sign_type), Ga.ptr, n, r.ctypes.data_as(C.c_void_p), float(h), float(isolevel),
+        S0p, _ptr_of(S), _prec(precision), Ga.mem, stream))
+    return S
+
+
+def flood_fill(res, S):
+    """igl::flood_fill(res,S) (include/igl/flood_fill.h): fills the NaN entries
+    of S (res[0] x res[1] x res[2], x fastest) in place and returns S."""
+    Sa = _Arg(S, np.float64)
+    if Sa.mem == N.GWN_HOST and Sa.obj is not S:
+        raise ValueError("S must be a contiguous float64 array (filled in place)")
+    if Sa.mem == N.GWN_DEVICE and Sa.obj.data_ptr() != S.data_ptr():
+        raise ValueError("S must be a contiguous float64 tensor (filled in place)")
+    r = np.ascontiguousarray(res, dtype=np.int32).reshape(3)
+    stream = _stream_ptr() if Sa.mem == N.GWN_DEVICE else None
+    N.check(N.load().gwn_flood_fill(r.ctypes.data_as(C.c_void_p), Sa.ptr, Sa.mem, stream))
+    return S
+
+
+def profile_enable(on: bool = True, accumulate: bool = False) -> None:
+    """Record CUDA events around each phase of this thread's calls (of the
+    last call only, or, with ``accumulate``, of every call until the next
+    profile_enable)."""
+    N.check(N.load().gwn_profile_enable(0 if not on else (2 if accumulate else 1)))
 
 
 def profile_read() -> dict:
-    """{phase name: milliseconds} of the last profiled call (waits for it)."""
-    names = C.create_string_buffer(4096)
-    ms = (C.c_float * 64)()
+    """{phase name: milliseconds} of the recorded phases (the last call's, or
+    summed over every call in accumulate mode); waits for them."""
+    names = C.create_string_buffer(1 << 18)
+    ms = (C.c_float * 8192)()
     n = C.c_int(0)
-    N.check(N.load().gwn_profile_read(names, 4096, ms, 64, C.byref(n)))
+    N.check(N.load().gwn_profile_read(names, 1 << 18, ms, 8192, C.byref(n)))
     keys = names.value.decode().split(";") if names.value else []
     out = {}
     for k, v in zip(keys, list(ms)[: n.value]):

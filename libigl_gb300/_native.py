@@ -57,6 +57,9 @@ SIGNATURES = {
     "gwn_octree_knn": ([_p, _p, _i, _i64, _i64, _p, _i, _p], _i),
     "gwn_knn": ([_p, _i64, _p, _i64, _i64, _p, _i, _p], _i),
     "gwn_eytzinger_slots": ([_i64], _i64),
+    "gwn_swept_volume_signed_distance": ([_p, _i64, _p, _i64, _p, _i64, _i, _p, _i64, _p, _d,
+                                          _d, _p, _p, _i, _i, _p], _i),
+    "gwn_flood_fill": ([_p, _p, _i, _p], _i),
     "gwn_eytzinger_aabb": ([_p, _p, _i64, _i, _p, _p, _p, _i, _p], _i),
     "gwn_eytzinger_winding_number_tree": ([_p, _i64, _p, _i64, _p, _p, _i, _p], _i),
     "gwn_eytzinger_winding_number": ([_p, _i64, _p, _i64, _p, _i64, _p, _p, _p, _i64, _p, _i64,

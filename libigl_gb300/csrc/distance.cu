@@ -603,30 +603,31 @@ void soup_squared_distance(const gwn_soup_impl& s, const void* Q, int q_dtype, i
   }
 }
 
-// Pseudonormal signs (W = +-1) and normals N (nullable) of every query from
-// its closest face I and point C.
-static void pseudonormal_signs(const double* P, int64_t nP, const double* V, int64_t nV,
-                               const int32_t* F, int64_t nF, const int32_t* I, const double* C,
-                               double* sqrD, double* sgn, double* N, cudaStream_t st) {
+void pseudonormal_precompute(const double* V, int64_t nV, const int32_t* F, int64_t nF,
+                             PseudonormalData& d, cudaStream_t st) {
   const int64_t ne = nF * 3;
   auto grid = [](int64_t n) { return (unsigned)std::max<int64_t>(1, (n + 255) / 256); };
-  DevBuf<double> FN((size_t)nF * 3, st), angle((size_t)ne, st), VN((size_t)std::max<int64_t>(nV, 1) * 3, st),
-      EN((size_t)ne * 3, st);
+  d.FN.alloc((size_t)nF * 3, st);
+  d.VN.alloc((size_t)std::max<int64_t>(nV, 1) * 3, st);
+  d.EN.alloc((size_t)ne * 3, st);
+  d.edge_of.alloc((size_t)ne, st);
+  DevBuf<double> angle((size_t)ne, st);
   DevBuf<uint32_t> vkey((size_t)ne, st), vkey_t((size_t)ne, st), eflag((size_t)ne, st);
   DevBuf<int32_t> vent((size_t)ne, st), vent_t((size_t)ne, st), eent((size_t)ne, st),
-      eent_t((size_t)ne, st), edge_of((size_t)ne, st);
+      eent_t((size_t)ne, st);
   DevBuf<unsigned long long> ekey((size_t)ne, st), ekey_t((size_t)ne, st);
-  launch_kernel(face_normals_kernel, grid(nF), 256, 0, st, V, F, nF, FN.get());
+  launch_kernel(face_normals_kernel, grid(nF), 256, 0, st, V, F, nF, d.FN.get());
   launch_kernel(corner_entries_kernel, grid(ne), 256, 0, st, V, F, nF, angle.get(), vkey.get(),
                 vent.get(), ekey.get(), eent.get());
   int vbits = 1;
   while (vbits < 32 && (int64_t(1) << vbits) < nV) ++vbits;
   radix_sort_pairs<uint32_t>(vkey.get(), vent.get(), vkey_t.get(), vent_t.get(), ne, 0,
                              (vbits + 7) / 8 * 8, st);
-  VN.zero(st);
+  d.VN.zero(st);
   launch_kernel(segment_normals_kernel<uint32_t>, grid(ne), 256, 0, st, (const uint32_t*)vkey.get(),
                 (const int32_t*)vent.get(), ne, (const double*)angle.get(),
-                (const double*)FN.get(), 0, (const uint32_t*)nullptr, VN.get(), (int32_t*)nullptr);
+                (const double*)d.FN.get(), 0, (const uint32_t*)nullptr, d.VN.get(),
+                (int32_t*)nullptr);
   radix_sort_pairs<unsigned long long>(ekey.get(), eent.get(), ekey_t.get(), eent_t.get(), ne, 0,
                                        64, st);
   launch_kernel(segment_start_flags_kernel, grid(ne), 256, 0, st,
@@ -634,11 +635,17 @@ static void pseudonormal_signs(const double* P, int64_t nP, const double* V, int
   exclusive_scan_u32(eflag.get(), eflag.get(), ne, st);
   launch_kernel(segment_normals_kernel<unsigned long long>, grid(ne), 256, 0, st,
                 (const unsigned long long*)ekey.get(), (const int32_t*)eent.get(), ne,
-                (const double*)angle.get(), (const double*)FN.get(), 1,
-                (const uint32_t*)eflag.get(), EN.get(), edge_of.get());
-  launch_kernel(pseudonormal_kernel, grid(nP), 256, 0, st, P, nP, V, F, nF,
-                (const double*)FN.get(), (const double*)VN.get(), (const double*)EN.get(),
-                (const int32_t*)edge_of.get(), (const double*)sqrD, I, C, sgn, N);
+                (const double*)angle.get(), (const double*)d.FN.get(), 1,
+                (const uint32_t*)eflag.get(), d.EN.get(), d.edge_of.get());
+}
+
+void pseudonormal_apply(const PseudonormalData& d, const double* P, int64_t nP, const double* V,
+                        const int32_t* F, int64_t nF, const int32_t* I, const double* C,
+                        const double* sqrD, double* sgn, double* N, cudaStream_t st) {
+  if (nP == 0) return;
+  launch_kernel(pseudonormal_kernel, (unsigned)((nP + 255) / 256), 256, 0, st, P, nP, V, F, nF,
+                (const double*)d.FN.get(), (const double*)d.VN.get(), (const double*)d.EN.get(),
+                (const int32_t*)d.edge_of.get(), sqrD, I, C, sgn, N);
 }
 
 void signed_distance_run(const double* P, int64_t nP, const double* V, int64_t nV,
@@ -672,7 +679,9 @@ void signed_distance_run(const double* P, int64_t nP, const double* V, int64_t n
     mode = 2;
   } else if (sign_type == GWN_SD_PSEUDONORMAL) {
     W.alloc((size_t)nP, st);
-    pseudonormal_signs(P, nP, V, nV, F, nF, I, C, sqrD.get(), W.get(), N, st);
+    PseudonormalData pn;
+    pseudonormal_precompute(V, nV, F, nF, pn, st);
+    pseudonormal_apply(pn, P, nP, V, F, nF, I, C, sqrD.get(), W.get(), N, st);
     mode = 3;
   }
   launch_kernel(combine_kernel, grid, 256, 0, st, (const double*)sqrD.get(),

@@ -564,17 +564,45 @@ __global__ void eval64_kernel(EvalTree T, const double* __restrict__ P, int64_t 
 struct Frame {
   double cx, cy, scale;
 };
+// The frame and the query cells' origin and scale, computed on the device
+// from the root box (so a call never waits for the device).
+struct EvalFrame {
+  Frame f;
+  float klx, kly, ksx, ksy;
+};
+
+__global__ void frame_kernel(const double* __restrict__ B1, const double* __restrict__ B2,
+                             EvalFrame* __restrict__ out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double cx = 0.5 * (B1[0] + B2[0]), cy = 0.5 * (B1[1] + B2[1]);
+  double ex = B2[0] - B1[0], ey = B2[1] - B1[1];
+  if (!isfinite(cx) || !isfinite(cy) || !isfinite(ex) || !isfinite(ey)) {
+    cx = cy = 0;
+    ex = ey = 1;
+  }
+  const double diag = sqrt(ex * ex + ey * ey);
+  int e2 = 0;
+  if (diag > 0) frexp(diag, &e2);  // diag = f 2^e2, f in [0.5, 1)
+  EvalFrame r;
+  r.f = Frame{cx, cy, ldexp(1.0, -e2)};
+  // 1024 x 1024 Morton cells over the root box grown 25%
+  const double hx = 0.625 * ex + 1e-300, hy = 0.625 * ey + 1e-300;
+  r.klx = (float)(cx - hx);
+  r.kly = (float)(cy - hy);
+  r.ksx = (float)(1024.0 / (2 * hx));
+  r.ksy = (float)(1024.0 / (2 * hy));
+  *out = r;
+}
 __device__ __forceinline__ void split_coord(double x, float& hi, float& lo) {
   hi = (float)x;
   lo = (float)(x - (double)hi);
 }
 
-// Node: box in the frame (rounded outward), for a leaf its segment's
-// endpoints (hi, lo); meta = (leaf, a | c0, b | c1, 0).
+// Node (32 bytes, one sector): box in the frame (rounded outward) and meta =
+// (leaf, a | c0, b | c1, 0).  A leaf's segment endpoints (hi, lo) sit in a
+// per-segment array, a pair's in a per-pair array (32 bytes each).
 struct NodeF {
   float4 box;
-  float4 shi;
-  float4 slo;
   int4 meta;
 };
 struct PairF {
@@ -590,17 +618,18 @@ __device__ __forceinline__ void seg_hilo(const double* V, int64_t a, int64_t b, 
   split_coord((V[2 * b + 1] - f.cy) * f.scale, hi.w, lo.w);
 }
 
-__global__ void prep_nodes_kernel(EvalTree T, Frame f, NodeF* __restrict__ nodes,
+__global__ void prep_nodes_kernel(EvalTree T, const EvalFrame* __restrict__ fr,
+                                  NodeF* __restrict__ nodes, PairF* __restrict__ segs,
                                   unsigned* status) {
   const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r >= T.nb) return;
+  const Frame f = fr->f;
   NodeF nd;
   const int32_t lf = T.leaf[r];
   nd.box = make_float4(__double2float_rd((T.B1[2 * r] - f.cx) * f.scale),
                        __double2float_rd((T.B1[2 * r + 1] - f.cy) * f.scale),
                        __double2float_ru((T.B2[2 * r] - f.cx) * f.scale),
                        __double2float_ru((T.B2[2 * r + 1] - f.cy) * f.scale));
-  nd.shi = nd.slo = make_float4(0.f, 0.f, 0.f, 0.f);
   nd.meta = make_int4(lf, 0, 0, 0);
   if (lf >= 0) {
     int64_t a = -1, b = -1;
@@ -612,7 +641,9 @@ __global__ void prep_nodes_kernel(EvalTree T, Frame f, NodeF* __restrict__ nodes
       atomicOr(status, kStatusBadInput);
       nd.meta = make_int4(-3, 0, 0, 0);  // skipped by the walk
     } else {
-      seg_hilo(T.V, a, b, f, nd.shi, nd.slo);
+      PairF sg;
+      seg_hilo(T.V, a, b, f, sg.hi, sg.lo);
+      segs[lf] = sg;
       nd.meta = make_int4(lf, (int)a, (int)b, 0);
     }
   } else if (lf == -1) {
@@ -628,10 +659,12 @@ __global__ void prep_nodes_kernel(EvalTree T, Frame f, NodeF* __restrict__ nodes
 }
 
 // Pair i: both endpoints in the frame (hi, lo); (ida, idb) for FP64 terms.
-__global__ void prep_pairs_kernel(EvalTree T, Frame f, PairF* __restrict__ pf,
-                                  int2* __restrict__ pid, int64_t npairs, unsigned* status) {
+__global__ void prep_pairs_kernel(EvalTree T, const EvalFrame* __restrict__ fr,
+                                  PairF* __restrict__ pf, int2* __restrict__ pid, int64_t npairs,
+                                  unsigned* status) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= npairs) return;
+  const Frame f = fr->f;
   int64_t a = T.I[2 * i], b = T.I[2 * i + 1];
   if (a < 0 || a >= T.nV || b < 0 || b >= T.nV) {
     atomicOr(status, kStatusBadInput);
@@ -645,11 +678,12 @@ __global__ void prep_pairs_kernel(EvalTree T, Frame f, PairF* __restrict__ pf,
 
 struct MixedTree {
   const NodeF* nodes;
+  const PairF* segs;
   const PairF* pf;
   const int2* pid;
   const double* V;
   int64_t nb;
-  Frame f;
+  const EvalFrame* fr;
 };
 
 // An FP32 angle term is trusted unless (a) the query is within 1e-9 of the
@@ -706,9 +740,10 @@ __global__ void __launch_bounds__(kT) eval_mixed_kernel(MixedTree T, const doubl
   const bool valid = i < nP;
   const int64_t q = valid ? (perm ? perm[i] : i) : 0;
   const double px = valid ? P[2 * q] : 0.0, py = valid ? P[2 * q + 1] : 0.0;
+  const Frame f = T.fr->f;
   float2 qh, ql;
-  split_coord((px - T.f.cx) * T.f.scale, qh.x, ql.x);
-  split_coord((py - T.f.cy) * T.f.scale, qh.y, ql.y);
+  split_coord((px - f.cx) * f.scale, qh.x, ql.x);
+  split_coord((py - f.cy) * f.scale, qh.y, ql.y);
   Sum32 acc;
   double acc64 = 0.0;
   bool active = valid;
@@ -719,9 +754,10 @@ __global__ void __launch_bounds__(kT) eval_mixed_kernel(MixedTree T, const doubl
     const NodeF* nd = T.nodes + r;
     const int4 meta = __ldg(&nd->meta);
     if (meta.x >= 0) {
-      if (active)
-        term_mixed(T, __ldg(&nd->shi), __ldg(&nd->slo), meta.y, meta.z, qh, ql, px, py, acc,
-                   acc64);
+      if (active) {
+        const PairF* sg = T.segs + meta.x;
+        term_mixed(T, __ldg(&sg->hi), __ldg(&sg->lo), meta.y, meta.z, qh, ql, px, py, acc, acc64);
+      }
       r = walk_next(r);
       continue;
     }
@@ -769,16 +805,16 @@ __device__ __forceinline__ uint32_t spread10(uint32_t x) {
   return x;
 }
 
-__global__ void keys2_kernel(const double* __restrict__ P, int64_t n, double lx, double ly,
-                             double sx, double sy, uint32_t* __restrict__ key) {
+__global__ void keys2_kernel(const double* __restrict__ P, int64_t n,
+                             const EvalFrame* __restrict__ fr, uint32_t* __restrict__ key) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  auto qz = [](double v, double l, double s) -> uint32_t {
-    double t = (v - l) * s;
-    t = fmin(fmax(t, 0.0), 1023.0);  // NaN -> 0
+  const float lx = fr->klx, ly = fr->kly, sx = fr->ksx, sy = fr->ksy;
+  auto qz = [](float v, float l, float s) -> uint32_t {
+    const float t = fminf(fmaxf((v - l) * s, 0.f), 1023.f);  // NaN -> 0
     return (uint32_t)t;
   };
-  key[i] = (spread10(qz(P[2 * i + 1], ly, sy)) << 1) | spread10(qz(P[2 * i], lx, sx));
+  key[i] = (spread10(qz((float)P[2 * i + 1], ly, sy)) << 1) | spread10(qz((float)P[2 * i], lx, sx));
 }
 
 void scan_into(const uint32_t* in, uint32_t* out, int64_t n, cudaStream_t st) {
@@ -930,27 +966,16 @@ void eytzinger_eval(const double* P, int64_t nP, const double* V, int64_t nV, co
     GWN_CUDA(cudaMemsetAsync(W, 0, (size_t)nP * sizeof(double), st));
     return;
   }
-  // Root box (host read) for the query order and the FP32 frame.
-  double lo[2], hi[2];
-  GWN_CUDA(cudaMemcpyAsync(lo, B1, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
-  GWN_CUDA(cudaMemcpyAsync(hi, B2, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
-  GWN_CUDA(cudaStreamSynchronize(st));
-  double cx = 0.5 * (lo[0] + hi[0]), cy = 0.5 * (lo[1] + hi[1]);
-  double ex = hi[0] - lo[0], ey = hi[1] - lo[1];
-  if (!std::isfinite(cx) || !std::isfinite(cy) || !std::isfinite(ex) || !std::isfinite(ey)) {
-    cx = cy = 0;
-    ex = ey = 1;
-  }
+  DevBuf<EvalFrame> frame(1, st);
+  launch_kernel(frame_kernel, 1, 32, 0, st, B1, B2, frame.get());
   DevBuf<int32_t> perm;
   if (nP >= 8192) {
     PhaseTimer ph("order_queries", st);
     GWN_REQUIRE(nP < (int64_t(1) << 31), "at most 2^31-1 queries per call");
-    const double hx = 0.625 * ex + 1e-300, hy = 0.625 * ey + 1e-300;
     DevBuf<uint32_t> key((size_t)nP, st);
     perm.alloc((size_t)nP, st);
-    // 1024 x 1024 Morton cells over the root box (grown 25%)
-    launch_kernel(keys2_kernel, nblk(nP), kT, 0, st, P, nP, cx - hx, cy - hy, 1024.0 / (2 * hx),
-                  1024.0 / (2 * hy), key.get());
+    launch_kernel(keys2_kernel, nblk(nP), kT, 0, st, P, nP, (const EvalFrame*)frame.get(),
+                  key.get());
     bucket_order(key.get(), nP, 1u << 20, perm.get(), st);
   }
   if (precision == GWN_PLAIN_FP64) {
@@ -960,20 +985,18 @@ void eytzinger_eval(const double* P, int64_t nP, const double* V, int64_t nV, co
   }
   const int64_t npairs = nI / 2;
   DevBuf<NodeF> nodes((size_t)nb, st);
+  DevBuf<PairF> segs((size_t)std::max<int64_t>(nE, 1), st);
   DevBuf<PairF> pf((size_t)std::max<int64_t>(npairs, 1), st);
   DevBuf<int2> pid((size_t)std::max<int64_t>(npairs, 1), st);
-  const double diag = std::sqrt(ex * ex + ey * ey);
-  int e2 = 0;
-  if (diag > 0 && std::isfinite(diag)) std::frexp(diag, &e2);  // diag = f * 2^e2, f in [0.5, 1)
-  const Frame frame{cx, cy, std::ldexp(1.0, -e2)};
   {
     PhaseTimer ph("prep", st);
-    launch_kernel(prep_nodes_kernel, nblk(nb), kT, 0, st, T, frame, nodes.get(), status);
+    launch_kernel(prep_nodes_kernel, nblk(nb), kT, 0, st, T, (const EvalFrame*)frame.get(),
+                  nodes.get(), segs.get(), status);
     if (npairs)
-      launch_kernel(prep_pairs_kernel, nblk(npairs), kT, 0, st, T, frame, pf.get(), pid.get(),
-                    npairs, status);
+      launch_kernel(prep_pairs_kernel, nblk(npairs), kT, 0, st, T, (const EvalFrame*)frame.get(),
+                    pf.get(), pid.get(), npairs, status);
   }
-  MixedTree M{nodes.get(), pf.get(), pid.get(), V, nb, frame};
+  MixedTree M{nodes.get(), segs.get(), pf.get(), pid.get(), V, nb, frame.get()};
   DevBuf<int32_t> redo((size_t)nP, st);
   DevBuf<uint32_t> nredo(1, st);
   nredo.zero(st);

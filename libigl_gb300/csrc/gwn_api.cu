@@ -41,7 +41,7 @@ struct PhaseRec {
   std::string name;
   cudaEvent_t start = nullptr, stop = nullptr;
 };
-thread_local bool g_profile = false;
+thread_local int g_profile = 0;  // 0 off, 1 per call, 2 accumulate across calls
 thread_local std::vector<PhaseRec> g_phases;
 void clear_phases() {
   for (auto& p : g_phases) {
@@ -53,7 +53,7 @@ void clear_phases() {
 }  // namespace
 
 void profile_begin_call() {
-  if (g_profile) clear_phases();
+  if (g_profile == 1) clear_phases();
 }
 
 PhaseTimer::PhaseTimer(const char* name, cudaStream_t st) {
@@ -571,8 +571,9 @@ int gwn_cloud_eval_arrays(const double* P, const double* N, const double* A, int
 // ---------------------------------------------------------------- profile --
 int gwn_profile_enable(int on) {
   return guarded("gwn_profile_enable", [&] {
-    g_profile = on != 0;
-    if (!g_profile) clear_phases();
+    GWN_REQUIRE(on >= 0 && on <= 2, "on must be 0, 1 or 2");
+    g_profile = on;
+    clear_phases();
   });
 }
 
@@ -821,6 +822,81 @@ int gwn_eytzinger_winding_number(const double* P, int64_t nP, const double* V, i
     if (mem == GWN_HOST) {
       GWN_CUDA(cudaMemcpyAsync(W, dW.dev, (size_t)nP * 8, cudaMemcpyDeviceToHost, st));
       status.check(st, "eytzinger_winding_number");
+    }
+  });
+}
+
+int gwn_swept_volume_signed_distance(const double* V, int64_t nV, const int32_t* F, int64_t nF,
+                                     const double* transforms, int64_t nT, int sign_type,
+                                     const double* GV, int64_t nGV, const int32_t* res, double h,
+                                     double isolevel, const double* S0, double* S, int precision,
+                                     int mem, void* stream) {
+  return guarded("gwn_swept_volume_signed_distance", [&] {
+    profile_begin_call();
+    GWN_REQUIRE(nV >= 0 && nF >= 0 && nT >= 0 && nGV >= 0, "sizes must be non-negative");
+    GWN_REQUIRE(nF == 0 || (V && F), "V and F must be non-null");
+    GWN_REQUIRE(nT == 0 || transforms, "transforms must be non-null");
+    GWN_REQUIRE(nGV == 0 || (GV && S), "GV and S must be non-null");
+    GWN_REQUIRE(res != nullptr, "res must be non-null");
+    GWN_REQUIRE(nGV < (int64_t(1) << 31), "at most 2^31-1 grid points");
+    GWN_REQUIRE(sign_type >= GWN_SD_PSEUDONORMAL && sign_type <= GWN_SD_FAST_WINDING_NUMBER,
+                "sign_type must be one of GWN_SD_*");
+    if (std::isfinite(isolevel))
+      GWN_REQUIRE(res[0] >= 0 && res[1] >= 0 && res[2] >= 0 &&
+                      (int64_t)res[0] * res[1] * res[2] == nGV,
+                  "with a finite isolevel #GV must equal res[0]*res[1]*res[2]");
+    check_precision(precision);
+    check_mem(mem);
+    ensure_device();
+    if (nGV == 0) return;
+    cudaStream_t st = as_stream(stream);
+    Staged<double> dV(V, (size_t)nV * 3, mem, st), dGV(GV, (size_t)nGV * 3, mem, st);
+    Staged<int32_t> dF(F, (size_t)nF * 3, mem, st);
+    Staged<double> dS(S, (size_t)nGV, mem, st, false);
+    if (S0) {
+      if (mem == GWN_HOST)
+        GWN_CUDA(cudaMemcpyAsync(dS.dev, S0, (size_t)nGV * 8, cudaMemcpyHostToDevice, st));
+      else if (S0 != S)
+        GWN_CUDA(cudaMemcpyAsync(dS.dev, S0, (size_t)nGV * 8, cudaMemcpyDeviceToDevice, st));
+    } else {
+      GWN_CUDA(cudaMemsetAsync(dS.dev, 0xff, (size_t)nGV * 8, st));  // NaN
+    }
+    std::vector<double> T((size_t)nT * 12);
+    if (nT) {
+      if (mem == GWN_HOST) {
+        std::copy(transforms, transforms + nT * 12, T.begin());
+      } else {
+        GWN_CUDA(cudaMemcpyAsync(T.data(), transforms, T.size() * 8, cudaMemcpyDeviceToHost, st));
+        GWN_CUDA(cudaStreamSynchronize(st));
+      }
+    }
+    const int32_t r3[3] = {res[0], res[1], res[2]};
+    swept_volume_run(dV.dev, nV, dF.dev, nF, T.data(), nT, sign_type, dGV.dev, nGV, r3, h,
+                     isolevel, dS.dev, precision, st);
+    if (mem == GWN_HOST) {
+      GWN_CUDA(cudaMemcpyAsync(S, dS.dev, (size_t)nGV * 8, cudaMemcpyDeviceToHost, st));
+      GWN_CUDA(cudaStreamSynchronize(st));
+    }
+  });
+}
+
+int gwn_flood_fill(const int32_t* res, double* S, int mem, void* stream) {
+  return guarded("gwn_flood_fill", [&] {
+    GWN_REQUIRE(res != nullptr, "res must be non-null");
+    GWN_REQUIRE(res[0] >= 0 && res[1] >= 0 && res[2] >= 0, "res must be non-negative");
+    const int64_t n = (int64_t)res[0] * res[1] * res[2];
+    GWN_REQUIRE(n == 0 || S, "S must be non-null");
+    GWN_REQUIRE(n < (int64_t(1) << 40), "grid too large");
+    check_mem(mem);
+    ensure_device();
+    if (n == 0) return;
+    cudaStream_t st = as_stream(stream);
+    Staged<double> dS(S, (size_t)n, mem, st);
+    const int32_t r3[3] = {res[0], res[1], res[2]};
+    flood_fill_run(r3, dS.dev, st);
+    if (mem == GWN_HOST) {
+      GWN_CUDA(cudaMemcpyAsync(S, dS.dev, (size_t)n * 8, cudaMemcpyDeviceToHost, st));
+      GWN_CUDA(cudaStreamSynchronize(st));
     }
   });
 }

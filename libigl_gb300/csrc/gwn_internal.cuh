@@ -40,6 +40,51 @@ void signed_distance_run(const double* P, int64_t nP, const double* V, int64_t n
                          double upper_bound, double* S, int32_t* I, double* C, double* N,
                          int precision, cudaStream_t st);
 
+// Pseudonormals of igl::pseudonormal_test (distance.cu): face, angle-weighted
+// vertex and uniform edge normals of a mesh, then per query the sign (+-1,
+// into sgn) and normal (N, nullable) at its closest face I and point C.
+struct PseudonormalData {
+  DevBuf<double> FN, VN, EN;
+  DevBuf<int32_t> edge_of;
+};
+void pseudonormal_precompute(const double* V, int64_t nV, const int32_t* F, int64_t nF,
+                             PseudonormalData& d, cudaStream_t st);
+void pseudonormal_apply(const PseudonormalData& d, const double* P, int64_t nP, const double* V,
+                        const int32_t* F, int64_t nF, const int32_t* I, const double* C,
+                        const double* sqrD, double* sgn, double* N, cudaStream_t st);
+
+// igl::swept_volume_signed_distance (swept.cu); device pointers; S holds S0
+// on entry.  transforms: nT x 12 row-major (the 3 x 4 [linear | translation]
+// rows of each affine transform).  Synchronizes `st`.
+void swept_volume_run(const double* V, int64_t nV, const int32_t* F, int64_t nF,
+                      const double* transforms_host, int64_t nT, int sign_type, const double* GV,
+                      int64_t nG, const int32_t res[3], double h, double isolevel, double* S,
+                      int precision, cudaStream_t st);
+// igl::flood_fill (swept.cu) over a res[0] x res[1] x res[2] grid (x fastest).
+void flood_fill_run(const int32_t res[3], double* S, cudaStream_t st);
+
+// Hierarchical exact winding number of a triangle mesh (hier.cu): the
+// caller's V / F stay referenced (device pointers) for the FP64 re-checks.
+struct HierTree {
+  const double* V = nullptr;
+  int64_t nV = 0;
+  const int32_t* F = nullptr;
+  int64_t nF = 0;
+  int n = 0;
+  int64_t nnodes = 0, ncap = 0;
+  double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0}, c[3] = {0, 0, 0};
+  double eps = 0;
+  DevMem<float4> nodes;   // 2 per node
+  DevMem<int32_t> capn;   // cap triangles per node
+  DevMem<float4> caps;    // 4 per cap triangle
+  DevMem<float4> tris;    // 4 per leaf triangle
+  DevMem<double> tris64;  // 9 per leaf triangle
+};
+void hier_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, HierTree& h,
+                cudaStream_t st);
+// W of every query (FP64 device arrays), mixed precision; synchronizes `st`.
+void hier_eval(const HierTree& h, const double* Q, int64_t nQ, double* W, cudaStream_t st);
+
 // Eytzinger AABB tree of segments (eytzinger.cu); device pointers.
 int64_t eytzinger_slots(int64_t m);
 void eytzinger_build(const double* PB1, const double* PB2, int64_t m, int dim, double* B1,

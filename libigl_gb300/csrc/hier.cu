@@ -1,0 +1,707 @@
+// Hierarchical exact winding number of a triangle mesh, the GPU form of
+// igl::WindingNumberAABB / igl::WindingNumberTree (include/igl/WindingNumberTree.h:
+// 180-350, WindingNumberAABB.h): seen from a point outside a node's box, the
+// node's triangles subtend the same solid angle as a cap closing their
+// boundary, so the sum over the node's triangles can be replaced by a sum
+// over the cap's triangles.  The value is the all-pairs sum's up to
+// rounding.
+//
+// Build.  Triangles are ordered along a Morton curve of their centroids and
+// a binary radix tree is built over that order (every internal node covers
+// a contiguous range of leaves); nodes are laid out in pre-order with a link
+// one past each subtree.  A node's boundary: over its triangles' directed
+// edges (a, b), the net count of each undirected edge {u < v} (+1 for u -> v,
+// -1 for v -> u); edges with a non-zero count are the boundary, with that
+// multiplicity and orientation.  Incidences (edge, leaf position) are sorted
+// by edge (stable, so leaf order within an edge), and each (edge, node) with
+// a non-zero count is emitted once, by the edge's first incidence under the
+// node.  The cap is the fan from one boundary vertex (the apex) over the
+// boundary edges: W(node) = sum over boundary edges (u -> v) of
+// W(apex, u, v) (fan triangles through the apex vanish and are dropped).  A
+// closed patch has no boundary and adds nothing from outside its box.  As in
+// the reference, a node's cap is used only when it has fewer triangles than
+// the node.
+//
+// Walk (mixed precision).  One thread per query (cell-ordered queries), the
+// warp moves through the pre-order nodes with per-lane resume positions (a
+// lane takes exactly its own walk).  At a node whose box, grown by the near
+// distance eps = 1e-3 x the mesh diagonal, excludes the query (FP32, boxes
+// rounded outward) and whose cap is usable, the lane adds the cap's FP32
+// terms and skips the subtree, so every cap term is at least eps from the
+// query, as every FP32 pair of the all-pairs path is; otherwise it descends.
+// A leaf's triangle is FP32 unless the query is inside its bounding sphere
+// grown by eps, then FP64 (the reference's formula).  Coordinates are taken
+// relative to the mesh box centre.  Results within 1e-3 of 0.5 are redone by
+// the FP64 all-pairs kernel.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "bh_common.cuh"
+#include "exact_terms.cuh"
+#include "gwn_internal.cuh"
+#include "sort.cuh"
+
+namespace gwn {
+namespace {
+
+constexpr int kT = 256;
+constexpr double kNearFrac = 1e-3;
+constexpr double kBand = 1e-3;
+constexpr double kInv2Pi = 0.15915494309189533577;
+inline unsigned nblk(int64_t n, int t = kT) { return (unsigned)std::max<int64_t>(1, (n + t - 1) / t); }
+
+__device__ __forceinline__ uint64_t spread21(uint64_t x) {
+  x &= 0x1fffffull;
+  x = (x | (x << 32)) & 0x1f00000000ffffull;
+  x = (x | (x << 16)) & 0x1f0000ff0000ffull;
+  x = (x | (x << 8)) & 0x100f00f00f00f00full;
+  x = (x | (x << 4)) & 0x10c30c30c30c30c3ull;
+  x = (x | (x << 2)) & 0x1249249249249249ull;
+  return x;
+}
+
+__global__ void mesh_bbox_kernel(const double* __restrict__ V, int64_t nV,
+                                 unsigned long long* __restrict__ mm) {
+  double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nV;
+       i += (int64_t)gridDim.x * blockDim.x)
+    for (int d = 0; d < 3; ++d) {
+      const double v = V[i * 3 + d];
+      if (isfinite(v)) {
+        lo[d] = fmin(lo[d], v);
+        hi[d] = fmax(hi[d], v);
+      }
+    }
+  for (int d = 0; d < 3; ++d) {
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[d] = fmin(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
+      hi[d] = fmax(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicMin(&mm[d], ordered_bits(lo[d]));
+      atomicMax(&mm[3 + d], ordered_bits(hi[d]));
+    }
+  }
+}
+
+__global__ void tri_keys_kernel(const double* __restrict__ V, int64_t nV,
+                                const int32_t* __restrict__ F, int64_t nF,
+                                const unsigned long long* __restrict__ mm,
+                                unsigned long long* __restrict__ key, int32_t* __restrict__ val,
+                                unsigned* status) {
+  const int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (f >= nF) return;
+  double c[3] = {0, 0, 0};
+  for (int k = 0; k < 3; ++k) {
+    int64_t v = F[f * 3 + k];
+    if (v < 0 || v >= nV) {
+      atomicOr(status, kStatusBadInput);
+      v = 0;
+    }
+    for (int d = 0; d < 3; ++d) c[d] += V[v * 3 + d];
+  }
+  uint64_t code = 0;
+  for (int d = 0; d < 3; ++d) {
+    const double lo = from_ordered_bits(mm[d]), hi = from_ordered_bits(mm[3 + d]);
+    const double ext = hi - lo;
+    double t = ext > 0 ? (c[d] / 3.0 - lo) / ext : 0.0;
+    t = fmin(fmax(t, 0.0), 1.0);  // NaN -> 0
+    code |= spread21((uint64_t)(t * 2097151.0)) << (2 - d);
+  }
+  key[f] = code;
+  val[f] = (int32_t)f;
+}
+
+// Common prefix length of sorted keys i and j, ties broken by index.
+__device__ __forceinline__ int delta_key(const unsigned long long* keys, int n, int i, int j) {
+  if (j < 0 || j >= n) return -1;
+  const unsigned long long a = keys[i], b = keys[j];
+  if (a == b) return 64 + __clz((unsigned)(i ^ j));
+  return __clzll((long long)(a ^ b));
+}
+
+// Binary radix tree over n sorted keys: internal nodes 0..n-2 (range of
+// leaves [first, last]), leaf j is node n-1+j.
+__global__ void radix_tree_kernel(const unsigned long long* __restrict__ keys, int n,
+                                  int32_t* __restrict__ left, int32_t* __restrict__ right,
+                                  int32_t* __restrict__ parent, int32_t* __restrict__ first,
+                                  int32_t* __restrict__ last) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n - 1) return;
+  const int d = (delta_key(keys, n, i, i + 1) - delta_key(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+  const int dmin = delta_key(keys, n, i, i - d);
+  int lmax = 2;
+  while (delta_key(keys, n, i, i + lmax * d) > dmin) lmax <<= 1;
+  int l = 0;
+  for (int t = lmax >> 1; t >= 1; t >>= 1)
+    if (delta_key(keys, n, i, i + (l + t) * d) > dmin) l += t;
+  const int j = i + l * d;
+  const int dnode = delta_key(keys, n, i, j);
+  int s = 0;
+  int t = l;
+  do {
+    t = (t + 1) >> 1;
+    if (delta_key(keys, n, i, i + (s + t) * d) > dnode) s += t;
+  } while (t > 1);
+  const int gamma = i + s * d + min(d, 0);
+  const int lo = min(i, j), hi = max(i, j);
+  const int lc = (lo == gamma) ? (n - 1 + gamma) : gamma;
+  const int rc = (hi == gamma + 1) ? (n - 1 + gamma + 1) : (gamma + 1);
+  left[i] = lc;
+  right[i] = rc;
+  parent[lc] = i;
+  parent[rc] = i;
+  first[i] = lo;
+  last[i] = hi;
+}
+
+// Subtree sizes (nodes) and boxes (FP64) bottom-up: the second
+// child to arrive at a parent merges.
+__global__ void bottom_up_kernel(const double* __restrict__ V, const int32_t* __restrict__ F,
+                                 int64_t nV, const int32_t* __restrict__ sorted_tri, int n,
+                                 const int32_t* __restrict__ left,
+                                 const int32_t* __restrict__ right,
+                                 const int32_t* __restrict__ parent, double* __restrict__ box,
+                                 int32_t* __restrict__ size, unsigned* __restrict__ flags) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const int node = n - 1 + j;
+  {
+    const int64_t f = sorted_tri[j];
+    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int k = 0; k < 3; ++k) {
+      int64_t v = F[f * 3 + k];
+      if (v < 0 || v >= nV) v = 0;
+      for (int d = 0; d < 3; ++d) {
+        lo[d] = fmin(lo[d], V[v * 3 + d]);
+        hi[d] = fmax(hi[d], V[v * 3 + d]);
+      }
+    }
+    for (int d = 0; d < 3; ++d) {
+      box[(int64_t)node * 6 + d] = lo[d];
+      box[(int64_t)node * 6 + 3 + d] = hi[d];
+    }
+    size[node] = 1;
+  }
+  if (n == 1) return;
+  int cur = node;
+  while (true) {
+    const int p = parent[cur];
+    __threadfence();
+    if (atomicAdd(&flags[p], 1u) == 0) return;  // the first child to arrive stops
+    __threadfence();
+    const int lc = left[p], rc = right[p];
+    for (int d = 0; d < 3; ++d) {
+      box[(int64_t)p * 6 + d] = fmin(box[(int64_t)lc * 6 + d], box[(int64_t)rc * 6 + d]);
+      box[(int64_t)p * 6 + 3 + d] =
+          fmax(box[(int64_t)lc * 6 + 3 + d], box[(int64_t)rc * 6 + 3 + d]);
+    }
+    size[p] = 1 + size[lc] + size[rc];
+    if (p == 0) return;
+    cur = p;
+  }
+}
+
+__global__ void preorder_kernel(const int32_t* __restrict__ left,
+                                const int32_t* __restrict__ parent,
+                                const int32_t* __restrict__ size, int nnodes,
+                                int32_t* __restrict__ pre) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= nnodes) return;
+  int p = 0, cur = x;
+  while (cur != 0) {
+    const int par = parent[cur];
+    const int lc = left[par];
+    p += 1 + (lc == cur ? 0 : size[lc]);
+    cur = par;
+  }
+  pre[x] = p;
+}
+
+// Directed-edge incidences of the sorted triangles: key {u < v} packed, value
+// 3 j + c (leaf position j, corner c: edge from corner c to corner c+1).
+__global__ void edge_incidence_kernel(const int32_t* __restrict__ F,
+                                      const int32_t* __restrict__ sorted_tri, int n,
+                                      unsigned long long* __restrict__ key,
+                                      int32_t* __restrict__ val) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= 3 * (int64_t)n) return;
+  const int64_t j = i / 3, c = i % 3;
+  const int64_t f = sorted_tri[j];
+  const uint32_t a = (uint32_t)max(F[f * 3 + c], 0), b = (uint32_t)max(F[f * 3 + (c + 1) % 3], 0);
+  const uint32_t u = min(a, b), v = max(a, b);
+  key[i] = ((unsigned long long)u << 32) | v;
+  val[i] = (int32_t)i;
+}
+
+__device__ __forceinline__ int edge_sign(const int32_t* F, const int32_t* sorted_tri, int32_t e) {
+  const int64_t j = e / 3, c = e % 3;
+  const int64_t f = sorted_tri[j];
+  return F[f * 3 + c] < F[f * 3 + (c + 1) % 3] ? 1 : -1;
+}
+
+__global__ void sign_flags_kernel(const int32_t* __restrict__ F,
+                                  const int32_t* __restrict__ sorted_tri,
+                                  const int32_t* __restrict__ val, int64_t n,
+                                  uint32_t* __restrict__ fl) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i > n) return;
+  fl[i] = i < n ? (uint32_t)(1 + edge_sign(F, sorted_tri, val[i])) : 0u;
+}
+
+// First index in [lo, hi) whose (key, leaf position) is past (k, jmax).
+__device__ __forceinline__ int64_t past(const unsigned long long* key, const int32_t* val,
+                                        int64_t lo, int64_t hi, unsigned long long k, int jmax) {
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    const unsigned long long km = key[mid];
+    const bool before = km < k || (km == k && val[mid] / 3 <= jmax);
+    if (before) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// kEmit == false: count the (edge, node) records each incidence emits;
+// true: write them (node pre-order index, record value = incidence index,
+// net count).
+template <bool kEmit>
+__global__ void boundary_records_kernel(const unsigned long long* __restrict__ key,
+                                        const int32_t* __restrict__ val, int64_t m, int n,
+                                        const int32_t* __restrict__ parent,
+                                        const int32_t* __restrict__ first,
+                                        const int32_t* __restrict__ last,
+                                        const int32_t* __restrict__ pre,
+                                        const uint32_t* __restrict__ ps,
+                                        uint32_t* __restrict__ cnt,
+                                        const uint32_t* __restrict__ off,
+                                        int32_t* __restrict__ rnode, int32_t* __restrict__ rinc,
+                                        int32_t* __restrict__ rnet) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  const unsigned long long k = key[t];
+  const int j = val[t] / 3;
+  const bool prev_same = t > 0 && key[t - 1] == k;
+  const int pj = prev_same ? val[t - 1] / 3 : -1;
+  uint32_t c = 0;
+  uint64_t w = kEmit ? off[t] : 0;
+  int cur = n - 1 + j;
+  while (cur != 0) {
+    const int r = parent[cur];
+    if (prev_same && pj >= first[r]) break;  // an earlier incidence of the edge emits here
+    const int64_t b = past(key, val, t, m, k, last[r]);
+    const int64_t net = ((int64_t)ps[b] - (int64_t)ps[t]) - (b - t);
+    if (net != 0) {
+      if (kEmit) {
+        rnode[w] = pre[r];
+        rinc[w] = (int32_t)t;
+        rnet[w] = (int32_t)net;
+        ++w;
+      }
+      ++c;
+    }
+    cur = r;
+  }
+  if (!kEmit) cnt[t] = c;
+}
+
+__global__ void iota_records_kernel(int32_t* __restrict__ p, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) p[i] = (int32_t)i;
+}
+
+__global__ void record_mult_kernel(const int32_t* __restrict__ rnet, const int32_t* __restrict__ order,
+                                   int64_t nrec, uint32_t* __restrict__ mult) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i > nrec) return;
+  mult[i] = i < nrec ? (uint32_t)abs(rnet[order[i]]) : 0u;
+}
+
+// Node record of the walk (32 bytes): box (FP32 in the centred frame, grown
+// by eps, rounded outward) with the link in lo.w; hi.w = cap start (>= 0:
+// usable cap of capn triangles), -1 (descend), or -2 - slot (leaf).
+struct NodeH {
+  float4 lo;
+  float4 hi;
+};
+
+struct HierDev {
+  const NodeH* nodes;
+  const int32_t* capn;
+  const TriF* caps;      // cap triangles, FP32 centred frame
+  const TriF* tris;      // leaf triangles by slot, FP32 centred frame
+  const double* tris64;  // leaf triangles by slot, 9 doubles
+  int nnodes;
+};
+
+__global__ void node_records_kernel(const double* __restrict__ box,
+                                    const int32_t* __restrict__ pre,
+                                    const int32_t* __restrict__ size, int n,
+                                    const uint32_t* __restrict__ cap_off,
+                                    const uint32_t* __restrict__ cap_cnt, double cx, double cy,
+                                    double cz, double eps, NodeH* __restrict__ nodes,
+                                    int32_t* __restrict__ capn) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nnodes = 2 * n - 1;
+  if (x >= nnodes) return;
+  const int p = pre[x];
+  const bool leaf = x >= n - 1;
+  NodeH h;
+  const double c[3] = {cx, cy, cz};
+  float lo[3], hi[3];
+  for (int d = 0; d < 3; ++d) {
+    lo[d] = __double2float_rd(box[(int64_t)x * 6 + d] - c[d] - eps);
+    hi[d] = __double2float_ru(box[(int64_t)x * 6 + 3 + d] - c[d] + eps);
+  }
+  int meta;
+  int cn = 0;
+  if (leaf) {
+    meta = -2 - (x - (n - 1));
+  } else {
+    cn = (int)cap_cnt[p];
+    const int tris_under = (size[x] + 1) / 2;
+    meta = cn < tris_under ? (int)cap_off[p] : -1;
+  }
+  h.lo = make_float4(lo[0], lo[1], lo[2], __int_as_float(p + size[x]));
+  h.hi = make_float4(hi[0], hi[1], hi[2], __int_as_float(meta));
+  nodes[p] = h;
+  capn[p] = cn;
+}
+
+// Cap triangles of every node: for the records of node r (in node order,
+// each repeated |net| times) the fan triangle (apex, u, v) oriented by the
+// record's sign, the apex being the first record's u; triangles through the
+// apex get a zero record.
+__global__ void cap_tris_kernel(const double* __restrict__ V, const int32_t* __restrict__ F,
+                                const int32_t* __restrict__ sorted_tri,
+                                const unsigned long long* __restrict__ key,
+                                const int32_t* __restrict__ order,
+                                const int32_t* __restrict__ rnode,
+                                const int32_t* __restrict__ rinc, const int32_t* __restrict__ rnet,
+                                int64_t nrec, const uint32_t* __restrict__ mult_off,
+                                const uint32_t* __restrict__ cap_off,
+                                const int32_t* __restrict__ first_rec, double cx, double cy,
+                                double cz, double eps, TriF* __restrict__ caps) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nrec) return;
+  const int32_t rec = order[i];
+  const int node = rnode[rec];
+  const unsigned long long k = key[rinc[rec]];
+  const uint32_t u0 = (uint32_t)(k >> 32), v0 = (uint32_t)(k & 0xffffffffu);
+  const int net = rnet[rec];
+  const uint32_t a = net > 0 ? u0 : v0, b = net > 0 ? v0 : u0;
+  const unsigned long long k0 = key[rinc[order[first_rec[node]]]];
+  const uint32_t apex = (uint32_t)(k0 >> 32);
+  const double c[3] = {cx, cy, cz};
+  double p[3][3];
+  const uint32_t vid[3] = {apex, a, b};
+  for (int s = 0; s < 3; ++s)
+    for (int d = 0; d < 3; ++d) p[s][d] = V[(int64_t)vid[s] * 3 + d] - c[d];
+  const bool degenerate = a == apex || b == apex;
+  TriF t = make_trif(p, eps);
+  if (degenerate) {
+    t.r0 = make_float4(0.f, 0.f, 0.f, 0.f);
+    t.r1 = t.r0;
+    t.r2 = t.r0;
+    t.r3 = make_float4(0.f, 0.f, 0.f, -1.f);  // never near: atan2(0, >= 0) = 0
+  }
+  const int reps = abs(net);
+  for (int r = 0; r < reps; ++r) caps[(int64_t)mult_off[i] + r] = t;
+  (void)cap_off;
+}
+
+__global__ void first_record_kernel(const int32_t* __restrict__ order,
+                                    const int32_t* __restrict__ rnode, int64_t nrec,
+                                    int32_t* __restrict__ first_rec,
+                                    const uint32_t* __restrict__ mult_off,
+                                    uint32_t* __restrict__ cap_off,
+                                    uint32_t* __restrict__ cap_cnt) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nrec) return;
+  const int node = rnode[order[i]];
+  if (i == 0 || rnode[order[i - 1]] != node) {
+    first_rec[node] = (int32_t)i;
+    cap_off[node] = mult_off[i];
+  }
+  if (i == nrec - 1 || rnode[order[i + 1]] != node)
+    cap_cnt[node] = mult_off[i + 1] - cap_off[node];
+}
+
+__global__ void leaf_tris_kernel(const double* __restrict__ V, const int32_t* __restrict__ F,
+                                 int64_t nV, const int32_t* __restrict__ sorted_tri, int n,
+                                 double cx, double cy, double cz, double eps,
+                                 TriF* __restrict__ tris, double* __restrict__ tris64) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const int64_t f = sorted_tri[j];
+  const double c[3] = {cx, cy, cz};
+  double p[3][3];
+  for (int s = 0; s < 3; ++s) {
+    int64_t v = F[f * 3 + s];
+    if (v < 0 || v >= nV) v = 0;
+    for (int d = 0; d < 3; ++d) {
+      const double x = V[v * 3 + d];
+      tris64[(int64_t)j * 9 + s * 3 + d] = x;
+      p[s][d] = x - c[d];
+    }
+  }
+  tris[j] = make_trif(p, eps);
+}
+
+// ----------------------------------------------------------------- walk ---
+__device__ __forceinline__ double tri64_term(const double* t, double px, double py, double pz) {
+  return vos_term64(t, t + 3, t + 6, px, py, pz);
+}
+
+template <typename QT>
+__global__ void __launch_bounds__(kT) hier_walk_kernel(HierDev H, const QT* __restrict__ Q,
+                                                       int64_t nQ,
+                                                       const int32_t* __restrict__ perm,
+                                                       double cx, double cy, double cz,
+                                                       double* __restrict__ W,
+                                                       int32_t* __restrict__ redo,
+                                                       uint32_t* __restrict__ nredo) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool valid = i < nQ;
+  const int64_t q = valid ? (perm ? perm[i] : i) : 0;
+  const double px = valid ? (double)Q[q * 3] : 0.0, py = valid ? (double)Q[q * 3 + 1] : 0.0,
+               pz = valid ? (double)Q[q * 3 + 2] : 0.0;
+  const float fx = (float)(px - cx), fy = (float)(py - cy), fz = (float)(pz - cz);
+  float acc = 0.f;
+  double acc64 = 0.0;
+  int resume = valid ? 0 : 0x7fffffff;
+  int x = 0;
+  while (x < H.nnodes) {
+    if (x >= resume) {
+      const NodeH nd = H.nodes[x];
+      const int meta = __float_as_int(nd.hi.w);
+      if (meta <= -2) {
+        const int slot = -2 - meta;
+        const TriF t = H.tris[slot];
+        const float dx = fx - t.r3.x, dy = fy - t.r3.y, dz = fz - t.r3.z;
+        if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < t.r3.w)
+          acc64 += tri64_term(H.tris64 + (int64_t)slot * 9, px, py, pz);
+        else
+          acc += vos_term32(t, fx, fy, fz);
+        resume = x + 1;
+      } else if (meta >= 0 && (fx < nd.lo.x || fx > nd.hi.x || fy < nd.lo.y || fy > nd.hi.y ||
+                               fz < nd.lo.z || fz > nd.hi.z)) {
+        const int cn = H.capn[x];
+        for (int k = 0; k < cn; ++k) acc += vos_term32(H.caps[meta + k], fx, fy, fz);
+        resume = __float_as_int(nd.lo.w);
+      } else {
+        resume = x + 1;
+      }
+    }
+    x = __reduce_min_sync(0xffffffffu, resume);
+  }
+  if (!valid) return;
+  const double w = ((double)acc + acc64) * kInv2Pi;
+  W[q] = w;
+  if (fabs(w - 0.5) <= kBand) redo[atomicAdd(nredo, 1u)] = (int32_t)q;
+}
+
+template <typename QT>
+__global__ void gather_kernel(const QT* __restrict__ Q, const int32_t* __restrict__ list,
+                              const uint32_t* __restrict__ n, double* __restrict__ out) {
+  const uint32_t m = *n;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+    const int64_t q = list[i];
+    for (int d = 0; d < 3; ++d) out[(int64_t)i * 3 + d] = (double)Q[q * 3 + d];
+  }
+}
+
+__global__ void scatter_kernel(const double* __restrict__ Wr, const int32_t* __restrict__ list,
+                               const uint32_t* __restrict__ n, double* __restrict__ W) {
+  const uint32_t m = *n;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
+    W[list[i]] = Wr[i];
+}
+
+}  // namespace
+
+void hier_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, HierTree& h,
+                cudaStream_t st) {
+  h.V = V;
+  h.nV = nV;
+  h.F = F;
+  h.nF = nF;
+  h.n = (int)nF;
+  if (nF == 0) return;
+  GWN_REQUIRE(nF < (int64_t(1) << 30), "at most 2^30-1 triangles");
+  GWN_REQUIRE(nV < (int64_t(1) << 31), "at most 2^31-1 vertices");
+  const int n = (int)nF;
+  const int nn = 2 * n - 1;
+  DevBuf<unsigned long long> mm(6, st);
+  init_minmax(mm.get(), 3, st);
+  launch_kernel(mesh_bbox_kernel, std::min<unsigned>(nblk(nV), 1024u), kT, 0, st, V, nV, mm.get());
+  unsigned long long mmh[6];
+  GWN_CUDA(cudaMemcpyAsync(mmh, mm.get(), sizeof(mmh), cudaMemcpyDeviceToHost, st));
+  GWN_CUDA(cudaStreamSynchronize(st));
+  double diag2 = 0;
+  for (int d = 0; d < 3; ++d) {
+    const double lo = from_ordered_bits(mmh[d]), hi = from_ordered_bits(mmh[3 + d]);
+    h.lo[d] = lo;
+    h.hi[d] = hi;
+    h.c[d] = std::isfinite(lo) && std::isfinite(hi) ? 0.5 * (lo + hi) : 0.0;
+    if (std::isfinite(hi - lo) && hi > lo) diag2 += (hi - lo) * (hi - lo);
+  }
+  h.eps = kNearFrac * std::sqrt(diag2);
+  // Morton order of the triangles
+  DevBuf<unsigned long long> key((size_t)n, st), key_t((size_t)n, st);
+  DevBuf<int32_t> sorted((size_t)n, st), val_t((size_t)n, st);
+  launch_kernel(tri_keys_kernel, nblk(n), kT, 0, st, V, nV, F, nF, (const unsigned long long*)mm.get(),
+                key.get(), sorted.get(), sticky_status_word());
+  radix_sort_pairs<unsigned long long>(key.get(), sorted.get(), key_t.get(), val_t.get(), n, 0, 63,
+                                       st);
+  // radix tree, sizes, boxes, pre-order
+  DevBuf<int32_t> left((size_t)std::max(n - 1, 1), st), right((size_t)std::max(n - 1, 1), st),
+      first((size_t)std::max(n - 1, 1), st), last((size_t)std::max(n - 1, 1), st),
+      parent((size_t)nn, st), size((size_t)nn, st), pre((size_t)nn, st);
+  DevBuf<double> box((size_t)nn * 6, st);
+  DevBuf<unsigned> flags((size_t)std::max(n - 1, 1), st);
+  flags.zero(st);
+  if (n > 1)
+    launch_kernel(radix_tree_kernel, nblk(n - 1), kT, 0, st, (const unsigned long long*)key.get(),
+                  n, left.get(), right.get(), parent.get(), first.get(), last.get());
+  launch_kernel(bottom_up_kernel, nblk(n), kT, 0, st, V, F, nV, (const int32_t*)sorted.get(), n,
+                (const int32_t*)left.get(), (const int32_t*)right.get(),
+                (const int32_t*)parent.get(), box.get(), size.get(), flags.get());
+  launch_kernel(preorder_kernel, nblk(nn), kT, 0, st, (const int32_t*)left.get(),
+                (const int32_t*)parent.get(), (const int32_t*)size.get(), nn, pre.get());
+  // boundary records
+  const int64_t m = 3 * (int64_t)n;
+  DevBuf<unsigned long long> ekey((size_t)m, st), ekey_t((size_t)m, st);
+  DevBuf<int32_t> eval((size_t)m, st), eval_t((size_t)m, st);
+  DevBuf<uint32_t> ps((size_t)m + 1, st), cnt((size_t)m + 1, st);
+  launch_kernel(edge_incidence_kernel, nblk(m), kT, 0, st, F, (const int32_t*)sorted.get(), n,
+                ekey.get(), eval.get());
+  int vbits = 1;
+  while (vbits < 31 && (int64_t(1) << vbits) < nV) ++vbits;
+  // key = u << 32 | v: sort the low vbits of v, then of u
+  radix_sort_pairs<unsigned long long>(ekey.get(), eval.get(), ekey_t.get(), eval_t.get(), m, 0,
+                                       (vbits + 7) / 8 * 8, st);
+  radix_sort_pairs<unsigned long long>(ekey.get(), eval.get(), ekey_t.get(), eval_t.get(), m, 32,
+                                       32 + (vbits + 7) / 8 * 8, st);
+  launch_kernel(sign_flags_kernel, nblk(m + 1), kT, 0, st, F, (const int32_t*)sorted.get(),
+                (const int32_t*)eval.get(), m, ps.get());
+  exclusive_scan_u32(ps.get(), ps.get(), m + 1, st);
+  int64_t nrec = 0;
+  if (n > 1) {
+    launch_kernel(boundary_records_kernel<false>, nblk(m), kT, 0, st,
+                  (const unsigned long long*)ekey.get(), (const int32_t*)eval.get(), m, n,
+                  (const int32_t*)parent.get(), (const int32_t*)first.get(),
+                  (const int32_t*)last.get(), (const int32_t*)pre.get(), (const uint32_t*)ps.get(),
+                  cnt.get(), (const uint32_t*)nullptr, (int32_t*)nullptr, (int32_t*)nullptr,
+                  (int32_t*)nullptr);
+    GWN_CUDA(cudaMemsetAsync(cnt.get() + m, 0, sizeof(uint32_t), st));
+    exclusive_scan_u32(cnt.get(), cnt.get(), m + 1, st);
+    uint32_t tot = 0;
+    GWN_CUDA(cudaMemcpyAsync(&tot, cnt.get() + m, sizeof(tot), cudaMemcpyDeviceToHost, st));
+    GWN_CUDA(cudaStreamSynchronize(st));
+    nrec = tot;
+  }
+  DevBuf<uint32_t> cap_off((size_t)nn, st), cap_cnt((size_t)nn, st);
+  cap_off.zero(st);
+  cap_cnt.zero(st);
+  int64_t ncap = 0;
+  DevBuf<int32_t> rnode, rinc, rnet, order, order_t, first_rec;
+  DevBuf<uint32_t> mult;
+  if (nrec > 0) {
+    rnode.alloc((size_t)nrec, st);
+    rinc.alloc((size_t)nrec, st);
+    rnet.alloc((size_t)nrec, st);
+    launch_kernel(boundary_records_kernel<true>, nblk(m), kT, 0, st,
+                  (const unsigned long long*)ekey.get(), (const int32_t*)eval.get(), m, n,
+                  (const int32_t*)parent.get(), (const int32_t*)first.get(),
+                  (const int32_t*)last.get(), (const int32_t*)pre.get(), (const uint32_t*)ps.get(),
+                  (uint32_t*)nullptr, (const uint32_t*)cnt.get(), rnode.get(), rinc.get(),
+                  rnet.get());
+    // records grouped by node (stable: edge order within a node)
+    DevBuf<uint32_t> nk((size_t)nrec, st), nk_t((size_t)nrec, st);
+    order.alloc((size_t)nrec, st);
+    order_t.alloc((size_t)nrec, st);
+    GWN_CUDA(cudaMemcpyAsync(nk.get(), rnode.get(), (size_t)nrec * 4, cudaMemcpyDeviceToDevice, st));
+    int nbits = 1;
+    while ((1 << nbits) < nn) ++nbits;
+    launch_kernel(iota_records_kernel, nblk(nrec), kT, 0, st, order.get(), nrec);
+    radix_sort_pairs<uint32_t>(nk.get(), order.get(), nk_t.get(), order_t.get(), nrec, 0, nbits, st);
+    mult.alloc((size_t)nrec + 1, st);
+    launch_kernel(record_mult_kernel, nblk(nrec + 1), kT, 0, st, (const int32_t*)rnet.get(),
+                  (const int32_t*)order.get(), nrec, mult.get());
+    exclusive_scan_u32(mult.get(), mult.get(), nrec + 1, st);
+    uint32_t tot = 0;
+    GWN_CUDA(cudaMemcpyAsync(&tot, mult.get() + nrec, sizeof(tot), cudaMemcpyDeviceToHost, st));
+    first_rec.alloc((size_t)nn, st);
+    launch_kernel(first_record_kernel, nblk(nrec), kT, 0, st, (const int32_t*)order.get(),
+                  (const int32_t*)rnode.get(), nrec, first_rec.get(), (const uint32_t*)mult.get(),
+                  cap_off.get(), cap_cnt.get());
+    GWN_CUDA(cudaStreamSynchronize(st));
+    ncap = tot;
+  }
+  h.nnodes = nn;
+  h.ncap = ncap;
+  h.nodes.alloc((size_t)nn * 2);
+  h.capn.alloc((size_t)nn);
+  h.caps.alloc((size_t)std::max<int64_t>(ncap, 1) * 4);
+  h.tris.alloc((size_t)n * 4);
+  h.tris64.alloc((size_t)n * 9);
+  NodeH* nodes = reinterpret_cast<NodeH*>(h.nodes.get());
+  TriF* caps = reinterpret_cast<TriF*>(h.caps.get());
+  TriF* tris = reinterpret_cast<TriF*>(h.tris.get());
+  if (ncap > 0)
+    launch_kernel(cap_tris_kernel, nblk(nrec), kT, 0, st, V, F, (const int32_t*)sorted.get(),
+                  (const unsigned long long*)ekey.get(), (const int32_t*)order.get(),
+                  (const int32_t*)rnode.get(), (const int32_t*)rinc.get(),
+                  (const int32_t*)rnet.get(), nrec, (const uint32_t*)mult.get(),
+                  (const uint32_t*)cap_off.get(), (const int32_t*)first_rec.get(), h.c[0], h.c[1],
+                  h.c[2], h.eps, caps);
+  launch_kernel(node_records_kernel, nblk(nn), kT, 0, st, (const double*)box.get(),
+                (const int32_t*)pre.get(), (const int32_t*)size.get(), n,
+                (const uint32_t*)cap_off.get(), (const uint32_t*)cap_cnt.get(), h.c[0], h.c[1],
+                h.c[2], h.eps, nodes, h.capn.get());
+  launch_kernel(leaf_tris_kernel, nblk(n), kT, 0, st, V, F, nV, (const int32_t*)sorted.get(), n,
+                h.c[0], h.c[1], h.c[2], h.eps, tris, h.tris64.get());
+  GWN_CUDA(cudaStreamSynchronize(st));
+}
+
+void hier_eval(const HierTree& h, const double* Q, int64_t nQ, double* W, cudaStream_t st) {
+  if (nQ == 0) return;
+  if (h.nF == 0) {
+    GWN_CUDA(cudaMemsetAsync(W, 0, (size_t)nQ * 8, st));
+    return;
+  }
+  GWN_REQUIRE(nQ < (int64_t(1) << 31), "at most 2^31-1 queries per call");
+  QueryOrder qo;
+  order_queries(Q, GWN_F64, nQ, h.lo, h.hi, qo, st);
+  DevBuf<int32_t> redo((size_t)nQ, st);
+  DevBuf<uint32_t> nredo(1, st);
+  nredo.zero(st);
+  const HierDev H{reinterpret_cast<const NodeH*>(h.nodes.get()), h.capn.get(),
+                  reinterpret_cast<const TriF*>(h.caps.get()),
+                  reinterpret_cast<const TriF*>(h.tris.get()), h.tris64.get(), (int)h.nnodes};
+  {
+    PhaseTimer ph("hier_walk", st);
+    launch_kernel(hier_walk_kernel<double>, nblk(nQ), kT, 0, st, H, Q, nQ,
+                  (const int32_t*)(qo.active ? qo.perm.get() : nullptr), h.c[0], h.c[1], h.c[2],
+                  W, redo.get(), nredo.get());
+  }
+  // FP64 all-pairs re-evaluation of the results within the band
+  uint32_t nr = 0;
+  GWN_CUDA(cudaMemcpyAsync(&nr, nredo.get(), sizeof(nr), cudaMemcpyDeviceToHost, st));
+  GWN_CUDA(cudaStreamSynchronize(st));
+  if (nr == 0) return;
+  PhaseTimer ph("hier_refine", st);
+  DevBuf<double> Qr((size_t)nr * 3, st), Wr((size_t)nr, st);
+  launch_kernel(gather_kernel<double>, std::min<unsigned>(nblk(nr), 1024u), kT, 0, st, Q,
+                (const int32_t*)redo.get(), (const uint32_t*)nredo.get(), Qr.get());
+  ExactArgs a{h.V, h.nV, 3, h.F, h.nF, Qr.get(), GWN_F64, (int64_t)nr, Wr.get(), GWN_F64,
+              GWN_PLAIN_FP64, false};
+  run_exact(a, st);
+  launch_kernel(scatter_kernel, std::min<unsigned>(nblk(nr), 1024u), kT, 0, st,
+                (const double*)Wr.get(), (const int32_t*)redo.get(), (const uint32_t*)nredo.get(), W);
+}
+
+}  // namespace gwn

@@ -13,6 +13,8 @@ input specification):
   served_meshes: the five benchmark configurations.
 * loops2d / loops2d_queries: closed wavy 2-D polygons (outer loops, holes
   and doubled loops) for the 2-D segment winding number.
+* swept_workload: a deformed ellipsoid under a screw motion and the grid
+  around its sweep, for swept-volume signed distances.
 """
 from __future__ import annotations
 
@@ -365,3 +367,35 @@ def loops2d_queries(n_cells: int = 16, seed: int = 8, nq: int = 10_000_000):
     rng = np.random.default_rng(seed)
     lo, hi = -0.05 * n_cells, 1.05 * n_cells
     return rng.uniform(lo, hi, (nq, 2))
+
+
+def _rotation(axis, ang):
+    axis = np.asarray(axis, float) / np.linalg.norm(axis)
+    K = np.array([[0, -axis[2], axis[1]], [axis[2], 0, -axis[0]], [-axis[1], axis[0], 0]])
+    return np.eye(3) + np.sin(ang) * K + (1 - np.cos(ang)) * K @ K
+
+
+def swept_workload(seed: int = 9, subdiv: int = 5, n_transforms: int = 64, res_max: int = 128):
+    """Icosphere (subdiv: 20*4^subdiv triangles) with a random spherical-harmonic
+    bump field, scaled to an ellipsoid (1, 0.6, 0.4); n_transforms rigid
+    motions x -> L x + t of a screw motion (a turn of 1.5 rad about a tilted
+    axis while moving 3 units along x and 0.5 up and down); a grid over the
+    sweep's box grown by 0.15, res_max points on the longest side, spacing h
+    equal on all sides.  Returns V, F, transforms (nT x 3 x 4), GV, res, h."""
+    rng = np.random.default_rng(seed)
+    V, F = icosphere(subdiv)
+    V = sh_deform(V, rng, lmax=6, sigma=0.06) * np.array([1.0, 0.6, 0.4])
+    T = np.zeros((n_transforms, 3, 4))
+    for k in range(n_transforms):
+        u = k / max(n_transforms - 1, 1)
+        T[k, :, :3] = _rotation([0.3, 1.0, 0.2], 1.5 * u)
+        T[k, :, 3] = [3.0 * u, 0.5 * np.sin(2 * np.pi * u), 0.3 * u]
+    P = np.concatenate([V @ T[k, :, :3].T + T[k, :, 3] for k in range(n_transforms)])
+    lo, hi = P.min(0) - 0.15, P.max(0) + 0.15
+    h = float((hi - lo).max() / (res_max - 1))
+    res = np.floor((hi - lo) / h).astype(np.int32) + 1
+    xs = [lo[d] + h * np.arange(res[d]) for d in range(3)]
+    Z, Y, X = np.meshgrid(xs[2], xs[1], xs[0], indexing="ij")
+    GV = np.ascontiguousarray(np.stack([X.ravel(), Y.ravel(), Z.ravel()], 1))
+    return (np.ascontiguousarray(V), np.ascontiguousarray(F, dtype=np.int32), T, GV,
+            res.astype(np.int32), h)

@@ -20,7 +20,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "liboracle.so")
 REF_SOUP_PATH = os.path.join(HERE, "_ref", "libref_soup.so")
 
-_SOURCES = ["gwn_oracle.cpp", "soup_port.cpp", "soup_hdk.cpp", "wn_hier.cpp", "distance.cpp", "aabb.cpp", "knn.cpp", "eytzinger.cpp"]
+_SOURCES = ["gwn_oracle.cpp", "soup_port.cpp", "soup_hdk.cpp", "wn_hier.cpp", "distance.cpp", "aabb.cpp", "knn.cpp", "eytzinger.cpp", "swept.cpp"]
 
 
 def build(force: bool = False) -> str:
@@ -105,6 +105,8 @@ def lib():
             L.oracle_eytzinger_wn_tree.argtypes = [p, p, i64, C.c_int, p, p]
             L.oracle_eytzinger_wn.argtypes = [p, i64, p, p, p, p, p, i64, p, p, p, C.c_int]
             L.oracle_segments_wn.argtypes = [p, i64, p, p, i64, p]
+        if hasattr(L, "oracle_flood_fill"):
+            L.oracle_flood_fill.argtypes = [p, p]
         if hasattr(L, "oracle_winding_number_hier"):
             L.oracle_winding_number_hier.argtypes = [p, i64, p, i64, p, i64, p, C.c_int]
             L.oracle_winding_number_hier.restype = C.c_int
@@ -474,3 +476,74 @@ def segment_boxes(V, E):
     V, E = _d(V), _i(E)
     A, B = V[E[:, 0]], V[E[:, 1]]
     return np.minimum(A, B), np.maximum(A, B)
+
+
+def flood_fill(res, S):
+    """igl::flood_fill(res,S) restated (swept.cpp): a filled copy of S."""
+    S = np.array(S, dtype=np.float64, copy=True)
+    r = np.ascontiguousarray(res, dtype=np.int32)
+    assert S.size == int(r[0]) * int(r[1]) * int(r[2])
+    lib().oracle_flood_fill(_ptr(r), _ptr(S))
+    return S
+
+
+def swept_volume_signed_distance(V, F, transforms, sign_type, GV, res, h, isolevel, S0=None):
+    """igl::swept_volume_signed_distance(V,F,transforms,sign_type,GV,res,h,
+    isolevel,S0,S) restated (include/igl/swept_volume_signed_distance.cpp:
+    21-160): the transforms in order, each over every grid point (vectorised
+    over the points, which are independent), with the reference's skip rules,
+    AABB closest triangle below (isolevel + sqrt(3) h)^2 (oracle AABB), sign
+    by type (exact winding number, the soup code on the float copy of V, the
+    pseudonormal test) and the running minimum; then flood_fill for a finite
+    isolevel.  transforms: nT x 3 x 4 [linear | translation]."""
+    V, GV = _d(V), _d(GV)
+    F = _d(F, np.int32)
+    T = np.asarray(transforms, dtype=np.float64).reshape(-1, 3, 4)
+    n = GV.shape[0]
+    S = np.full(n, np.nan) if S0 is None else np.array(S0, dtype=np.float64, copy=True)
+    finite = bool(np.isfinite(isolevel))
+    iso = float(isolevel) if finite else np.inf
+    ext = (iso if finite else 0.0) + np.sqrt(3.0) * h
+    min_sqrd = (np.sqrt(3.0) * h + iso) ** 2 if finite else np.inf
+    skip = iso - np.sqrt(3.0) * h
+    if F.shape[0]:
+        lo, hi = V.min(0) - ext, V.max(0) + ext
+        tree = AABB(V, F)
+        soup = None
+        if sign_type == SIGNED_DISTANCE_TYPE_FAST_WINDING_NUMBER:
+            soup = SoupPort(V.astype(np.float32).astype(np.float64), F, order=2)
+        for A in T:
+            L, t = A[:, :3], A[:, 3]
+            act = np.ones(n, bool)
+            if finite:
+                act &= ~((S == S) & (S < skip))
+            d = GV - t
+            gv = np.empty_like(GV)
+            for j in range(3):
+                gv[:, j] = (d[:, 0] * L[0, j] + d[:, 1] * L[1, j]) + d[:, 2] * L[2, j]
+            if finite:
+                act &= np.all((lo <= gv) & (gv <= hi), axis=1)
+            idx = np.flatnonzero(act)
+            if idx.size == 0:
+                continue
+            q = np.ascontiguousarray(gv[idx])
+            sqrd, I, Cp = tree.squared_distance(q, min_sqrd)
+            if sign_type in (SIGNED_DISTANCE_TYPE_WINDING_NUMBER, SIGNED_DISTANCE_TYPE_DEFAULT):
+                s = 1.0 - 2.0 * winding_number(V, F, q)
+            elif sign_type == SIGNED_DISTANCE_TYPE_FAST_WINDING_NUMBER:
+                s = 1.0 - 2.0 * np.abs(soup.eval(q, 2.0))
+            elif sign_type == SIGNED_DISTANCE_TYPE_PSEUDONORMAL:
+                s = np.empty(idx.size)
+                Nrm = np.empty((idx.size, 3))
+                lib().oracle_pseudonormal(_ptr(V), V.shape[0], _ptr(F), F.shape[0], _ptr(q),
+                                          idx.size, _ptr(I), _ptr(Cp), _ptr(s), _ptr(Nrm))
+            else:
+                s = np.ones(idx.size)
+            ok = sqrd < min_sqrd
+            sd = s * np.sqrt(sqrd)
+            cur = S[idx]
+            new = np.where(cur == cur, np.where(sd < cur, sd, cur), sd)
+            S[idx[ok]] = new[ok]
+    if finite:
+        S = flood_fill(res, S)
+    return S

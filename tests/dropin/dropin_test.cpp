@@ -5,6 +5,7 @@
 // plus the octree and exact winding number on the same data.  Prints
 // "name value" lines that the Python test compares with the CPU oracle.
 #include <cmath>
+#include <limits>
 #include <cstdio>
 #include <vector>
 
@@ -13,9 +14,11 @@
 #include <igl/eytzinger_aabb.h>
 #include <igl/eytzinger_aabb_winding_number.h>
 #include <igl/eytzinger_aabb_winding_number_tree.h>
+#include <igl/flood_fill.h>
 #include <igl/knn.h>
 #include <igl/octree.h>
 #include <igl/signed_distance.h>
+#include <igl/swept_volume_signed_distance.h>
 #include <igl/winding_number.h>
 
 static int failures = 0;
@@ -148,6 +151,36 @@ int main() {
     check_near("eytzinger_wn_batch0", Wq(0), 1.0, 1e-6);
     check_near("eytzinger_wn_batch1", Wq(1), 0.0, 1e-6);
     check_near("eytzinger_wn_batch2", Wq(2), 1.0, 1e-6);
+  }
+  // flood fill: one signed cell fills a 3 x 2 x 2 grid
+  {
+    Eigen::VectorXd S(12);
+    for (int i = 0; i < 12; ++i) S(i) = std::nan("");
+    S(7) = 0.75;
+    Eigen::Matrix<int, 1, 3> res;
+    res.set({3, 2, 2});
+    igl::flood_fill(res, S);
+    for (int i = 0; i < 12; ++i) check_near("flood_fill", S(i), 0.75, 0.0);
+  }
+  // swept volume of the unit tet under the identity and a unit shift in x:
+  // unsigned distances 2 below the first copy's bottom face and sqrt(4.005)
+  // from the shifted copy's vertex (2, 0, 0)
+  {
+    Eigen::MatrixXd Vt(4, 3);
+    Vt.set({0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 1});
+    Eigen::MatrixXi Ft(4, 3);
+    Ft.set({0, 2, 1, 0, 3, 2, 0, 1, 3, 1, 2, 3});
+    std::vector<Eigen::Affine3d> Ts(2);
+    Ts[1](0, 3) = 1.0;
+    Eigen::MatrixXd GVt(2, 3);
+    GVt.set({0.1, 0.1, -2.0, 4.0, 0.05, 0.05});
+    Eigen::Matrix<int, 1, 3> res;
+    res.set({2, 1, 1});
+    Eigen::VectorXd St;
+    igl::swept_volume_signed_distance(Vt, Ft, Ts, igl::SIGNED_DISTANCE_TYPE_UNSIGNED, GVt, res,
+                                      0.1, std::numeric_limits<double>::infinity(), St);
+    check_near("swept_below", St(0), 2.0, 1e-12);
+    check_near("swept_vertex", St(1), std::sqrt(4.005), 1e-12);
   }
   std::printf("failures %d\n", failures);
   return failures ? 1 : 0;
