@@ -252,6 +252,24 @@ int gwn_signed_distance(const double* P, int64_t nP, const double* V, int64_t nV
                         int precision, int mem, void* stream);
 
 /* ------------------------------------------------------------------------
+ * Hierarchical exact winding number (igl::WindingNumberAABB,
+ * include/igl/WindingNumberAABB.h:23-60 over WindingNumberTree.h:263-350):
+ * a tree over the mesh whose nodes carry the cap (fan over the node's
+ * boundary edges) that replaces the node's triangles for points outside its
+ * box.  The value is the exact winding number's (gwn_winding_number) up to
+ * rounding.  gwn_wn_aabb_build copies V (#V x 3 float64) and F (#F x 3
+ * int32) to the device; gwn_wn_aabb_eval evaluates Q (#Q x 3 float64) in
+ * mixed precision (FP32 terms at least 1e-3 x the mesh diagonal from the
+ * query, FP64 nearer, FP64 all-pairs for results within 1e-3 of 0.5).
+ * ---------------------------------------------------------------------- */
+typedef struct gwn_wn_aabb gwn_wn_aabb;
+int gwn_wn_aabb_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, int mem,
+                      void* stream, gwn_wn_aabb** out);
+int gwn_wn_aabb_eval(const gwn_wn_aabb* tree, const double* Q, int64_t nQ, double* W, int mem,
+                     void* stream);
+void gwn_wn_aabb_free(gwn_wn_aabb* tree);
+
+/* ------------------------------------------------------------------------
  * Swept volumes (the batched caller of the winding number and the signed
  * distance on grids).
  *

@@ -35,6 +35,7 @@ __all__ = [
     "fast_winding_number_cloud", "fast_winding_number_cloud_oneshot", "device_status",
     "Server", "signed_distance", "knn", "eytzinger_aabb", "eytzinger_aabb_winding_number_tree",
     "eytzinger_aabb_winding_number", "swept_volume_signed_distance", "flood_fill",
+    "WindingNumberAABB",
 ]
 
 _PREC = {"fp64": N.GWN_PLAIN_FP64, "plain": N.GWN_PLAIN_FP64, "mixed": N.GWN_MIXED}
@@ -466,6 +467,46 @@ def knn(P, V, k: int):
     N.check(N.load().gwn_knn(Pa.ptr, Pa.shape[0], Va.ptr, Va.shape[0], int(k), _ptr_of(I),
                              Pa.mem, stream))
     return I
+
+
+# ------------------------------------------ hierarchical exact winding --
+class WindingNumberAABB:
+    """igl::WindingNumberAABB (include/igl/WindingNumberAABB.h) on the GPU:
+    the exact winding number of a triangle mesh through a tree of boundary
+    caps.  ``WindingNumberAABB(V, F).winding_number(Q)``; V, F host arrays or
+    CUDA tensors (copied to the device), Q likewise."""
+
+    def __init__(self, V, F):
+        Va = _Arg(V, np.float64)
+        Fa = _Arg(F, np.int32, allowed=(np.int32,))
+        _same_mem(Va, Fa)
+        if Va.shape[1:] != (3,) or Fa.shape[1:] != (3,):
+            raise ValueError("V must be #V x 3 and F #F x 3")
+        self._h = C.c_void_p()
+        stream = _stream_ptr() if Va.mem == N.GWN_DEVICE else None
+        N.check(N.load().gwn_wn_aabb_build(Va.ptr, Va.shape[0], Fa.ptr, Fa.shape[0], Va.mem,
+                                           stream, C.byref(self._h)))
+
+    def winding_number(self, Q):
+        Qa = _Arg(Q, np.float64)
+        if len(Qa.shape) != 2 or Qa.shape[1] != 3:
+            raise ValueError("Q must be #Q x 3")
+        W = _empty_like_mem(Qa.mem, (Qa.shape[0],), np.float64, like=Qa)
+        stream = _stream_ptr() if Qa.mem == N.GWN_DEVICE else None
+        N.check(N.load().gwn_wn_aabb_eval(self._h, Qa.ptr, Qa.shape[0], _ptr_of(W), Qa.mem,
+                                          stream))
+        return W
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            N.load().gwn_wn_aabb_free(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ------------------------------------------- 2-D Eytzinger AABB winding --

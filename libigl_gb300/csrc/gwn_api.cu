@@ -4,6 +4,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -201,6 +202,12 @@ struct gwn_octree {
 };
 struct gwn_cloud {
   gwn_cloud_impl impl;
+};
+struct gwn_wn_aabb {
+  int device = 0;
+  DevMem<double> V;
+  DevMem<int32_t> F;
+  HierTree tree;
 };
 
 namespace {
@@ -900,5 +907,54 @@ int gwn_flood_fill(const int32_t* res, double* S, int mem, void* stream) {
     }
   });
 }
+
+int gwn_wn_aabb_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, int mem,
+                      void* stream, gwn_wn_aabb** out) {
+  return guarded("gwn_wn_aabb_build", [&] {
+    GWN_REQUIRE(out != nullptr, "out must be non-null");
+    *out = nullptr;
+    GWN_REQUIRE(nV >= 0 && nF >= 0, "sizes must be non-negative");
+    GWN_REQUIRE(nF == 0 || (V && F), "V and F must be non-null");
+    check_mem(mem);
+    ensure_device();
+    cudaStream_t st = as_stream(stream);
+    auto h = std::make_unique<gwn_wn_aabb>();
+    GWN_CUDA(cudaGetDevice(&h->device));
+    h->V.alloc((size_t)std::max<int64_t>(nV, 1) * 3);
+    h->F.alloc((size_t)std::max<int64_t>(nF, 1) * 3);
+    const cudaMemcpyKind kind = mem == GWN_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    if (nV) GWN_CUDA(cudaMemcpyAsync(h->V.get(), V, (size_t)nV * 24, kind, st));
+    if (nF) GWN_CUDA(cudaMemcpyAsync(h->F.get(), F, (size_t)nF * 12, kind, st));
+    DeviceStatus status(st, true);
+    hier_build(h->V.get(), nV, h->F.get(), nF, h->tree, status.ptr(), st);
+    status.check(st, "wn_aabb_build");
+    *out = h.release();
+  });
+}
+
+int gwn_wn_aabb_eval(const gwn_wn_aabb* tree, const double* Q, int64_t nQ, double* W, int mem,
+                     void* stream) {
+  return guarded("gwn_wn_aabb_eval", [&] {
+    profile_begin_call();
+    GWN_REQUIRE(tree != nullptr, "tree handle is null");
+    GWN_REQUIRE(nQ >= 0, "nQ must be non-negative");
+    GWN_REQUIRE(nQ == 0 || (Q && W), "Q and W must be non-null");
+    GWN_REQUIRE(nQ < (int64_t(1) << 31), "at most 2^31-1 queries per call");
+    check_mem(mem);
+    ensure_device();
+    check_device_of(tree->device);
+    if (nQ == 0) return;
+    cudaStream_t st = as_stream(stream);
+    Staged<double> dQ(Q, (size_t)nQ * 3, mem, st);
+    Staged<double> dW(W, (size_t)nQ, mem, st, false);
+    hier_eval(tree->tree, dQ.dev, nQ, dW.dev, st);
+    if (mem == GWN_HOST) {
+      GWN_CUDA(cudaMemcpyAsync(W, dW.dev, (size_t)nQ * 8, cudaMemcpyDeviceToHost, st));
+      GWN_CUDA(cudaStreamSynchronize(st));
+    }
+  });
+}
+
+void gwn_wn_aabb_free(gwn_wn_aabb* tree) { delete tree; }
 
 }  // extern "C"

@@ -80,8 +80,9 @@ struct HierTree {
   DevMem<float4> tris;    // 4 per leaf triangle
   DevMem<double> tris64;  // 9 per leaf triangle
 };
+// Out-of-range triangle indices set kStatusBadInput in *status.
 void hier_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, HierTree& h,
-                cudaStream_t st);
+                unsigned* status, cudaStream_t st);
 // W of every query (FP64 device arrays), mixed precision; synchronizes `st`.
 void hier_eval(const HierTree& h, const double* Q, int64_t nQ, double* W, cudaStream_t st);
 

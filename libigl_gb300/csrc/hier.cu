@@ -222,15 +222,18 @@ __global__ void preorder_kernel(const int32_t* __restrict__ left,
 
 // Directed-edge incidences of the sorted triangles: key {u < v} packed, value
 // 3 j + c (leaf position j, corner c: edge from corner c to corner c+1).
+// (Indices out of range, already reported by tri_keys_kernel, read as 0.)
 __global__ void edge_incidence_kernel(const int32_t* __restrict__ F,
-                                      const int32_t* __restrict__ sorted_tri, int n,
+                                      const int32_t* __restrict__ sorted_tri, int n, int64_t nV,
                                       unsigned long long* __restrict__ key,
                                       int32_t* __restrict__ val) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= 3 * (int64_t)n) return;
   const int64_t j = i / 3, c = i % 3;
   const int64_t f = sorted_tri[j];
-  const uint32_t a = (uint32_t)max(F[f * 3 + c], 0), b = (uint32_t)max(F[f * 3 + (c + 1) % 3], 0);
+  const int32_t fa = F[f * 3 + c], fb = F[f * 3 + (c + 1) % 3];
+  const uint32_t a = (fa < 0 || fa >= nV) ? 0u : (uint32_t)fa;
+  const uint32_t b = (fb < 0 || fb >= nV) ? 0u : (uint32_t)fb;
   const uint32_t u = min(a, b), v = max(a, b);
   key[i] = ((unsigned long long)u << 32) | v;
   val[i] = (int32_t)i;
@@ -239,7 +242,7 @@ __global__ void edge_incidence_kernel(const int32_t* __restrict__ F,
 __device__ __forceinline__ int edge_sign(const int32_t* F, const int32_t* sorted_tri, int32_t e) {
   const int64_t j = e / 3, c = e % 3;
   const int64_t f = sorted_tri[j];
-  return F[f * 3 + c] < F[f * 3 + (c + 1) % 3] ? 1 : -1;
+  return F[f * 3 + c] < F[f * 3 + (c + 1) % 3] ? 1 : -1;  // orientation of {u < v}
 }
 
 __global__ void sign_flags_kernel(const int32_t* __restrict__ F,
@@ -412,12 +415,13 @@ __global__ void cap_tris_kernel(const double* __restrict__ V, const int32_t* __r
   (void)cap_off;
 }
 
+// Per node with records: its first record (position in the node-sorted
+// order) and the offset of its cap triangles.
 __global__ void first_record_kernel(const int32_t* __restrict__ order,
                                     const int32_t* __restrict__ rnode, int64_t nrec,
                                     int32_t* __restrict__ first_rec,
                                     const uint32_t* __restrict__ mult_off,
-                                    uint32_t* __restrict__ cap_off,
-                                    uint32_t* __restrict__ cap_cnt) {
+                                    uint32_t* __restrict__ cap_off) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= nrec) return;
   const int node = rnode[order[i]];
@@ -425,6 +429,18 @@ __global__ void first_record_kernel(const int32_t* __restrict__ order,
     first_rec[node] = (int32_t)i;
     cap_off[node] = mult_off[i];
   }
+}
+
+// Per node with records: the number of its cap triangles (launched after
+// first_record_kernel, whose offsets it reads).
+__global__ void cap_count_kernel(const int32_t* __restrict__ order,
+                                 const int32_t* __restrict__ rnode, int64_t nrec,
+                                 const uint32_t* __restrict__ mult_off,
+                                 const uint32_t* __restrict__ cap_off,
+                                 uint32_t* __restrict__ cap_cnt) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nrec) return;
+  const int node = rnode[order[i]];
   if (i == nrec - 1 || rnode[order[i + 1]] != node)
     cap_cnt[node] = mult_off[i + 1] - cap_off[node];
 }
@@ -523,14 +539,14 @@ __global__ void scatter_kernel(const double* __restrict__ Wr, const int32_t* __r
 }  // namespace
 
 void hier_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, HierTree& h,
-                cudaStream_t st) {
+                unsigned* status, cudaStream_t st) {
   h.V = V;
   h.nV = nV;
   h.F = F;
   h.nF = nF;
   h.n = (int)nF;
   if (nF == 0) return;
-  GWN_REQUIRE(nF < (int64_t(1) << 30), "at most 2^30-1 triangles");
+  GWN_REQUIRE(nF < (int64_t(1) << 29), "at most 2^29-1 triangles");
   GWN_REQUIRE(nV < (int64_t(1) << 31), "at most 2^31-1 vertices");
   const int n = (int)nF;
   const int nn = 2 * n - 1;
@@ -553,7 +569,7 @@ void hier_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, HierT
   DevBuf<unsigned long long> key((size_t)n, st), key_t((size_t)n, st);
   DevBuf<int32_t> sorted((size_t)n, st), val_t((size_t)n, st);
   launch_kernel(tri_keys_kernel, nblk(n), kT, 0, st, V, nV, F, nF, (const unsigned long long*)mm.get(),
-                key.get(), sorted.get(), sticky_status_word());
+                key.get(), sorted.get(), status);
   radix_sort_pairs<unsigned long long>(key.get(), sorted.get(), key_t.get(), val_t.get(), n, 0, 63,
                                        st);
   // radix tree, sizes, boxes, pre-order
@@ -577,7 +593,7 @@ void hier_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, HierT
   DevBuf<int32_t> eval((size_t)m, st), eval_t((size_t)m, st);
   DevBuf<uint32_t> ps((size_t)m + 1, st), cnt((size_t)m + 1, st);
   launch_kernel(edge_incidence_kernel, nblk(m), kT, 0, st, F, (const int32_t*)sorted.get(), n,
-                ekey.get(), eval.get());
+                nV, ekey.get(), eval.get());
   int vbits = 1;
   while (vbits < 31 && (int64_t(1) << vbits) < nV) ++vbits;
   // key = u << 32 | v: sort the low vbits of v, then of u
@@ -637,7 +653,10 @@ void hier_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, HierT
     first_rec.alloc((size_t)nn, st);
     launch_kernel(first_record_kernel, nblk(nrec), kT, 0, st, (const int32_t*)order.get(),
                   (const int32_t*)rnode.get(), nrec, first_rec.get(), (const uint32_t*)mult.get(),
-                  cap_off.get(), cap_cnt.get());
+                  cap_off.get());
+    launch_kernel(cap_count_kernel, nblk(nrec), kT, 0, st, (const int32_t*)order.get(),
+                  (const int32_t*)rnode.get(), nrec, (const uint32_t*)mult.get(),
+                  (const uint32_t*)cap_off.get(), cap_cnt.get());
     GWN_CUDA(cudaStreamSynchronize(st));
     ncap = tot;
   }

@@ -11,8 +11,9 @@
 // kernel applies the two skip rules and compacts the surviving points with
 // their inverse-transformed positions, the library's closest-triangle search
 // (bounded) runs on that batch, the points it found closer than the bound
-// are compacted again, and the sign (exact winding number, soup fast winding
-// number or pseudonormal) and a min-update kernel run on those.  Each grid
+// are compacted again, and the sign (exact winding number: the cap
+// hierarchy of hier.cu in mixed precision, all pairs in FP64; soup fast
+// winding number; or pseudonormal) and a min-update kernel run on those.  Each grid
 // point sees the transforms in the reference's order, so the skip rule (which
 // depends on the running minimum) gives the reference's result.  The mesh's
 // search tree, soup tree and pseudonormals are built once.
@@ -269,10 +270,14 @@ void swept_volume_run(const double* V, int64_t nV, const int32_t* F, int64_t nF,
                   256, 0, st, V, nV, mm.get());
     gwn_soup_impl tree;
     PseudonormalData pn;
+    HierTree hier;
+    const bool use_hier = (sign_type == GWN_SD_WINDING_NUMBER || sign_type == GWN_SD_DEFAULT) &&
+                          precision == GWN_MIXED;
     {
       PhaseTimer ph("build", st);
       soup_build(tree, V, nV, F, nF, 2, true, st);
       if (sign_type == GWN_SD_PSEUDONORMAL) pseudonormal_precompute(V, nV, F, nF, pn, st);
+      if (use_hier) hier_build(V, nV, F, nF, hier, sticky_status_word(), st);
     }
     DevBuf<double> Q((size_t)nG * 3, st), sqrD((size_t)nG, st), C((size_t)nG * 3, st),
         W((size_t)nG, st), Q2((size_t)nG * 3, st), d2((size_t)nG, st), C2((size_t)nG * 3, st);
@@ -314,7 +319,9 @@ void swept_volume_run(const double* V, int64_t nV, const int32_t* F, int64_t nF,
                     min_sqrd, Q2.get(), g2.get(), d2.get(), I2.get(), C2.get(), cnt.get() + 1);
       const unsigned m = read_count(1);
       if (m == 0) continue;
-      if (mode == 1) {
+      if (mode == 1 && use_hier) {
+        hier_eval(hier, Q2.get(), m, W.get(), st);
+      } else if (mode == 1) {
         ExactArgs a{V, nV, 3, F, nF, Q2.get(), GWN_F64, (int64_t)m, W.get(), GWN_F64, precision,
                     false};
         run_exact(a, st);

@@ -14,6 +14,7 @@
 #include <igl/eytzinger_aabb.h>
 #include <igl/eytzinger_aabb_winding_number.h>
 #include <igl/eytzinger_aabb_winding_number_tree.h>
+#include <igl/WindingNumberAABB.h>
 #include <igl/flood_fill.h>
 #include <igl/knn.h>
 #include <igl/octree.h>
@@ -181,6 +182,21 @@ int main() {
                                       0.1, std::numeric_limits<double>::infinity(), St);
     check_near("swept_below", St(0), 2.0, 1e-12);
     check_near("swept_vertex", St(1), std::sqrt(4.005), 1e-12);
+  }
+  // WindingNumberAABB: unit tet, outward
+  {
+    Eigen::MatrixXd Vt(4, 3);
+    Vt.set({0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 1});
+    Eigen::MatrixXi Ft(4, 3);
+    Ft.set({0, 2, 1, 0, 3, 2, 0, 1, 3, 1, 2, 3});
+    igl::WindingNumberAABB<double, int> hier;
+    hier.set_mesh(Vt, Ft);
+    hier.grow();
+    Eigen::RowVector3d pin, pout;
+    pin.set({0.1, 0.1, 0.1});
+    pout.set({2, 2, 2});
+    check_near("wn_aabb_inside", hier.winding_number(pin), 1.0, 1e-6);
+    check_near("wn_aabb_outside", hier.winding_number(pout), 0.0, 1e-6);
   }
   std::printf("failures %d\n", failures);
   return failures ? 1 : 0;
