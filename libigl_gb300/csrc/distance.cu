@@ -82,11 +82,18 @@ struct ClosestParams {
 // depth must stay below it (checked on the host, else the walk is used).
 constexpr int kStack = 96;
 
+// Best candidate so far: squared distance, slot, closest point, and an FP32
+// upper bound of the distance (sqrt(d2) rounded up) for the pruning tests.
 struct Best {
   double d2;
   int slot;
   D3 c;
+  float bound;
 };
+
+__device__ __forceinline__ float dist_bound(double d2) {
+  return __fsqrt_ru(__double2float_ru(d2));
+}
 
 // Squared distance from p to triangle (a, b, c) in FP32, same regions.
 __device__ float dist2_triangle32(float px, float py, float pz, float ax, float ay, float az,
@@ -129,29 +136,34 @@ __device__ float dist2_triangle32(float px, float py, float pz, float ax, float 
   return dx * dx + dy * dy + dz * dz;
 }
 
-// FP32 screen of a leaf: true when the triangle cannot be strictly closer
-// than the current best (its FP32 distance minus the triangle's stored
-// slack and the query-rounding slack 1e-6 (S + d) is still at least it).
+// FP32 screen of a leaf: true when the triangle is farther than the
+// current best (its FP32 distance minus the triangle's stored slack and the
+// query-rounding slack 1e-6 (S + d) is above the best's upper bound).
 __device__ __forceinline__ bool screened_out(const ClosestParams& prm, int slot, float fx,
-                                             float fy, float fz, float S, double best) {
+                                             float fy, float fz, float S, float bound) {
   const float4 t0 = __ldg(&prm.tf[(int64_t)slot * 3]);
   const float4 t1 = __ldg(&prm.tf[(int64_t)slot * 3 + 1]);
   const float4 t2 = __ldg(&prm.tf[(int64_t)slot * 3 + 2]);
   const float d = sqrtf(dist2_triangle32(fx, fy, fz, t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z,
                                          t1.w, t2.x));
   const float lower = d - t2.y - 1e-6f * (S + d);
-  return lower > 0.f && (double)lower * (double)lower >= best;
+  return lower > bound;
 }
 
+// A candidate replaces the best when strictly closer, or equally close with
+// a smaller input triangle index: with pruning only of what is strictly
+// farther, every triangle at the smallest distance is evaluated, so the
+// result does not depend on the visiting order.
 __device__ __forceinline__ void eval_leaf(const ClosestParams& prm, int slot, D3 q, Best& b) {
   const double* t = prm.td + (int64_t)slot * 9;
   const D3 cp = closest_on_triangle(q, {t[0], t[1], t[2]}, {t[3], t[4], t[5]}, {t[6], t[7], t[8]});
   const D3 d = dsub(q, cp);
   const double d2 = ddot(d, d);
-  if (d2 < b.d2) {
+  if (d2 < b.d2 || (d2 == b.d2 && b.slot >= 0 && prm.tri_index[slot] < prm.tri_index[b.slot])) {
     b.d2 = d2;
     b.slot = slot;
     b.c = cp;
+    b.bound = dist_bound(d2);
   }
 }
 
@@ -191,7 +203,7 @@ __global__ void __launch_bounds__(128) closest_kernel(ClosestParams prm, const Q
   const bool walk = valid && finite && prm.nnodes > 0;
   const float fx = (float)q.x, fy = (float)q.y, fz = (float)q.z;
   const float S = fmaxf(fabsf(fx), fmaxf(fabsf(fy), fabsf(fz))) + prm.cmax;
-  Best b{up_sqr_d, -1, {0, 0, 0}};
+  Best b{up_sqr_d, -1, {0, 0, 0}, dist_bound(up_sqr_d)};
   // 1. greedy descent to one leaf: an initial bound
   if (walk) {
     int n = 0;
@@ -220,7 +232,7 @@ __global__ void __launch_bounds__(128) closest_kernel(ClosestParams prm, const Q
     if (node >= resume) {
       const bool leaf = link < 0;
       const float lb = sphere_lower_bound(a, fx, fy, fz, S);
-      if (lb > 0.f && (double)lb * (double)lb >= b.d2) {
+      if (lb > b.bound) {
         resume = leaf ? node + 1 : link;
       } else if (leaf) {
         eval_leaf(prm, ~link, q, b);
@@ -274,7 +286,7 @@ __global__ void __launch_bounds__(128) closest_dfs_kernel(ClosestParams prm,
   if (i >= nQ) return;
   const int64_t qi = perm ? (int64_t)perm[i] : i;
   const D3 q{(double)Q[qi * 3], (double)Q[qi * 3 + 1], (double)Q[qi * 3 + 2]};
-  Best b{up_sqr_d, -1, {0, 0, 0}};
+  Best b{up_sqr_d, -1, {0, 0, 0}, dist_bound(up_sqr_d)};
   if (isfinite(q.x) && isfinite(q.y) && isfinite(q.z) && prm.nnodes > 0) {
     const float fx = (float)q.x, fy = (float)q.y, fz = (float)q.z;
     const float S = fmaxf(fabsf(fx), fmaxf(fabsf(fy), fabsf(fz))) + prm.cmax;
@@ -288,9 +300,9 @@ __global__ void __launch_bounds__(128) closest_dfs_kernel(ClosestParams prm,
       --sp;
       const int ref = stk_n[sp];
       const float lb = stk_lb[sp];
-      if ((double)lb * (double)lb >= b.d2) continue;
+      if (lb > b.bound) continue;
       if (ref < 0) {
-        if (!screened_out(prm, ~ref, fx, fy, fz, S, b.d2)) eval_leaf(prm, ~ref, q, b);
+        if (!screened_out(prm, ~ref, fx, fy, fz, S, b.bound)) eval_leaf(prm, ~ref, q, b);
         continue;
       }
       const float4* sn = prm.snode + 4 * (int64_t)ref;
@@ -302,7 +314,7 @@ __global__ void __launch_bounds__(128) closest_dfs_kernel(ClosestParams prm,
       const bool left_first = lbl <= lbr;
       const int far_n = left_first ? r : l, near_n = left_first ? l : r;
       const float far_lb = left_first ? lbr : lbl, near_lb = left_first ? lbl : lbr;
-      if ((double)far_lb * (double)far_lb < b.d2) {
+      if (!(far_lb > b.bound)) {
         if (sp == kStack) {
           atomicOr(status, kStatusBadInput);
           break;
@@ -311,7 +323,7 @@ __global__ void __launch_bounds__(128) closest_dfs_kernel(ClosestParams prm,
         stk_lb[sp] = far_lb;
         ++sp;
       }
-      if ((double)near_lb * (double)near_lb < b.d2) {
+      if (!(near_lb > b.bound)) {
         if (sp == kStack) {
           atomicOr(status, kStatusBadInput);
           break;
