@@ -6,17 +6,20 @@
 // point is carried into the mesh's frame by the inverse of the rigid motion,
 // ((g - t) L), points outside the mesh box grown by isolevel + sqrt(3) h are
 // skipped, and the closest triangle below (isolevel + sqrt(3) h)^2 gives
-// s sqrt(d2) (s from the sign type), kept as the running minimum.  Here every
-// transform is one pass over all grid points on the device: an activation
-// kernel applies the two skip rules and compacts the surviving points with
-// their inverse-transformed positions, the library's closest-triangle search
-// (bounded) runs on that batch, the points it found closer than the bound
-// are compacted again, and the sign (exact winding number: the cap
-// hierarchy of hier.cu in mixed precision, all pairs in FP64; soup fast
-// winding number; or pseudonormal) and a min-update kernel run on those.  Each grid
-// point sees the transforms in the reference's order, so the skip rule (which
-// depends on the running minimum) gives the reference's result.  The mesh's
-// search tree, soup tree and pseudonormals are built once.
+// s sqrt(d2) (s from the sign type), kept as the running minimum.  Here the
+// transforms go through in chunks of up to 16: an activation kernel takes
+// every grid point not yet below the skip level (the running minimum only
+// decreases, so such a point is skipped by the whole chunk) with every
+// transform of the chunk, applies the box rule and compacts the surviving
+// (point, transform) pairs; the library's bounded closest-triangle search
+// runs on that batch, the pairs closer than the bound are compacted again
+// and signed (exact winding number: the cap hierarchy of hier.cu in mixed
+// precision, all pairs in FP64; soup fast winding number; or pseudonormal),
+// and their values land in a per-chunk table.  A last kernel replays the
+// chunk's transforms in order for every point with the reference's skip
+// rule and running minimum, so values the reference would not have computed
+// are ignored and the result is the reference's.  The mesh's search tree,
+// soup tree, cap hierarchy and pseudonormals are built once.
 //
 // Flood fill.  The reference scans the grid once (x fastest) and fills each
 // unsigned (NaN) cell from the signed cells around it.  Its result, read off
@@ -61,84 +64,110 @@ __global__ void mesh_box_kernel(const double* __restrict__ V, int64_t nV,
   }
 }
 
-struct Affine {
-  double m[12];  // rows of [L | t]
-};
-
 struct SweepParams {
   bool finite_iso;
   double skip_below;  // isolevel - sqrt(3) h
   double ext;         // box growth
 };
 
-// The reference's two skip rules and ((g - t) L) for the surviving points,
-// compacted into Q / gidx (order of the batch: arbitrary).
-__global__ void activate_kernel(const double* __restrict__ GV, int64_t nG,
-                                const double* __restrict__ S, Affine A, SweepParams sp,
-                                const unsigned long long* __restrict__ mm,
-                                double* __restrict__ Q, int32_t* __restrict__ gidx,
-                                unsigned* __restrict__ cnt) {
+// Transforms go through in chunks of K.  For a chunk: every grid point not
+// already deeper than the skip level (the running minimum only decreases,
+// so such a point is skipped by every transform of the chunk) and every
+// transform k of the chunk: the inverse motion ((g - t) L, products and sums
+// unfused in the reference's order) and the box test; surviving (point,
+// transform) pairs are compacted into Q / gidx / kidx (batch order:
+// arbitrary).
+__global__ void activate_chunk_kernel(const double* __restrict__ GV, int64_t nG,
+                                      const double* __restrict__ S,
+                                      const double* __restrict__ T, int K, SweepParams sp,
+                                      const unsigned long long* __restrict__ mm,
+                                      double* __restrict__ Q, int32_t* __restrict__ gidx,
+                                      int32_t* __restrict__ kidx, unsigned* __restrict__ cnt) {
   const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (g >= nG) return;
   const double sg = S[g];
   if (sp.finite_iso && sg == sg && sg < sp.skip_below) return;
-  const double d0 = __dsub_rn(GV[g * 3], A.m[3]), d1 = __dsub_rn(GV[g * 3 + 1], A.m[7]),
-               d2 = __dsub_rn(GV[g * 3 + 2], A.m[11]);
-  double gv[3];
-  for (int j = 0; j < 3; ++j)
-    gv[j] = __dadd_rn(__dadd_rn(__dmul_rn(d0, A.m[j]), __dmul_rn(d1, A.m[4 + j])),
-                      __dmul_rn(d2, A.m[8 + j]));
-  if (sp.finite_iso) {
-    for (int j = 0; j < 3; ++j) {
-      const double lo = __dsub_rn(from_ordered_bits(mm[j]), sp.ext);
-      const double hi = __dadd_rn(from_ordered_bits(mm[3 + j]), sp.ext);
-      if (!(lo <= gv[j] && gv[j] <= hi)) return;
-    }
+  const double x = GV[g * 3], y = GV[g * 3 + 1], z = GV[g * 3 + 2];
+  double lo[3], hi[3];
+  for (int j = 0; j < 3; ++j) {
+    lo[j] = __dsub_rn(from_ordered_bits(mm[j]), sp.ext);
+    hi[j] = __dadd_rn(from_ordered_bits(mm[3 + j]), sp.ext);
   }
-  const unsigned k = atomicAdd(cnt, 1u);
-  Q[(int64_t)k * 3] = gv[0];
-  Q[(int64_t)k * 3 + 1] = gv[1];
-  Q[(int64_t)k * 3 + 2] = gv[2];
-  gidx[k] = (int32_t)g;
+  for (int k = 0; k < K; ++k) {
+    const double* A = T + 12 * k;
+    const double d0 = __dsub_rn(x, A[3]), d1 = __dsub_rn(y, A[7]), d2 = __dsub_rn(z, A[11]);
+    double gv[3];
+    bool inside = true;
+    for (int j = 0; j < 3; ++j) {
+      gv[j] = __dadd_rn(__dadd_rn(__dmul_rn(d0, A[j]), __dmul_rn(d1, A[4 + j])),
+                        __dmul_rn(d2, A[8 + j]));
+      inside &= lo[j] <= gv[j] && gv[j] <= hi[j];
+    }
+    if (sp.finite_iso && !inside) continue;
+    const unsigned i = atomicAdd(cnt, 1u);
+    Q[(int64_t)i * 3] = gv[0];
+    Q[(int64_t)i * 3 + 1] = gv[1];
+    Q[(int64_t)i * 3 + 2] = gv[2];
+    gidx[i] = (int32_t)g;
+    kidx[i] = k;
+  }
 }
 
-// The batch's points closer than the bound (the only ones the reference
+// The batch's pairs closer than the bound (the only ones the reference
 // signs), compacted with their distance, closest face and point.
 __global__ void select_kernel(int64_t n, const double* __restrict__ Q,
-                              const int32_t* __restrict__ gidx, const double* __restrict__ sqrD,
-                              const int32_t* __restrict__ I, const double* __restrict__ C,
-                              double min_sqrd, double* __restrict__ Q2, int32_t* __restrict__ g2,
-                              double* __restrict__ d2, int32_t* __restrict__ I2,
-                              double* __restrict__ C2, unsigned* __restrict__ cnt) {
-  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (k >= n || !(sqrD[k] < min_sqrd)) return;
+                              const int32_t* __restrict__ gidx, const int32_t* __restrict__ kidx,
+                              const double* __restrict__ sqrD, const int32_t* __restrict__ I,
+                              const double* __restrict__ C, double min_sqrd,
+                              double* __restrict__ Q2, int32_t* __restrict__ g2,
+                              int32_t* __restrict__ k2, double* __restrict__ d2,
+                              int32_t* __restrict__ I2, double* __restrict__ C2,
+                              unsigned* __restrict__ cnt) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n || !(sqrD[i] < min_sqrd)) return;
   const int64_t j = atomicAdd(cnt, 1u);
   for (int c = 0; c < 3; ++c) {
-    Q2[j * 3 + c] = Q[k * 3 + c];
-    C2[j * 3 + c] = C[k * 3 + c];
+    Q2[j * 3 + c] = Q[i * 3 + c];
+    C2[j * 3 + c] = C[i * 3 + c];
   }
-  g2[j] = gidx[k];
-  d2[j] = sqrD[k];
-  I2[j] = I[k];
+  g2[j] = gidx[i];
+  k2[j] = kidx[i];
+  d2[j] = sqrD[i];
+  I2[j] = I[i];
 }
 
-// S(g) = min(S(g), s sqrt(d2)) for the batch's points closer than the bound
-// (std::min's operand order; a NaN S(g) takes the new value).
-__global__ void update_kernel(int64_t n, const int32_t* __restrict__ gidx,
-                              const double* __restrict__ sqrD, const double* __restrict__ W,
-                              int mode, double min_sqrd, double* __restrict__ S) {
-  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  const double d2 = sqrD[k];
+// SD[k nG + g] = s sqrt(d2) for the pairs closer than the bound (s from the
+// sign mode: 1, 1 - 2 W, 1 - 2 |W|, or the pseudonormal sign W).
+__global__ void scatter_sd_kernel(int64_t n, const int32_t* __restrict__ gidx,
+                                  const int32_t* __restrict__ kidx,
+                                  const double* __restrict__ sqrD,
+                                  const double* __restrict__ W, int mode, double min_sqrd,
+                                  int64_t nG, double* __restrict__ SD) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double d2 = sqrD[i];
   if (!(d2 < min_sqrd)) return;
   double s = 1.0;
-  if (mode == 1) s = 1.0 - 2.0 * W[k];
-  else if (mode == 2) s = 1.0 - 2.0 * fabs(W[k]);
-  else if (mode == 3) s = W[k];
-  const double sd = s * sqrt(d2);
-  const int64_t g = gidx[k];
-  const double cur = S[g];
-  S[g] = cur == cur ? (sd < cur ? sd : cur) : sd;
+  if (mode == 1) s = 1.0 - 2.0 * W[i];
+  else if (mode == 2) s = 1.0 - 2.0 * fabs(W[i]);
+  else if (mode == 3) s = W[i];
+  SD[(int64_t)kidx[i] * nG + gidx[i]] = s * sqrt(d2);
+}
+
+// The reference's loop over the chunk's transforms for every grid point, in
+// order: stop at the skip level, else S = min(S, value) where the transform
+// produced one (std::min's operand order; a NaN S takes the value).
+__global__ void update_chunk_kernel(int64_t nG, int K, const double* __restrict__ SD,
+                                    SweepParams sp, double* __restrict__ S) {
+  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (g >= nG) return;
+  double cur = S[g];
+  for (int k = 0; k < K; ++k) {
+    if (sp.finite_iso && cur == cur && cur < sp.skip_below) break;
+    const double v = SD[(int64_t)k * nG + g];
+    if (v == v) cur = cur == cur ? (v < cur ? v : cur) : v;
+  }
+  S[g] = cur;
 }
 
 // ------------------------------------------------------------ flood fill --
@@ -279,10 +308,17 @@ void swept_volume_run(const double* V, int64_t nV, const int32_t* F, int64_t nF,
       if (sign_type == GWN_SD_PSEUDONORMAL) pseudonormal_precompute(V, nV, F, nF, pn, st);
       if (use_hier) hier_build(V, nV, F, nF, hier, sticky_status_word(), st);
     }
-    DevBuf<double> Q((size_t)nG * 3, st), sqrD((size_t)nG, st), C((size_t)nG * 3, st),
-        W((size_t)nG, st), Q2((size_t)nG * 3, st), d2((size_t)nG, st), C2((size_t)nG * 3, st);
-    DevBuf<int32_t> gidx((size_t)nG, st), I((size_t)nG, st), g2((size_t)nG, st),
-        I2((size_t)nG, st);
+    // up to 16 transforms per chunk, about 8M (point, transform) slots
+    const int K = (int)std::max<int64_t>(1, std::min<int64_t>(16, (int64_t(8) << 20) / nG));
+    const int64_t cap = nG * K;
+    GWN_REQUIRE(cap < (int64_t(1) << 31), "too many grid points");
+    DevBuf<double> Tdev((size_t)nT * 12, st);
+    Tdev.upload(transforms_host, (size_t)nT * 12, st);
+    DevBuf<double> Q((size_t)cap * 3, st), sqrD((size_t)cap, st), C((size_t)cap * 3, st),
+        W((size_t)cap, st), Q2((size_t)cap * 3, st), d2((size_t)cap, st), C2((size_t)cap * 3, st),
+        SD((size_t)cap, st);
+    DevBuf<int32_t> gidx((size_t)cap, st), kidx((size_t)cap, st), I((size_t)cap, st),
+        g2((size_t)cap, st), k2((size_t)cap, st), I2((size_t)cap, st);
     DevBuf<unsigned> cnt(2, st);
     auto read_count = [&](int which) {
       unsigned v = 0;
@@ -295,46 +331,57 @@ void swept_volume_run(const double* V, int64_t nV, const int32_t* F, int64_t nF,
     else if (sign_type == GWN_SD_FAST_WINDING_NUMBER) mode = 2;
     else if (sign_type == GWN_SD_PSEUDONORMAL) mode = 3;
     const unsigned grid = (unsigned)((nG + 255) / 256);
-    for (int64_t t = 0; t < nT; ++t) {
-      Affine A;
-      for (int k = 0; k < 12; ++k) A.m[k] = transforms_host[t * 12 + k];
+    auto blocks = [](int64_t n) { return (unsigned)std::max<int64_t>(1, (n + 255) / 256); };
+    for (int64_t t0 = 0; t0 < nT; t0 += K) {
+      const int Kc = (int)std::min<int64_t>(K, nT - t0);
       cnt.zero(st);
+      GWN_CUDA(cudaMemsetAsync(SD.get(), 0xff, (size_t)nG * Kc * sizeof(double), st));  // NaN
       {
         PhaseTimer ph("activate", st);
-        launch_kernel(activate_kernel, grid, 256, 0, st, GV, nG, (const double*)S, A, sp,
-                      (const unsigned long long*)mm.get(), Q.get(), gidx.get(), cnt.get());
+        launch_kernel(activate_chunk_kernel, grid, 256, 0, st, GV, nG, (const double*)S,
+                      (const double*)(Tdev.get() + t0 * 12), Kc, sp,
+                      (const unsigned long long*)mm.get(), Q.get(), gidx.get(), kidx.get(),
+                      cnt.get());
       }
       const unsigned n = read_count(0);
-      if (n == 0) continue;
-      soup_squared_distance(tree, Q.get(), GWN_F64, n, min_sqrd, sqrD.get(), I.get(), C.get(), st);
-      if (mode == 0) {
-        launch_kernel(update_kernel, (unsigned)((n + 255) / 256), 256, 0, st, (int64_t)n,
-                      (const int32_t*)gidx.get(), (const double*)sqrD.get(),
-                      (const double*)W.get(), mode, min_sqrd, S);
-        continue;
+      if (n > 0) {
+        soup_squared_distance(tree, Q.get(), GWN_F64, n, min_sqrd, sqrD.get(), I.get(), C.get(),
+                              st);
+        if (mode == 0) {
+          launch_kernel(scatter_sd_kernel, blocks(n), 256, 0, st, (int64_t)n,
+                        (const int32_t*)gidx.get(), (const int32_t*)kidx.get(),
+                        (const double*)sqrD.get(), (const double*)nullptr, mode, min_sqrd, nG,
+                        SD.get());
+        } else {
+          launch_kernel(select_kernel, blocks(n), 256, 0, st, (int64_t)n, (const double*)Q.get(),
+                        (const int32_t*)gidx.get(), (const int32_t*)kidx.get(),
+                        (const double*)sqrD.get(), (const int32_t*)I.get(),
+                        (const double*)C.get(), min_sqrd, Q2.get(), g2.get(), k2.get(), d2.get(),
+                        I2.get(), C2.get(), cnt.get() + 1);
+          const unsigned m = read_count(1);
+          if (m > 0) {
+            if (mode == 1 && use_hier) {
+              hier_eval(hier, Q2.get(), m, W.get(), st);
+            } else if (mode == 1) {
+              ExactArgs a{V, nV, 3, F, nF, Q2.get(), GWN_F64, (int64_t)m, W.get(), GWN_F64,
+                          precision, false};
+              run_exact(a, st);
+            } else if (mode == 2) {
+              soup_eval(tree, 2.0f, Q2.get(), GWN_F64, m, W.get(), GWN_F64, precision, st);
+            } else {
+              PhaseTimer ph("pseudonormal", st);
+              pseudonormal_apply(pn, Q2.get(), m, V, F, nF, I2.get(), C2.get(), d2.get(),
+                                 W.get(), nullptr, st);
+            }
+            launch_kernel(scatter_sd_kernel, blocks(m), 256, 0, st, (int64_t)m,
+                          (const int32_t*)g2.get(), (const int32_t*)k2.get(),
+                          (const double*)d2.get(), (const double*)W.get(), mode, min_sqrd, nG,
+                          SD.get());
+          }
+        }
       }
-      launch_kernel(select_kernel, (unsigned)((n + 255) / 256), 256, 0, st, (int64_t)n,
-                    (const double*)Q.get(), (const int32_t*)gidx.get(),
-                    (const double*)sqrD.get(), (const int32_t*)I.get(), (const double*)C.get(),
-                    min_sqrd, Q2.get(), g2.get(), d2.get(), I2.get(), C2.get(), cnt.get() + 1);
-      const unsigned m = read_count(1);
-      if (m == 0) continue;
-      if (mode == 1 && use_hier) {
-        hier_eval(hier, Q2.get(), m, W.get(), st);
-      } else if (mode == 1) {
-        ExactArgs a{V, nV, 3, F, nF, Q2.get(), GWN_F64, (int64_t)m, W.get(), GWN_F64, precision,
-                    false};
-        run_exact(a, st);
-      } else if (mode == 2) {
-        soup_eval(tree, 2.0f, Q2.get(), GWN_F64, m, W.get(), GWN_F64, precision, st);
-      } else {
-        PhaseTimer ph("pseudonormal", st);
-        pseudonormal_apply(pn, Q2.get(), m, V, F, nF, I2.get(), C2.get(), d2.get(), W.get(),
-                           nullptr, st);
-      }
-      launch_kernel(update_kernel, (unsigned)((m + 255) / 256), 256, 0, st, (int64_t)m,
-                    (const int32_t*)g2.get(), (const double*)d2.get(), (const double*)W.get(),
-                    mode, min_sqrd, S);
+      PhaseTimer ph("update", st);
+      launch_kernel(update_chunk_kernel, grid, 256, 0, st, nG, Kc, (const double*)SD.get(), sp, S);
     }
   }
   if (finite_iso) {
