@@ -40,8 +40,7 @@ constexpr int kKnnMaxK = 64;
 constexpr int kKnnStack = 192;
 
 struct KnnTree {
-  const double* cn;
-  const double* w;
+  const float4* box;  // per cell: {lo.xyz, count}, {hi.xyz, 0}, FP32 rounded outward
   const int32_t* ch;
   const int64_t* start;
   const int32_t* count;
@@ -134,21 +133,32 @@ struct Heap {
   }
 };
 
-// FP32 lower bound of the distance from q to cell c's cube (centre cn, width
-// w), box rounded outward; minus 1e-6 (S + d) for the query's rounding.
-__device__ __forceinline__ float cell_lower_bound(const KnnTree& t, int c, float fx, float fy,
-                                                  float fz, float S) {
-  const double h = 0.5 * t.w[c];
-  float d2 = 0.f;
-  const float fq[3] = {fx, fy, fz};
-#pragma unroll
+// Cell boxes for the search: the cube (centre cn, width w) rounded outward
+// to FP32, and the cell's point count.
+__global__ void cell_boxes_kernel(const double* __restrict__ cn, const double* __restrict__ w,
+                                  const int32_t* __restrict__ count, int64_t ncells,
+                                  float4* __restrict__ box) {
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  const double h = 0.5 * w[c];
+  float lo[3], hi[3];
   for (int a = 0; a < 3; ++a) {
-    const double cc = t.cn[(int64_t)c * 3 + a];
-    const float lo = __double2float_rd(cc - h), hi = __double2float_ru(cc + h);
-    const float e = fmaxf(fmaxf(lo - fq[a], fq[a] - hi), 0.f);
-    d2 = fmaf(e, e, d2);
+    const double cc = cn[c * 3 + a];
+    lo[a] = __double2float_rd(cc - h);
+    hi[a] = __double2float_ru(cc + h);
   }
-  const float d = sqrtf(d2);
+  box[2 * c] = make_float4(lo[0], lo[1], lo[2], __int_as_float(count[c]));
+  box[2 * c + 1] = make_float4(hi[0], hi[1], hi[2], 0.f);
+}
+
+// FP32 lower bound of the distance from q to a cell's box; minus 1e-6 (S + d)
+// for the query's rounding.
+__device__ __forceinline__ float cell_lower_bound(float4 lo, float4 hi, float fx, float fy,
+                                                  float fz, float S) {
+  const float ex = fmaxf(fmaxf(lo.x - fx, fx - hi.x), 0.f);
+  const float ey = fmaxf(fmaxf(lo.y - fy, fy - hi.y), 0.f);
+  const float ez = fmaxf(fmaxf(lo.z - fz, fz - hi.z), 0.f);
+  const float d = sqrtf(fmaf(ez, ez, fmaf(ey, ey, ex * ex)));
   return fmaxf(d - 1e-6f * (S + d), 0.f);
 }
 
@@ -166,6 +176,9 @@ __global__ void __launch_bounds__(128) knn_octree_kernel(KnnTree t, const QT* __
   double hd[kKnnMaxK];
   int32_t hi[kKnnMaxK];
   Heap heap{hd, hi, 0, k};
+  // FP32 upper bound of the k-th distance once the heap is full (pruning
+  // only what is strictly farther)
+  float kbound = INFINITY;
   int stk[kKnnStack];
   float slb[kKnnStack];
   int sp = 0;
@@ -176,10 +189,11 @@ __global__ void __launch_bounds__(128) knn_octree_kernel(KnnTree t, const QT* __
     --sp;
     const int c = stk[sp];
     const float lb = slb[sp];
-    if (heap.n == k && (double)lb > heap.d[0]) continue;
+    if (lb > kbound) continue;
     if (t.ch[(int64_t)c * 8] < 0) {  // leaf: its first point (knn.cpp:121-125)
       const int32_t p = t.perm[t.start[c]];
       heap.offer(point_dist(t.P, p, qx, qy, qz), p);
+      if (heap.n == k) kbound = __double2float_ru(heap.d[0]);
       continue;
     }
     int cc[8];
@@ -187,9 +201,10 @@ __global__ void __launch_bounds__(128) knn_octree_kernel(KnnTree t, const QT* __
     int m = 0;
     for (int o = 0; o < 8; ++o) {
       const int x = t.ch[(int64_t)c * 8 + o];
-      if (t.count[x] == 0) continue;
-      const float l = cell_lower_bound(t, x, fx, fy, fz, S);
-      if (heap.n == k && (double)l > heap.d[0]) continue;
+      const float4 blo = __ldg(&t.box[2 * (int64_t)x]);
+      if (__float_as_int(blo.w) == 0) continue;  // empty cell
+      const float l = cell_lower_bound(blo, __ldg(&t.box[2 * (int64_t)x + 1]), fx, fy, fz, S);
+      if (l > kbound) continue;
       int j = m++;  // insertion by descending bound: the nearest ends up last (popped first)
       while (j > 0 && cl[j - 1] < l) {
         cc[j] = cc[j - 1];
@@ -295,8 +310,12 @@ static void knn_t(const gwn_octree_impl& tree, const QT* Q, int64_t nQ, int64_t 
   GWN_CUDA(cudaStreamSynchronize(st));
   double cmax;
   std::memcpy(&cmax, &mxh, 8);
-  KnnTree t{tree.cn.get(), tree.w.get(), tree.ch.get(), tree.start.get(), tree.count.get(),
-            tree.perm.get(), tree.P.get(), tree.n, (float)cmax};
+  DevBuf<float4> box((size_t)tree.ncells * 2, st);
+  launch_kernel(cell_boxes_kernel, (unsigned)((tree.ncells + 255) / 256), 256, 0, st,
+                (const double*)tree.cn.get(), (const double*)tree.w.get(),
+                (const int32_t*)tree.count.get(), tree.ncells, box.get());
+  KnnTree t{box.get(), tree.ch.get(), tree.start.get(), tree.count.get(), tree.perm.get(),
+            tree.P.get(), tree.n, (float)cmax};
   DevBuf<int32_t> over((size_t)nQ, st);
   DevBuf<unsigned> nover(1, st);
   nover.zero(st);
