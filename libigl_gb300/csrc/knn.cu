@@ -28,7 +28,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 
+#include "bh_common.cuh"
 #include "gwn_common.cuh"
 #include "gwn_internal.cuh"
 #include "octree.cuh"
@@ -164,12 +166,14 @@ __device__ __forceinline__ float cell_lower_bound(float4 lo, float4 hi, float fx
 
 template <typename QT>
 __global__ void __launch_bounds__(128) knn_octree_kernel(KnnTree t, const QT* __restrict__ Q,
-                                                         int64_t nQ, int k,
+                                                         int64_t nQ,
+                                                         const int32_t* __restrict__ perm, int k,
                                                          int32_t* __restrict__ I,
                                                          int32_t* __restrict__ overflow,
                                                          unsigned* __restrict__ n_overflow) {
-  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (q >= nQ) return;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nQ) return;
+  const int64_t q = perm ? (int64_t)perm[i] : i;
   const double qx = (double)Q[q * 3], qy = (double)Q[q * 3 + 1], qz = (double)Q[q * 3 + 2];
   const float fx = (float)qx, fy = (float)qy, fz = (float)qz;
   const float S = fmaxf(fabsf(fx), fmaxf(fabsf(fy), fabsf(fz))) + t.cmax;
@@ -316,11 +320,22 @@ static void knn_t(const gwn_octree_impl& tree, const QT* Q, int64_t nQ, int64_t 
                 (const int32_t*)tree.count.get(), tree.ncells, box.get());
   KnnTree t{box.get(), tree.ch.get(), tree.start.get(), tree.count.get(), tree.perm.get(),
             tree.P.get(), tree.n, (float)cmax};
+  // queries grouped by Morton cell of the root cube, so neighbouring threads
+  // walk the same cells
+  double root[4];
+  GWN_CUDA(cudaMemcpyAsync(root, tree.cn.get(), 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  GWN_CUDA(cudaMemcpyAsync(root + 3, tree.w.get(), sizeof(double), cudaMemcpyDeviceToHost, st));
+  GWN_CUDA(cudaStreamSynchronize(st));
+  const double lo[3] = {root[0] - 0.5 * root[3], root[1] - 0.5 * root[3], root[2] - 0.5 * root[3]};
+  const double hi[3] = {root[0] + 0.5 * root[3], root[1] + 0.5 * root[3], root[2] + 0.5 * root[3]};
+  QueryOrder qo;
+  order_queries(Q, std::is_same<QT, double>::value ? GWN_F64 : GWN_F32, nQ, lo, hi, qo, st);
   DevBuf<int32_t> over((size_t)nQ, st);
   DevBuf<unsigned> nover(1, st);
   nover.zero(st);
-  launch_kernel(knn_octree_kernel<QT>, (unsigned)((nQ + 127) / 128), 128, 0, st, t, Q, nQ, (int)kk,
-                I, over.get(), nover.get());
+  launch_kernel(knn_octree_kernel<QT>, (unsigned)((nQ + 127) / 128), 128, 0, st, t, Q, nQ,
+                (const int32_t*)(qo.active ? qo.perm.get() : nullptr), (int)kk, I, over.get(),
+                nover.get());
   unsigned no = 0;
   GWN_CUDA(cudaMemcpyAsync(&no, nover.get(), 4, cudaMemcpyDeviceToHost, st));
   GWN_CUDA(cudaStreamSynchronize(st));
