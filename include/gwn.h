@@ -73,7 +73,7 @@ int gwn_device_status(unsigned int* flags, int clear);
  * dim = 3: V is nV x 3, F is nF x 3 (triangles), O is nO x 3.
  * dim = 2: V is nV x 2, F is nF x 2 (edges),     O is nO x 2.
  * W (nO) receives sum over elements of solid angle / 4pi (or angle / 2pi).
- * GWN_MIXED with dim = 3, float64 O and W, at least 16384 triangles and 1024
+ * GWN_MIXED with dim = 3, float64 O and W, at least 4096 triangles and 1024
  * queries evaluates through the cap hierarchy of gwn_wn_aabb (same value up
  * to rounding, built for the call); otherwise every pair is summed.
  * ---------------------------------------------------------------------- */

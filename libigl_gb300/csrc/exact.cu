@@ -45,7 +45,7 @@ constexpr int kTile64 = 64;       // triangles per FP64 tile
 constexpr double kNearFrac = 1e-3;
 // Mixed-precision calls with at least this many triangles and queries use
 // the cap hierarchy; below, building it costs about what all pairs do.
-constexpr int64_t kHierMinTriangles = 16384;
+constexpr int64_t kHierMinTriangles = 4096;
 constexpr int64_t kHierMinQueries = 1024;
 constexpr double kBand = 1e-3;    // |W - 0.5| band that triggers FP64 re-evaluation
 constexpr float kInv2PiF = 0.15915494309189533577f;

@@ -6,7 +6,8 @@
 // over the cap's triangles.  The value is the all-pairs sum's up to
 // rounding.
 //
-// Build.  Triangles are ordered along a Morton curve of their centroids and
+// Build.  Triangles are ordered along a Morton curve of their centroids (a
+// 1024^3 grid over the mesh box; ties by input order) and
 // a binary radix tree is built over that order (every internal node covers
 // a contiguous range of leaves); nodes are laid out in pre-order with a link
 // one past each subtree.  A node's boundary: over its triangles' directed
@@ -113,7 +114,7 @@ __global__ void tri_keys_kernel(const double* __restrict__ V, int64_t nV,
     const double ext = hi - lo;
     double t = ext > 0 ? (c[d] / 3.0 - lo) / ext : 0.0;
     t = fmin(fmax(t, 0.0), 1.0);  // NaN -> 0
-    code |= spread21((uint64_t)(t * 2097151.0)) << (2 - d);
+    code |= spread21((uint64_t)(t * 1023.0)) << (2 - d);
   }
   key[f] = code;
   val[f] = (int32_t)f;
@@ -652,6 +653,7 @@ void hier_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, HierT
   GWN_REQUIRE(nV < (int64_t(1) << 31), "at most 2^31-1 vertices");
   const int n = (int)nF;
   const int nn = 2 * n - 1;
+  PhaseTimer ph_all("hier_build", st);
   DevBuf<unsigned long long> mm(6, st);
   init_minmax(mm.get(), 3, st);
   launch_kernel(mesh_bbox_kernel, std::min<unsigned>(nblk(nV), 1024u), kT, 0, st, V, nV, mm.get());
@@ -672,7 +674,7 @@ void hier_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, HierT
   DevBuf<int32_t> sorted((size_t)n, st), val_t((size_t)n, st);
   launch_kernel(tri_keys_kernel, nblk(n), kT, 0, st, V, nV, F, nF, (const unsigned long long*)mm.get(),
                 key.get(), sorted.get(), status);
-  radix_sort_pairs<unsigned long long>(key.get(), sorted.get(), key_t.get(), val_t.get(), n, 0, 63,
+  radix_sort_pairs<unsigned long long>(key.get(), sorted.get(), key_t.get(), val_t.get(), n, 0, 30,
                                        st);
   // radix tree, sizes, boxes, pre-order
   DevBuf<int32_t> left((size_t)std::max(n - 1, 1), st), right((size_t)std::max(n - 1, 1), st),
