@@ -730,6 +730,55 @@ __global__ void __launch_bounds__(128) cloud_eval_fp64_kernel(CloudEvalParams pr
   if (valid) W[qi] = (WT)acc;
 }
 
+// FP64 re-evaluation of the listed queries (results within the band of
+// 0.5), one warp per query: the lanes share the query's walk (the listed
+// queries lie anywhere on the surface, so a warp of 32 of them would walk
+// the union of 32 walks); a leaf's dipoles are split over the lanes, a far
+// cell's expansion is evaluated by one lane, and the lanes' sums are added
+// at the end.
+template <typename QT, typename WT>
+__global__ void __launch_bounds__(128) cloud_refine_warp_kernel(CloudEvalParams prm,
+                                                                const QT* __restrict__ Q,
+                                                                const int32_t* __restrict__ list,
+                                                                const unsigned* __restrict__ count,
+                                                                WT* __restrict__ W) {
+  const unsigned n = *count;
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t w = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); w < (int64_t)n;
+       w += nwarps) {
+    const int64_t qi = list[w];
+    const double qx = (double)Q[qi * 3], qy = (double)Q[qi * 3 + 1], qz = (double)Q[qi * 3 + 2];
+    double acc = 0.0;
+    int node = 0;
+    while (node < prm.nnodes) {
+      const CloudNodeD* r = prm.nd + node;
+      const int4 l = r->l;
+      if (l.w) {
+        for (int j = lane; j < l.z; j += 32) {
+          const double* pd = prm.pd + ((int64_t)l.y + j) * 6;
+          acc += dipole64(pd[0] - qx, pd[1] - qy, pd[2] - qz, pd[3], pd[4], pd[5]);
+        }
+        node = l.x;
+      } else if (node == 0) {
+        node = 1;
+      } else if (far64(qx, qy, qz, r->cm, r->r, prm.beta)) {
+        if (lane == 0) {
+          const double lx = __dsub_rn(r->cm[0], qx), ly = __dsub_rn(r->cm[1], qy),
+                       lz = __dsub_rn(r->cm[2], qz);
+          const double rr = sqrt(lx * lx + ly * ly + lz * lz);
+          acc += expansion<double>(r->ec, lx, ly, lz, rr, prm.num_terms);
+        }
+        node = l.x;
+      } else {
+        node = node + 1;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) W[qi] = (WT)acc;
+  }
+}
+
 // beta <= 0: direct sum over every point (:300-310).  FP64 plain, or FP32
 // with FP64 near-field dipoles.
 template <typename QT, typename WT, bool kMixed>
@@ -1108,8 +1157,8 @@ static void cloud_eval_t(const gwn_cloud_impl& c, double beta, const void* Qv, i
     GWN_CUDA(cudaGetLastError());
     {
       PhaseTimer ph("refine", st);
-      launch_kernel(cloud_eval_fp64_kernel<QT, WT>, grid, 128, 0, st, prm, Q, nullptr, list.get(),
-                                                           count.get(), nQ, W);
+      launch_kernel(cloud_refine_warp_kernel<QT, WT>, (unsigned)(num_sms() * 8), 128, 0, st, prm,
+                    Q, (const int32_t*)list.get(), (const unsigned*)count.get(), W);
     }
     GWN_CUDA(cudaGetLastError());
   } else {
