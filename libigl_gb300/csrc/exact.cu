@@ -542,6 +542,12 @@ void launch_exact2(const ExactArgs& a, cudaStream_t st) {
 
 }  // namespace
 
+void exact_refine_listed(const double* tris64, int64_t nF, const double* Q, const int32_t* list,
+                         const unsigned* count, double* W, cudaStream_t st) {
+  launch_kernel(exact3_refine_kernel<double, double>, num_sms() * 4, kThreads, 0, st, tris64, nF, Q,
+                W, list, count);
+}
+
 void run_exact(const ExactArgs& a, cudaStream_t st) {
   const bool qd = a.q_dtype == GWN_F64, wd = a.w_dtype == GWN_F64;
   if (a.dim == 3) {

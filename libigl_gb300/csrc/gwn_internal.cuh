@@ -27,6 +27,12 @@ struct ExactArgs {
 
 void run_exact(const ExactArgs& a, cudaStream_t st);
 
+// FP64 all-pairs winding number of the listed queries (W[list[j]] for j <
+// *count, read on the device), one block per query; tris64 holds nF
+// triangles as 9 doubles (a, b, c).
+void exact_refine_listed(const double* tris64, int64_t nF, const double* Q, const int32_t* list,
+                         const unsigned* count, double* W, cudaStream_t st);
+
 // No-allocation exact winding number (device pointers, mixed precision,
 // triangles); scratch in a static device array of fixed capacity.
 int64_t noalloc_max_triangles();

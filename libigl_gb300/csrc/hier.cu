@@ -38,7 +38,7 @@
 // every record and the query are hi + lo FP32 pairs, so every difference
 // a - q is accurate to FP32 rounding of the difference itself; terms are
 // summed with compensation.  Results within 1e-3 of 0.5 are redone by the
-// FP64 all-pairs kernel.
+// FP64 all-pairs kernel, one block per query.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -622,22 +622,7 @@ __global__ void __launch_bounds__(kT) hier_walk_kernel(HierDev H, const QT* __re
   if (fabs(w - 0.5) <= kBand) redo[atomicAdd(nredo, 1u)] = (int32_t)q;
 }
 
-template <typename QT>
-__global__ void gather_kernel(const QT* __restrict__ Q, const int32_t* __restrict__ list,
-                              const uint32_t* __restrict__ n, double* __restrict__ out) {
-  const uint32_t m = *n;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
-    const int64_t q = list[i];
-    for (int d = 0; d < 3; ++d) out[(int64_t)i * 3 + d] = (double)Q[q * 3 + d];
-  }
-}
 
-__global__ void scatter_kernel(const double* __restrict__ Wr, const int32_t* __restrict__ list,
-                               const uint32_t* __restrict__ n, double* __restrict__ W) {
-  const uint32_t m = *n;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
-    W[list[i]] = Wr[i];
-}
 
 }  // namespace
 
@@ -811,20 +796,10 @@ void hier_eval(const HierTree& h, const double* Q, int64_t nQ, double* W, cudaSt
                   (const int32_t*)(qo.active ? qo.perm.get() : nullptr), h.c[0], h.c[1], h.c[2],
                   W, redo.get(), nredo.get());
   }
-  // FP64 all-pairs re-evaluation of the results within the band
-  uint32_t nr = 0;
-  GWN_CUDA(cudaMemcpyAsync(&nr, nredo.get(), sizeof(nr), cudaMemcpyDeviceToHost, st));
-  GWN_CUDA(cudaStreamSynchronize(st));
-  if (nr == 0) return;
+  // FP64 all-pairs re-evaluation of the results within the band, one block
+  // per listed query
   PhaseTimer ph("hier_refine", st);
-  DevBuf<double> Qr((size_t)nr * 3, st), Wr((size_t)nr, st);
-  launch_kernel(gather_kernel<double>, std::min<unsigned>(nblk(nr), 1024u), kT, 0, st, Q,
-                (const int32_t*)redo.get(), (const uint32_t*)nredo.get(), Qr.get());
-  ExactArgs a{h.V, h.nV, 3, h.F, h.nF, Qr.get(), GWN_F64, (int64_t)nr, Wr.get(), GWN_F64,
-              GWN_PLAIN_FP64, false};
-  run_exact(a, st);
-  launch_kernel(scatter_kernel, std::min<unsigned>(nblk(nr), 1024u), kT, 0, st,
-                (const double*)Wr.get(), (const int32_t*)redo.get(), (const uint32_t*)nredo.get(), W);
+  exact_refine_listed(h.tris64.get(), h.nF, Q, redo.get(), nredo.get(), W, st);
 }
 
 }  // namespace gwn
