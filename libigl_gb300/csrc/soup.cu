@@ -10,9 +10,11 @@
 //  build (all on the device)
 //   1. per triangle: FP64 bounding box and centroid; boxes with a non-finite
 //      coordinate are excluded, as UT_BVH::init does (FWNFS.h:4606-4615);
-//   2. 63-bit Morton key of the centroid, stable radix sort;
-//   3. binary radix tree over the sorted keys (internal node i splits at the
-//      highest differing key bit, ties broken by index);
+//   2. 63-bit Morton key of the centroid, stable radix sort (the starting
+//      order of the build);
+//   3. binary tree, top-down: binned splits that minimise the children's
+//      (triangles x squared box diagonal), exact object splits below 33
+//      triangles (soup_tree.cu);
 //   4. one bottom-up pass: each leaf computes the HDK per-triangle data
 //      (area-weighted normal N, centroid P, the second-moment integrals
 //      Nijk; FWNFS.h:6668-6890), and the second thread to reach an internal
@@ -285,44 +287,6 @@ __global__ void tri_keys_kernel(const double* __restrict__ V, int64_t nV,
   vals[f] = (int32_t)f;
 }
 
-__device__ __forceinline__ int delta_key(const unsigned long long* keys, int n, int i, int j) {
-  if (j < 0 || j >= n) return -1;
-  const unsigned long long a = keys[i], b = keys[j];
-  if (a == b) return 64 + __clz((unsigned)(i ^ j));
-  return __clzll((long long)(a ^ b));
-}
-
-// Binary radix tree over n sorted keys: internal nodes 0..n-2, leaf j is node n-1+j.
-__global__ void radix_tree_kernel(const unsigned long long* __restrict__ keys, int n,
-                                  int32_t* __restrict__ left, int32_t* __restrict__ right,
-                                  int32_t* __restrict__ parent) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n - 1) return;
-  const int d = (delta_key(keys, n, i, i + 1) - delta_key(keys, n, i, i - 1)) >= 0 ? 1 : -1;
-  const int dmin = delta_key(keys, n, i, i - d);
-  int lmax = 2;
-  while (delta_key(keys, n, i, i + lmax * d) > dmin) lmax <<= 1;
-  int l = 0;
-  for (int t = lmax >> 1; t >= 1; t >>= 1)
-    if (delta_key(keys, n, i, i + (l + t) * d) > dmin) l += t;
-  const int j = i + l * d;
-  const int dnode = delta_key(keys, n, i, j);
-  int s = 0;
-  int t = l;
-  do {
-    t = (t + 1) >> 1;
-    if (delta_key(keys, n, i, i + (s + t) * d) > dnode) s += t;
-  } while (t > 1);
-  const int gamma = i + s * d + min(d, 0);
-  const int lo = min(i, j), hi = max(i, j);
-  const int lc = (lo == gamma) ? (n - 1 + gamma) : gamma;
-  const int rc = (hi == gamma + 1) ? (n - 1 + gamma + 1) : (gamma + 1);
-  left[i] = lc;
-  right[i] = rc;
-  parent[lc] = i;
-  parent[rc] = i;
-}
-
 __global__ void bottom_up_kernel(const double* __restrict__ V, const int32_t* __restrict__ F,
                                  const int32_t* __restrict__ sorted_tri, int n, int order,
                                  const int32_t* __restrict__ left,
@@ -349,7 +313,7 @@ __global__ void bottom_up_kernel(const double* __restrict__ V, const int32_t* __
   if (n == 1) return;
   int cur = node;
   int levels = 0;
-  while (true) {
+  while (levels < n) {  // a tree over n leaves is less than n deep
     const int p = parent[cur];
     __threadfence();
     if (atomicAdd(&flags[p], 1u) == 0) return;  // first child to arrive stops here
@@ -378,7 +342,7 @@ __global__ void preorder_kernel(const int32_t* __restrict__ left,
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   if (x >= nnodes) return;
   int p = 0, dep = 0, cur = x;
-  while (cur != root) {
+  while (cur != root && dep < nnodes) {
     const int par = parent[cur];
     const int lc = left[par];
     p += 1 + (lc == cur ? 0 : size[lc]);
@@ -621,11 +585,7 @@ void soup_build(gwn_soup_impl& s, const double* V, int64_t nV, const int32_t* F,
   DevBuf<BuildM> M((size_t)nnodes, st);
   DevBuf<int32_t> dmax(1, st);
   dmax.zero(st);
-  if (n > 1) {
-    launch_kernel(radix_tree_kernel, (n - 1 + 255) / 256, 256, 0, st, keys.get(), n, left.get(), right.get(),
-                                                           parent.get());
-    GWN_CUDA(cudaGetLastError());
-  }
+  soup_tree_build(V, F, vals.get(), n, lo, hi, left.get(), right.get(), parent.get(), st);
   launch_kernel(bottom_up_kernel, (n + 127) / 128, 128, 0, st, V, F, vals.get(), n, order, left.get(),
                                                     right.get(), parent.get(), M.get(), size.get(),
                                                     flags.get(), dmax.get());
