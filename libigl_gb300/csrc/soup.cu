@@ -585,7 +585,7 @@ void soup_build(gwn_soup_impl& s, const double* V, int64_t nV, const int32_t* F,
   DevBuf<BuildM> M((size_t)nnodes, st);
   DevBuf<int32_t> dmax(1, st);
   dmax.zero(st);
-  soup_tree_build(V, F, vals.get(), n, lo, hi, left.get(), right.get(), parent.get(), st);
+  soup_tree_build(V, nV, F, vals.get(), n, lo, hi, left.get(), right.get(), parent.get(), st);
   launch_kernel(bottom_up_kernel, (n + 127) / 128, 128, 0, st, V, F, vals.get(), n, order, left.get(),
                                                     right.get(), parent.get(), M.get(), size.get(),
                                                     flags.get(), dmax.get());

@@ -53,12 +53,13 @@ struct gwn_soup_impl {
   size_t bytes = 0;
 };
 
-// Binary tree over the n kept triangles vals[0..n) (soup_tree.cu): on
-// return vals holds the leaf (slot) order; internal nodes are 0..n-2 (root
-// 0) and leaf j is node n-1+j; clo/chi bound the triangles' centroids.
-void soup_tree_build(const double* V, const int32_t* F, int32_t* vals, int n, const double* clo,
-                     const double* chi, int32_t* left, int32_t* right, int32_t* parent,
-                     cudaStream_t st);
+// Binary tree over the n triangles vals[0..n) (soup_tree.cu): on return
+// vals holds the leaf (slot) order; internal nodes are 0..n-2 (root 0) and
+// leaf j is node n-1+j; clo/chi bound the triangles' centroids.  Vertex
+// indices outside [0, nV) read vertex 0 (callers report them).
+void soup_tree_build(const double* V, int64_t nV, const int32_t* F, int32_t* vals, int n,
+                     const double* clo, const double* chi, int32_t* left, int32_t* right,
+                     int32_t* parent, cudaStream_t st);
 
 void soup_build(gwn_soup_impl& s, const double* V, int64_t nV, const int32_t* F, int64_t nF,
                 int order, bool host_mode, cudaStream_t st);

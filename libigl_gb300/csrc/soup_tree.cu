@@ -89,8 +89,9 @@ __device__ __forceinline__ int node_id(int gap, int root_m) {
 __host__ __device__ inline double clamp_f32_range(double x) { return fmin(fmax(x, -3.0e38), 3.0e38); }
 
 // FP32 centroid and vertex box of each kept triangle in slot order.
-__global__ void bt_init_kernel(const double* __restrict__ V, const int32_t* __restrict__ F,
-                               const int32_t* __restrict__ vals, int n, float4* __restrict__ rc,
+__global__ void bt_init_kernel(const double* __restrict__ V, int64_t nV,
+                               const int32_t* __restrict__ F, const int32_t* __restrict__ vals,
+                               int n, float4* __restrict__ rc,
                                float4* __restrict__ rlo, float4* __restrict__ rhi,
                                int* __restrict__ segid, int first_seg) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -98,7 +99,8 @@ __global__ void bt_init_kernel(const double* __restrict__ V, const int32_t* __re
   const int32_t f = vals[p];
   double c[3] = {0, 0, 0}, lo[3], hi[3];
   for (int k = 0; k < 3; ++k) {
-    const int64_t v = F[(int64_t)f * 3 + k];
+    int64_t v = F[(int64_t)f * 3 + k];
+    if (v < 0 || v >= nV) v = 0;  // reported by the caller's own checks
     for (int d = 0; d < 3; ++d) {
       const double x = clamp_f32_range(V[v * 3 + d]);
       c[d] += x;
@@ -509,7 +511,8 @@ __global__ void __launch_bounds__(128) bt_small_kernel(const float4* __restrict_
 
 }  // namespace
 
-void soup_tree_build(const double* V, const int32_t* F, int32_t* vals, int n, const double* clo,
+void soup_tree_build(const double* V, int64_t nV, const int32_t* F, int32_t* vals, int n,
+                     const double* clo,
                      const double* chi, int32_t* left, int32_t* right, int32_t* parent,
                      cudaStream_t st) {
   if (n < 2) return;
@@ -537,7 +540,7 @@ void soup_tree_build(const double* V, const int32_t* F, int32_t* vals, int n, co
   }
   const bool large = n > kSmall;
   const unsigned gridN = (unsigned)((n + 255) / 256);
-  launch_kernel(bt_init_kernel, gridN, 256, 0, st, V, F, (const int32_t*)vals, n, rc.get(),
+  launch_kernel(bt_init_kernel, gridN, 256, 0, st, V, nV, F, (const int32_t*)vals, n, rc.get(),
                 rlo.get(), rhi.get(), segid.get(), large ? 0 : -1);
   if (large) {
     launch_kernel(bt_root_kernel, 1, 1, 0, st, root, segA.get(), (unsigned*)nullptr);
