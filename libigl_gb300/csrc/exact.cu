@@ -466,7 +466,7 @@ void launch_exact3(const ExactArgs& a, cudaStream_t st) {
       std::is_same<WT, double>::value && a.nF >= kHierMinTriangles && a.nQ >= kHierMinQueries) {
     DeviceStatus status(st, a.host_mode);
     HierTree h;
-    hier_build(a.V, a.nV, a.F, a.nF, h, status.ptr(), st);
+    hier_build(a.V, a.nV, a.F, a.nF, h, status.ptr(), st, true);
     hier_eval(h, static_cast<const double*>(a.Q), a.nQ, static_cast<double*>(a.W), st);
     status.check(st, "winding_number (hierarchy)");
     return;

@@ -119,7 +119,10 @@ class DevBuf {
 };
 
 // Persistent device allocation owned by a handle (cudaMalloc / cudaFree), so
-// its lifetime does not depend on any caller stream.
+// its lifetime does not depend on any caller stream.  A structure that lives
+// for one call only can take its memory stream-ordered instead (ordered()
+// before alloc: cudaMallocFromPoolAsync / cudaFreeAsync on that stream), so
+// that neither the allocation nor the release synchronizes the device.
 template <typename T>
 class DevMem {
  public:
@@ -128,13 +131,28 @@ class DevMem {
   ~DevMem() { release(); }
   DevMem(const DevMem&) = delete;
   DevMem& operator=(const DevMem&) = delete;
+  void ordered(cudaStream_t s) {
+    release();
+    ordered_ = true;
+    stream_ = s;
+  }
   void alloc(size_t n) {
     release();
     n_ = n;
-    if (n) GWN_CUDA(cudaMalloc(reinterpret_cast<void**>(&p_), n * sizeof(T)));
+    if (!n) return;
+    if (ordered_)
+      GWN_CUDA(cudaMallocFromPoolAsync(reinterpret_cast<void**>(&p_), n * sizeof(T), device_pool(),
+                                       stream_));
+    else
+      GWN_CUDA(cudaMalloc(reinterpret_cast<void**>(&p_), n * sizeof(T)));
   }
   void release() {
-    if (p_) cudaFree(p_);
+    if (p_) {
+      if (ordered_)
+        cudaFreeAsync(p_, stream_);
+      else
+        cudaFree(p_);
+    }
     p_ = nullptr;
     n_ = 0;
   }
@@ -145,6 +163,8 @@ class DevMem {
  private:
   T* p_ = nullptr;
   size_t n_ = 0;
+  bool ordered_ = false;
+  cudaStream_t stream_ = nullptr;
 };
 
 inline size_t dtype_size(int dt) { return dt == GWN_F64 ? 8 : 4; }

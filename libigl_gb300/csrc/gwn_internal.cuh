@@ -86,10 +86,13 @@ struct HierTree {
   DevMem<float4> tris;    // 4 per leaf triangle
   DevMem<double> tris64;  // 9 per leaf triangle
 };
-// Out-of-range triangle indices set kStatusBadInput in *status.
+// Out-of-range triangle indices set kStatusBadInput in *status.  With
+// per_call, the tree's memory is stream-ordered on `st` (a tree built and
+// used inside one call); otherwise it is owned like a handle's.  The build
+// ends with work still queued on `st`.
 void hier_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, HierTree& h,
-                unsigned* status, cudaStream_t st);
-// W of every query (FP64 device arrays), mixed precision; synchronizes `st`.
+                unsigned* status, cudaStream_t st, bool per_call = false);
+// W of every query (FP64 device arrays), mixed precision, queued on `st`.
 void hier_eval(const HierTree& h, const double* Q, int64_t nQ, double* W, cudaStream_t st);
 
 // Eytzinger AABB tree of segments (eytzinger.cu); device pointers.

@@ -627,7 +627,14 @@ __global__ void __launch_bounds__(kT) hier_walk_kernel(HierDev H, const QT* __re
 }  // namespace
 
 void hier_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, HierTree& h,
-                unsigned* status, cudaStream_t st) {
+                unsigned* status, cudaStream_t st, bool per_call) {
+  if (per_call) {
+    h.nodes.ordered(st);
+    h.capn.ordered(st);
+    h.caps.ordered(st);
+    h.tris.ordered(st);
+    h.tris64.ordered(st);
+  }
   h.V = V;
   h.nV = nV;
   h.F = F;
@@ -772,7 +779,6 @@ void hier_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, HierT
                 h.c[2], h.eps, nodes, h.capn.get());
   launch_kernel(leaf_tris_kernel, nblk(n), kT, 0, st, V, F, nV, (const int32_t*)sorted.get(), n,
                 h.c[0], h.c[1], h.c[2], h.eps, tris, h.tris64.get());
-  GWN_CUDA(cudaStreamSynchronize(st));
 }
 
 void hier_eval(const HierTree& h, const double* Q, int64_t nQ, double* W, cudaStream_t st) {

@@ -306,7 +306,7 @@ void swept_volume_run(const double* V, int64_t nV, const int32_t* F, int64_t nF,
       PhaseTimer ph("build", st);
       soup_build(tree, V, nV, F, nF, 2, true, st);
       if (sign_type == GWN_SD_PSEUDONORMAL) pseudonormal_precompute(V, nV, F, nF, pn, st);
-      if (use_hier) hier_build(V, nV, F, nF, hier, sticky_status_word(), st);
+      if (use_hier) hier_build(V, nV, F, nF, hier, sticky_status_word(), st, true);
     }
     // up to 16 transforms per chunk, about 8M (point, transform) slots
     const int K = (int)std::max<int64_t>(1, std::min<int64_t>(16, (int64_t(8) << 20) / nG));
