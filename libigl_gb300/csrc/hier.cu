@@ -43,6 +43,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <memory>
 
 #include "bh_common.cuh"
 #include "exact_terms.cuh"
@@ -53,6 +54,7 @@ namespace gwn {
 namespace {
 
 constexpr int kT = 256;
+constexpr int kMaxSplit = 8;  // subtrees walked in parallel when queries are few
 constexpr double kNearFrac = 1e-3;
 constexpr double kBand = 1e-3;
 constexpr double kInv2Pi = 0.15915494309189533577;
@@ -568,7 +570,19 @@ __global__ void __launch_bounds__(kT) hier_walk_kernel(HierDev H, const QT* __re
                                                        double cx, double cy, double cz,
                                                        double* __restrict__ W,
                                                        int32_t* __restrict__ redo,
-                                                       uint32_t* __restrict__ nredo) {
+                                                       uint32_t* __restrict__ nredo,
+                                                       const int2* __restrict__ ranges,
+                                                       const int* __restrict__ nranges,
+                                                       double* __restrict__ part) {
+  // ranges: walk only the subtree [ranges[y].x, ranges[y].y) of y = blockIdx.y
+  // and write the partial sum (solid angle) to part[y * nQ + q]
+  int x0 = 0, x1 = H.nnodes;
+  if (ranges) {
+    if ((int)blockIdx.y >= *nranges) return;
+    const int2 rg = ranges[blockIdx.y];
+    x0 = rg.x;
+    x1 = rg.y;
+  }
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const bool valid = i < nQ;
   const int64_t q = valid ? (perm ? perm[i] : i) : 0;
@@ -583,9 +597,26 @@ __global__ void __launch_bounds__(kT) hier_walk_kernel(HierDev H, const QT* __re
   }
   Sum32 acc;
   double acc64 = 0.0;
-  int resume = valid ? 0 : 0x7fffffff;
-  int x = 0;
-  while (x < H.nnodes) {
+  int resume = valid ? x0 : 0x7fffffff;
+  if (ranges && valid) {
+    // a query outside the root's box takes the root's cap alone (in
+    // subtree 0), as the whole-tree walk does, instead of one cap per subtree
+    const NodeH r0 = H.nodes[0];
+    const int meta0 = __float_as_int(r0.hi.w);
+    if (meta0 >= 0 && (qh.x < r0.lo.x || qh.x > r0.hi.x || qh.y < r0.lo.y || qh.y > r0.hi.y ||
+                       qh.z < r0.lo.z || qh.z > r0.hi.z)) {
+      if (blockIdx.y == 0) {
+        const int cn = H.capn[0];
+        for (int k = 0; k < cn; ++k) {
+          const TriH t = H.caps[meta0 + k];
+          acc.add(trih_term32(t, rel_a(t, qh, ql)));
+        }
+      }
+      resume = 0x7fffffff;
+    }
+  }
+  int x = x0;
+  while (x < x1) {
     if (x >= resume) {
       const NodeH nd = H.nodes[x];
       const int meta = __float_as_int(nd.hi.w);
@@ -617,7 +648,56 @@ __global__ void __launch_bounds__(kT) hier_walk_kernel(HierDev H, const QT* __re
     x = __reduce_min_sync(0xffffffffu, resume);
   }
   if (!valid) return;
+  if (part) {
+    part[(int64_t)blockIdx.y * nQ + q] = acc.value() + acc64;
+    return;
+  }
   const double w = (acc.value() + acc64) * kInv2Pi;
+  W[q] = w;
+  if (fabs(w - 0.5) <= kBand) redo[atomicAdd(nredo, 1u)] = (int32_t)q;
+}
+
+// The top of the tree cut into at most S subtrees (breadth first; a leaf
+// above the cut stays whole): ranges of pre-order positions.  One thread.
+__global__ void frontier_kernel(const NodeH* __restrict__ nodes, int S, int2* __restrict__ ranges,
+                                int* __restrict__ nranges) {
+  auto end_of = [&](int y) {
+    const int meta = __float_as_int(nodes[y].hi.w);
+    return meta <= -2 ? y + 1 : __float_as_int(nodes[y].lo.w);
+  };
+  int cur[8], nxt[8];
+  int nc = 1;
+  cur[0] = 0;
+  bool grew = true;
+  while (grew && nc * 2 <= S) {
+    grew = false;
+    int m = 0;
+    for (int i = 0; i < nc; ++i) {
+      const int y = cur[i];
+      if (__float_as_int(nodes[y].hi.w) <= -2) {
+        nxt[m++] = y;
+      } else {
+        nxt[m++] = y + 1;
+        nxt[m++] = end_of(y + 1);
+        grew = true;
+      }
+    }
+    for (int i = 0; i < m; ++i) cur[i] = nxt[i];
+    nc = m;
+  }
+  for (int i = 0; i < nc; ++i) ranges[i] = make_int2(cur[i], end_of(cur[i]));
+  *nranges = nc;
+}
+
+// W from the subtrees' partial sums (fixed order), and the FP64 re-check list.
+__global__ void hier_sum_kernel(const double* __restrict__ part, int S, int64_t nQ,
+                                double* __restrict__ W, int32_t* __restrict__ redo,
+                                uint32_t* __restrict__ nredo) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= nQ) return;
+  double a = 0.0;
+  for (int y = 0; y < S; ++y) a += part[(int64_t)y * nQ + q];
+  const double w = a * kInv2Pi;
   W[q] = w;
   if (fabs(w - 0.5) <= kBand) redo[atomicAdd(nredo, 1u)] = (int32_t)q;
 }
@@ -646,6 +726,7 @@ void hier_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, HierT
   const int n = (int)nF;
   const int nn = 2 * n - 1;
   PhaseTimer ph_all("hier_build", st);
+  auto ph_part = std::make_unique<PhaseTimer>("hier_build_tree", st);
   DevBuf<unsigned long long> mm(6, st);
   init_minmax(mm.get(), 3, st);
   launch_kernel(mesh_bbox_kernel, std::min<unsigned>(nblk(nV), 1024u), kT, 0, st, V, nV, mm.get());
@@ -684,6 +765,7 @@ void hier_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, HierT
   launch_kernel(preorder_kernel, nblk(nn), kT, 0, st, (const int32_t*)left.get(),
                 (const int32_t*)parent.get(), (const int32_t*)size.get(), nn, pre.get());
   // boundary records
+  ph_part = std::make_unique<PhaseTimer>("hier_build_records", st);
   const int64_t m = 3 * (int64_t)n;
   DevBuf<unsigned long long> ekey((size_t)m, st), ekey_t((size_t)m, st);
   DevBuf<int32_t> eval((size_t)m, st), eval_t((size_t)m, st);
@@ -756,6 +838,7 @@ void hier_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, HierT
     GWN_CUDA(cudaStreamSynchronize(st));
     ncap = tot;
   }
+  ph_part = std::make_unique<PhaseTimer>("hier_build_emit", st);
   h.nnodes = nn;
   h.ncap = ncap;
   h.nodes.alloc((size_t)nn * 2);
@@ -796,11 +879,32 @@ void hier_eval(const HierTree& h, const double* Q, int64_t nQ, double* W, cudaSt
   const HierDev H{reinterpret_cast<const NodeH*>(h.nodes.get()), h.capn.get(),
                   reinterpret_cast<const TriH*>(h.caps.get()),
                   reinterpret_cast<const TriH*>(h.tris.get()), h.tris64.get(), (int)h.nnodes};
+  // Too few queries to fill the GPU: each warp of queries walks one of up to
+  // 8 subtrees (blockIdx.y), and the partial sums are added in a fixed order.
+  const int64_t warps = (nQ + 31) / 32;
+  const int64_t want = 3 * (int64_t)num_sms() * 32;
+  int S = 1;
+  while (S < kMaxSplit && warps * S < want) S *= 2;
   {
     PhaseTimer ph("hier_walk", st);
-    launch_kernel(hier_walk_kernel<double>, nblk(nQ), kT, 0, st, H, Q, nQ,
-                  (const int32_t*)(qo.active ? qo.perm.get() : nullptr), h.c[0], h.c[1], h.c[2],
-                  W, redo.get(), nredo.get());
+    if (S == 1) {
+      launch_kernel(hier_walk_kernel<double>, nblk(nQ), kT, 0, st, H, Q, nQ,
+                    (const int32_t*)(qo.active ? qo.perm.get() : nullptr), h.c[0], h.c[1],
+                    h.c[2], W, redo.get(), nredo.get(), (const int2*)nullptr,
+                    (const int*)nullptr, (double*)nullptr);
+    } else {
+      DevBuf<int2> ranges(kMaxSplit, st);
+      DevBuf<int> nranges(1, st);
+      DevBuf<double> part((size_t)S * nQ, st);
+      part.zero(st);
+      launch_kernel(frontier_kernel, 1, 1, 0, st, H.nodes, S, ranges.get(), nranges.get());
+      launch_kernel(hier_walk_kernel<double>, dim3(nblk(nQ), S), kT, 0, st, H, Q, nQ,
+                    (const int32_t*)(qo.active ? qo.perm.get() : nullptr), h.c[0], h.c[1],
+                    h.c[2], W, redo.get(), nredo.get(), (const int2*)ranges.get(),
+                    (const int*)nranges.get(), part.get());
+      launch_kernel(hier_sum_kernel, nblk(nQ), kT, 0, st, (const double*)part.get(), S, nQ, W,
+                    redo.get(), nredo.get());
+    }
   }
   // FP64 all-pairs re-evaluation of the results within the band, one block
   // per listed query
