@@ -673,10 +673,9 @@ __global__ void __launch_bounds__(128, 6) cloud_eval_mixed_kernel(CloudEvalParam
       }
       queue_cloud64(prm, nq, nqueued, want, ~node, acc64);
     }
-    if (__any_sync(full, open))
-      node = node + 1;
-    else
-      node = __reduce_min_sync(full, resume);
+    // a lane that opens the node wants node + 1, every other lane is past
+    // the node (resume > node): the warp goes to the smallest of them
+    node = __reduce_min_sync(full, open ? node + 1 : resume);
   }
   if (nqueued) flush_cloud64(prm, nq, nqueued, acc64);
   if (!valid) return;
@@ -728,10 +727,9 @@ __global__ void __launch_bounds__(128) cloud_eval_fp64_kernel(CloudEvalParams pr
         open = true;
       }
     }
-    if (__any_sync(full, open))
-      node = node + 1;
-    else
-      node = __reduce_min_sync(full, resume);
+    // a lane that opens the node wants node + 1, every other lane is past
+    // the node (resume > node): the warp goes to the smallest of them
+    node = __reduce_min_sync(full, open ? node + 1 : resume);
   }
   if (valid) W[qi] = (WT)acc;
 }

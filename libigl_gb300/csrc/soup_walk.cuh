@@ -299,10 +299,9 @@ __device__ __forceinline__ void walk_mixed(const EvalParams& prm, bool valid, do
       if (want64) nq.e[nqueued + __popc(m64 & lt_mask)] = make_int2(slot64, lane);
       nqueued += k;
     }
-    if (__any_sync(full, open))
-      node = node + 1;
-    else
-      node = __reduce_min_sync(full, resume);
+    // a lane that opens the node wants node + 1, every other lane is past
+    // the node (resume > node): the warp goes to the smallest of them
+    node = __reduce_min_sync(full, open ? node + 1 : resume);
   }
   if (nqueued) flush_near64(prm.td, nq, nqueued, acc64);
 }
@@ -353,10 +352,9 @@ __device__ __forceinline__ double walk_fp64(const EvalParams& prm, bool valid, d
         }
       }
     }
-    if (__any_sync(full, open))
-      node = node + 1;
-    else
-      node = __reduce_min_sync(full, resume);
+    // a lane that opens the node wants node + 1, every other lane is past
+    // the node (resume > node): the warp goes to the smallest of them
+    node = __reduce_min_sync(full, open ? node + 1 : resume);
   }
   return acc;
 }
