@@ -43,6 +43,7 @@ namespace {
 constexpr int kBins = 32;         // one bin per lane of the split warp
 constexpr int kSmall = 32;        // one triangle per lane of the small-segment warp
 constexpr int kMedianLevel = 40;  // bounds the depth of the binned levels
+constexpr int kMaxBinnedSegs = 1 << 18;  // a wider level splits at the median (bins <= 705 MB)
 
 struct Seg {
   int l, r;            // slot range [l, r)
@@ -550,17 +551,20 @@ void soup_tree_build(const double* V, int64_t nV, const int32_t* F, int32_t* val
   int S = large ? 1 : 0;
   const unsigned gridBin = (unsigned)std::min<int64_t>(gridN, (int64_t)num_sms() * 8);
   for (int level = 0; S > 0; ++level) {
-    const size_t nb = (size_t)S * 3 * kBins;
+    const bool median_only = level >= kMedianLevel || S > kMaxBinnedSegs;
+    const size_t nb = median_only ? 0 : (size_t)S * 3 * kBins;
     DevBuf<unsigned> cnt(nb, st), blo(nb * 3, st), bhi(nb * 3, st);
-    cnt.zero(st);
-    GWN_CUDA(cudaMemsetAsync(blo.get(), 0xff, blo.bytes(), st));
-    bhi.zero(st);
-    launch_kernel(bt_bin_kernel, gridBin, 256, 0, st, (const float4*)rc.get(),
-                  (const float4*)rlo.get(), (const float4*)rhi.get(), (const int*)segid.get(), n,
-                  (const Seg*)segA.get(), cnt.get(), blo.get(), bhi.get());
+    if (!median_only) {
+      cnt.zero(st);
+      GWN_CUDA(cudaMemsetAsync(blo.get(), 0xff, blo.bytes(), st));
+      bhi.zero(st);
+      launch_kernel(bt_bin_kernel, gridBin, 256, 0, st, (const float4*)rc.get(),
+                    (const float4*)rlo.get(), (const float4*)rhi.get(), (const int*)segid.get(),
+                    n, (const Seg*)segA.get(), cnt.get(), blo.get(), bhi.get());
+    }
     launch_kernel(bt_split_kernel, (unsigned)((S + 3) / 4), 128, 0, st, (const Seg*)segA.get(), S,
                   (const unsigned*)cnt.get(), (const unsigned*)blo.get(),
-                  (const unsigned*)bhi.get(), sp.get(), level >= kMedianLevel ? 1 : 0);
+                  (const unsigned*)bhi.get(), sp.get(), median_only ? 1 : 0);
     GWN_CUDA(cudaMemsetAsync(counts.get() + 1, 0, sizeof(unsigned), st));
     launch_kernel(bt_children_kernel, (unsigned)((S + 127) / 128), 128, 0, st,
                   (const Seg*)segA.get(), S, sp.get(), n, segB.get(), counts.get() + 1,

@@ -162,3 +162,45 @@ def test_device_tensors_and_repeatability(mesh, cuda):
     Ws = bvh.eval(sub, 2.0, precision="mixed")
     assert np.abs(Ws - Wh[::7]).max() <= 1e-6
     assert G.device_status() == 0
+
+
+def _check_tree(V, F, Q):
+    bvh = G.FastWindingNumberBVH(V, F, order=2)
+    nodes, links, tri = bvh.export()
+    n = F.shape[0]
+    assert sorted(tri.tolist()) == list(range(n))
+    assert nodes.shape[0] == 2 * n - 1
+    # pre-order with skip links: an internal node's subtree is [p + 1, link)
+    internal = links >= 0
+    idx = np.nonzero(internal)[0]
+    assert np.all(links[idx] > idx + 1) and np.all(links[idx] <= 2 * n - 1)
+    if n > 1:
+        assert links[0] == 2 * n - 1
+    assert sorted((~links[~internal]).tolist()) == list(range(n))
+    W64 = bvh.eval(Q, 2.0, precision="fp64")
+    Wcpu = O.soup_tree_eval(V, F, nodes, tri, Q, 2.0, order=2)
+    assert np.abs(W64 - Wcpu).max() < 1e-11
+    Wm = bvh.eval(Q, 2.0, precision="mixed")
+    assert np.abs(Wm - W64).max() <= TOL_MIXED
+
+
+def test_tree_builder_corner_cases(cuda):
+    """The binned top-down builder (soup_tree.cu): sizes around the 32
+    triangles one warp finishes, triangles whose centroids all coincide (no
+    bin separates them: middle splits), and a flat mesh (zero extent on one
+    axis)."""
+    rng = np.random.default_rng(71)
+    V, F = synth.icosphere(3)
+    F = np.ascontiguousarray(F, dtype=np.int32)
+    Q = np.ascontiguousarray(rng.uniform(-1.3, 1.3, (500, 3)))
+    for m in (2, 3, 31, 32, 33, 34, 64, 65, 200):
+        _check_tree(V, np.ascontiguousarray(F[:m]), Q)
+    # 300 copies of one triangle, flipped every other time: equal centroids
+    Fd = np.ascontiguousarray(np.tile(np.array([[0, 1, 2], [0, 2, 1]], np.int32), (150, 1)))
+    _check_tree(V, Fd, Q)
+    # a flat grid of triangles in z = 0
+    g = np.stack(np.meshgrid(np.linspace(0, 1, 30), np.linspace(0, 1, 30), indexing="ij"), -1)
+    Vf = np.concatenate([g.reshape(-1, 2), np.zeros((900, 1))], 1)
+    a = (np.arange(29)[:, None] * 30 + np.arange(29)[None, :]).ravel()
+    Ff = np.concatenate([np.stack([a, a + 30, a + 1], 1), np.stack([a + 1, a + 30, a + 31], 1)])
+    _check_tree(np.ascontiguousarray(Vf), np.ascontiguousarray(Ff, dtype=np.int32), Q * 0.8 + 0.3)
