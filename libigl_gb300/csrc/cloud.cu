@@ -50,7 +50,7 @@ constexpr int kSmallCell = 64;
 constexpr double kNearFrac = 1e-3;
 constexpr double kBand = 1e-3;
 constexpr double kPi4 = 4.0 * kPi;
-constexpr float kPi4F = (float)(4.0 * kPi);
+constexpr float kInvPi4F = (float)(1.0 / (4.0 * kPi));
 
 inline unsigned blocks(int64_t n, int t = 256) {
   return (unsigned)std::max<int64_t>(1, (n + t - 1) / t);
@@ -497,6 +497,52 @@ __device__ __forceinline__ T expansion(const T* ec, T lx, T ly, T lz, T r, int n
   return wn;
 }
 
+// The FP32 form of expansion<float> for the mixed walk: the same terms with
+// one reciprocal square root in place of its divisions (c3 = 1/(4 pi r^3),
+// c5 = c3 / r^2, c7 = c5 / r^2).
+__device__ __forceinline__ float expansion_f32(const float* ec, float lx, float ly, float lz,
+                                               float r2, int num_terms) {
+  const float ir = rsqrtf(r2);
+  const float ir2 = ir * ir;
+  const float c3 = ir2 * ir * kInvPi4F;
+  float wn = (lx * ec[0] + ly * ec[1] + lz * ec[2]) * c3;
+  if (num_terms > 3) {
+    const float c5 = c3 * ir2;
+    const float s = -3.f * c5;
+    const float l[3] = {lx, ly, lz};
+    float acc = 0.f;
+#pragma unroll
+    for (int v = 0; v < 3; ++v)
+#pragma unroll
+      for (int u = 0; u < 3; ++u) {
+        float sd = (l[u] * l[v]) * s;
+        if (u == v) sd += c3;
+        acc += sd * ec[3 + u + 3 * v];
+      }
+    wn += acc;
+    if (num_terms > 12) {
+      const float c7 = c5 * ir2;
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        float acc3 = 0.f;
+#pragma unroll
+        for (int v = 0; v < 3; ++v)
+#pragma unroll
+          for (int u = 0; u < 3; ++u) {
+            float rcd = 0.f;
+            if (u == v) rcd += l[i];
+            if (u == i) rcd += l[v];
+            if (v == i) rcd += l[u];
+            const float ltl = l[u] * l[v] * c7;
+            acc3 += (15.f * l[i] * ltl + s * rcd) * ec[12 + i * 9 + u + 3 * v];
+          }
+        wn += acc3;
+      }
+    }
+  }
+  return wn;
+}
+
 // The reference's test `|CM - q| > beta R` (:265-266), FP64, pinned order.
 __device__ __forceinline__ bool far64(double qx, double qy, double qz, const double* cm, double r,
                                       double beta) {
@@ -628,8 +674,8 @@ __global__ void __launch_bounds__(128, 6) cloud_eval_mixed_kernel(CloudEvalParam
             want = true;
           } else {
             const float4 an = __ldg(&prm.pf[slot * 2 + 1]);
-            const float rn = sqrtf(r2);
-            acc += fmaf(lx, an.x, fmaf(ly, an.y, lz * an.z)) / (kPi4F * (r2 * rn));
+            const float ir = rsqrtf(r2);
+            acc += fmaf(lx, an.x, fmaf(ly, an.y, lz * an.z)) * (ir * ir * ir * kInvPi4F);
           }
         }
         queue_cloud64(prm, nq, nqueued, want, (int)slot, acc64);
@@ -664,7 +710,7 @@ __global__ void __launch_bounds__(128, 6) cloud_eval_mixed_kernel(CloudEvalParam
               ec[4 * k + 2] = e.z;
               ec[4 * k + 3] = e.w;
             }
-            acc += expansion<float>(ec, dx, dy, dz, sqrtf(r2), prm.num_terms);
+            acc += expansion_f32(ec, dx, dy, dz, r2, prm.num_terms);
           }
           resume = l.x;
         } else {
@@ -806,7 +852,8 @@ __global__ void __launch_bounds__(256) cloud_direct_kernel(const float4* __restr
         acc64 += dipole64(d[0] - qx, d[1] - qy, d[2] - qz, d[3], d[4], d[5]);
       } else {
         const float4 an = __ldg(&pf[j * 2 + 1]);
-        acc += fmaf(lx, an.x, fmaf(ly, an.y, lz * an.z)) / (kPi4F * (r2 * sqrtf(r2)));
+        const float ir = rsqrtf(r2);
+        acc += fmaf(lx, an.x, fmaf(ly, an.y, lz * an.z)) * (ir * ir * ir * kInvPi4F);
       }
     } else {
       const double* d = pd + j * 6;
