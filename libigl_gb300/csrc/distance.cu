@@ -150,6 +150,21 @@ __device__ __forceinline__ bool screened_out(const ClosestParams& prm, int slot,
   return lower > bound;
 }
 
+// FP32 bounds of the distance from q to a leaf's triangle: its FP32
+// distance minus / plus the triangle's stored slack and the query-rounding
+// slack 1e-6 (S + d).
+__device__ __forceinline__ void leaf_bounds(const ClosestParams& prm, int slot, float fx, float fy,
+                                            float fz, float S, float& lower, float& upper) {
+  const float4 t0 = __ldg(&prm.tf[(int64_t)slot * 3]);
+  const float4 t1 = __ldg(&prm.tf[(int64_t)slot * 3 + 1]);
+  const float4 t2 = __ldg(&prm.tf[(int64_t)slot * 3 + 2]);
+  const float d = sqrtf(dist2_triangle32(fx, fy, fz, t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z,
+                                         t1.w, t2.x));
+  const float e = t2.y + 1e-6f * (S + d);
+  lower = d - e;
+  upper = __fadd_ru(d, e);
+}
+
 // A candidate replaces the best when strictly closer, or equally close with
 // a smaller input triangle index: with pruning only of what is strictly
 // farther, every triangle at the smallest distance is evaluated, so the
@@ -290,6 +305,24 @@ __global__ void __launch_bounds__(128) closest_dfs_kernel(ClosestParams prm,
   if (isfinite(q.x) && isfinite(q.y) && isfinite(q.z) && prm.nnodes > 0) {
     const float fx = (float)q.x, fy = (float)q.y, fz = (float)q.z;
     const float S = fmaxf(fabsf(fx), fmaxf(fabsf(fy), fabsf(fz))) + prm.cmax;
+    // ub: an FP32 upper bound of the best distance (the smallest FP32 upper
+    // bound of any leaf seen, or of the FP64 best).  A leaf whose FP32 lower
+    // bound is within ub becomes a candidate; the FP64 closest point is
+    // computed only for the candidates still within ub at the end (or when
+    // the four candidate slots are full), so every triangle that can be the
+    // closest, ties included, is evaluated in FP64 as before.
+    float ub = b.bound;
+    int cs0 = 0, cs1 = 0, cs2 = 0, cs3 = 0;
+    float cl0 = 0.f, cl1 = 0.f, cl2 = 0.f, cl3 = 0.f;
+    int nc = 0;
+    auto flush = [&]() {
+      if (nc > 0 && !(cl0 > ub)) eval_leaf(prm, cs0, q, b);
+      if (nc > 1 && !(cl1 > ub)) eval_leaf(prm, cs1, q, b);
+      if (nc > 2 && !(cl2 > ub)) eval_leaf(prm, cs2, q, b);
+      if (nc > 3 && !(cl3 > ub)) eval_leaf(prm, cs3, q, b);
+      nc = 0;
+      ub = fminf(ub, b.bound);
+    };
     int stk_n[kStack];
     float stk_lb[kStack];
     int sp = 0;
@@ -300,9 +333,19 @@ __global__ void __launch_bounds__(128) closest_dfs_kernel(ClosestParams prm,
       --sp;
       const int ref = stk_n[sp];
       const float lb = stk_lb[sp];
-      if (lb > b.bound) continue;
+      if (lb > ub) continue;
       if (ref < 0) {
-        if (!screened_out(prm, ~ref, fx, fy, fz, S, b.bound)) eval_leaf(prm, ~ref, q, b);
+        float lower, upper;
+        leaf_bounds(prm, ~ref, fx, fy, fz, S, lower, upper);
+        if (!(lower > ub)) {
+          if (nc == 4) flush();
+          if (nc == 0) { cs0 = ~ref; cl0 = lower; }
+          else if (nc == 1) { cs1 = ~ref; cl1 = lower; }
+          else if (nc == 2) { cs2 = ~ref; cl2 = lower; }
+          else { cs3 = ~ref; cl3 = lower; }
+          ++nc;
+          ub = fminf(ub, upper);
+        }
         continue;
       }
       const float4* sn = prm.snode + 4 * (int64_t)ref;
@@ -314,7 +357,7 @@ __global__ void __launch_bounds__(128) closest_dfs_kernel(ClosestParams prm,
       const bool left_first = lbl <= lbr;
       const int far_n = left_first ? r : l, near_n = left_first ? l : r;
       const float far_lb = left_first ? lbr : lbl, near_lb = left_first ? lbl : lbr;
-      if (!(far_lb > b.bound)) {
+      if (!(far_lb > ub)) {
         if (sp == kStack) {
           atomicOr(status, kStatusBadInput);
           break;
@@ -323,7 +366,7 @@ __global__ void __launch_bounds__(128) closest_dfs_kernel(ClosestParams prm,
         stk_lb[sp] = far_lb;
         ++sp;
       }
-      if (!(near_lb > b.bound)) {
+      if (!(near_lb > ub)) {
         if (sp == kStack) {
           atomicOr(status, kStatusBadInput);
           break;
@@ -333,6 +376,7 @@ __global__ void __launch_bounds__(128) closest_dfs_kernel(ClosestParams prm,
         ++sp;
       }
     }
+    flush();
   }
   sqrD[qi] = b.d2;
   I[qi] = b.slot >= 0 ? prm.tri_index[b.slot] : -1;
