@@ -563,8 +563,36 @@ __device__ __forceinline__ double tri64_term(const double* t, double px, double 
   return vos_term64(t, t + 3, t + 6, px, py, pz);
 }
 
+// Per-warp queue of the FP64 leaf terms: the lanes that need one append
+// (slot, lane); when the queue would overflow, and at the end, the warp
+// evaluates up to 32 queued terms at once, one per lane, and every lane adds
+// its own terms in queue order (its walk order), so that the FP64
+// instructions run with the whole warp instead of the few lanes near a leaf.
+struct HierQueue {
+  int2 e[32];
+  double q[32][3];  // each lane's FP64 query
+};
+
+__device__ __forceinline__ void flush_hier64(const double* __restrict__ tris64,
+                                             const HierQueue& hq, int n, double& acc64) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  __syncwarp();
+  int2 e = make_int2(0, lane);
+  if (lane < n) e = hq.e[lane];
+  double v = 0.0;
+  if (lane < n)
+    v = tri64_term(tris64 + (int64_t)e.x * 9, hq.q[e.y][0], hq.q[e.y][1], hq.q[e.y][2]);
+  for (int k = 0; k < n; ++k) {
+    const double vk = __shfl_sync(full, v, k);
+    const int ok = __shfl_sync(full, e.y, k);
+    if (ok == lane) acc64 += vk;
+  }
+  __syncwarp();
+}
+
 template <typename QT>
-__global__ void __launch_bounds__(kT) hier_walk_kernel(HierDev H, const QT* __restrict__ Q,
+__global__ void __launch_bounds__(kT, 4) hier_walk_kernel(HierDev H, const QT* __restrict__ Q,
                                                        int64_t nQ,
                                                        const int32_t* __restrict__ perm,
                                                        double cx, double cy, double cz,
@@ -597,6 +625,13 @@ __global__ void __launch_bounds__(kT) hier_walk_kernel(HierDev H, const QT* __re
   }
   Sum32 acc;
   double acc64 = 0.0;
+  __shared__ HierQueue hqs[kT / 32];
+  HierQueue& hq = hqs[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  hq.q[lane][0] = px;
+  hq.q[lane][1] = py;
+  hq.q[lane][2] = pz;
+  int nqueued = 0;  // warp-uniform
   int resume = valid ? x0 : 0x7fffffff;
   if (ranges && valid) {
     // a query outside the root's box takes the root's cap alone (in
@@ -617,6 +652,8 @@ __global__ void __launch_bounds__(kT) hier_walk_kernel(HierDev H, const QT* __re
   }
   int x = x0;
   while (x < x1) {
+    bool want64 = false;
+    int slot64 = 0;
     if (x >= resume) {
       const NodeH nd = H.nodes[x];
       const int meta = __float_as_int(nd.hi.w);
@@ -628,10 +665,12 @@ __global__ void __launch_bounds__(kT) hier_walk_kernel(HierDev H, const QT* __re
         const float mx = a.x + (t.r0.w + t.r1.z) * (1.f / 3.f);
         const float my = a.y + (t.r1.x + t.r1.w) * (1.f / 3.f);
         const float mz = a.z + (t.r1.y + t.r2.x) * (1.f / 3.f);
-        if (fmaf(mx, mx, fmaf(my, my, mz * mz)) < t.r3.w)
-          acc64 += tri64_term(H.tris64 + (int64_t)slot * 9, px, py, pz);
-        else
+        if (fmaf(mx, mx, fmaf(my, my, mz * mz)) < t.r3.w) {
+          want64 = true;
+          slot64 = slot;
+        } else {
           acc.add(trih_term32(t, a));
+        }
         resume = x + 1;
       } else if (meta >= 0 && (qh.x < nd.lo.x || qh.x > nd.hi.x || qh.y < nd.lo.y ||
                                qh.y > nd.hi.y || qh.z < nd.lo.z || qh.z > nd.hi.z)) {
@@ -645,8 +684,19 @@ __global__ void __launch_bounds__(kT) hier_walk_kernel(HierDev H, const QT* __re
         resume = x + 1;
       }
     }
+    const unsigned m64 = __ballot_sync(0xffffffffu, want64);
+    if (m64) {
+      const int k = __popc(m64);
+      if (nqueued + k > 32) {
+        flush_hier64(H.tris64, hq, nqueued, acc64);
+        nqueued = 0;
+      }
+      if (want64) hq.e[nqueued + __popc(m64 & ((1u << lane) - 1u))] = make_int2(slot64, lane);
+      nqueued += k;
+    }
     x = __reduce_min_sync(0xffffffffu, resume);
   }
+  if (nqueued) flush_hier64(H.tris64, hq, nqueued, acc64);
   if (!valid) return;
   if (part) {
     part[(int64_t)blockIdx.y * nQ + q] = acc.value() + acc64;
