@@ -579,8 +579,8 @@ __device__ __forceinline__ void read_q(const QT* Q, const int32_t* perm, const i
 // queued terms at once, one per lane, so each FP64 instruction serves the
 // whole warp; each lane still adds its own terms in walk order.  The lanes'
 // FP64 queries live here too (read only at FP64 re-checks and flushes), and
-// the walk runs 6 blocks of 128 threads per SM (80 registers): C3's 8M-query
-// evaluation 22.4 -> 20.7 ms against 5 blocks with the queries in registers.
+// the walk runs 8 blocks of 128 threads per SM (64 registers; with the
+// division-free FP32 terms, 18.2 -> 17.4 ms for C3's 8M queries against 6).
 struct CloudNearQueue {
   int2 e[32];
   double q[32][3];  // each lane's FP64 query
@@ -632,7 +632,7 @@ __device__ __forceinline__ void queue_cloud64(const CloudEvalParams& prm, CloudN
 }
 
 template <typename QT, typename WT>
-__global__ void __launch_bounds__(128, 6) cloud_eval_mixed_kernel(CloudEvalParams prm, const QT* __restrict__ Q,
+__global__ void __launch_bounds__(128, 8) cloud_eval_mixed_kernel(CloudEvalParams prm, const QT* __restrict__ Q,
                                                                const int32_t* __restrict__ perm,
                                                                int64_t nQ, WT* __restrict__ W,
                                                                int32_t* __restrict__ refine_list,
