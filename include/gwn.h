@@ -50,6 +50,17 @@ enum gwn_status {
 enum gwn_dtype { GWN_F32 = 0, GWN_F64 = 1 };
 enum gwn_precision { GWN_PLAIN_FP64 = 0, GWN_MIXED = 1 };
 enum gwn_mem { GWN_HOST = 0, GWN_DEVICE = 1 };
+/* Triangle-soup tree (gwn_soup_build_tree):
+ *   GWN_TREE_REFERENCE -- the reference's own 4-wide SAH tree (UT_BVH<4>),
+ *                         built on the GPU node for node, with its FP32
+ *                         moments and FP32 open test: the same tree cut as
+ *                         igl::fast_winding_number, so results equal the
+ *                         reference's up to its FP32 rounding.
+ *   GWN_TREE_BINNED    -- a binary tree of binned splits (triangles x
+ *                         squared box diagonal); a different tree cut, so
+ *                         results differ from the reference's at the level
+ *                         of the approximation (a few 1e-3). */
+enum gwn_soup_tree { GWN_TREE_REFERENCE = 0, GWN_TREE_BINNED = 1 };
 
 /* Message of the last failing call on this thread ("" if none). */
 const char* gwn_last_error(void);
@@ -63,6 +74,17 @@ int gwn_version(void);
 #define GWN_STATUS_WAIT_TIMEOUT 1u
 #define GWN_STATUS_BAD_INPUT 2u
 int gwn_device_status(unsigned int* flags, int clear);
+
+/* Failure-path testing (no counterpart in the reference, which has asserts
+ * only).  The next n launches of a kernel that streams triangles through a
+ * bounded bulk-copy ring (the exact path's all-pairs sweeps, in
+ * gwn_winding_number and gwn_winding_number_noalloc) initialise one mbarrier
+ * for one more arrival than they make, so their first wait runs out of its
+ * budget (about 50 ms); each such kernel then makes the missing arrival,
+ * waits for its copies in flight, records GWN_STATUS_WAIT_TIMEOUT and
+ * returns.  The call reports GWN_ERR_TIMEOUT (host memory) or the status bit
+ * (device memory); the device stays usable.  n = 0 cancels. */
+int gwn_debug_fail_next_waits(int n);
 
 /* ------------------------------------------------------------------------
  * Exact generalized winding number.
@@ -94,9 +116,14 @@ int gwn_winding_number(const double* V, int64_t nV, int dim, const int32_t* F, i
  * GWN_ERR_INVALID_ARGUMENT.  All calls share that array and leave their
  * contents in it, so calls that overlap on the GPU (on different streams)
  * race; calls on one stream are ordered.  The first call on a device looks up
- * the array's device address: make it before any stream capture.
- * dev_status (optional device pointer, zeroed by the caller) receives
- * GWN_STATUS_* bits for failures found on the device. */
+ * the array's device address and keeps it for the life of the process: make
+ * that call before any stream capture, and make no call after a
+ * cudaDeviceReset (the kept address would be stale).  V must hold nV > 0
+ * vertices whenever nF > 0.  dev_status (optional device pointer, zeroed by
+ * the caller) receives GWN_STATUS_* bits for failures found on the device
+ * (an index of F outside V, a bounded wait that gave up); with dev_status
+ * NULL they are kept in a word of the same static memory, which
+ * gwn_device_status reads and clears. */
 #define GWN_NOALLOC_MAX_TRIANGLES 65536
 int gwn_winding_number_noalloc(const double* V, int64_t nV, const int32_t* F, int64_t nF,
                                const double* O, int64_t nO, double* W, unsigned int* dev_status,
@@ -120,15 +147,31 @@ int gwn_winding_number_noalloc(const double* V, int64_t nV, const int32_t* F, in
 typedef struct gwn_soup gwn_soup;
 
 typedef struct gwn_soup_stats {
-  int64_t num_triangles;   /* triangles kept (non-finite boxes excluded) */
-  int64_t num_nodes;       /* binary tree nodes, leaves included          */
-  int64_t device_bytes;    /* device memory held by the handle            */
+  int64_t num_triangles;   /* triangles kept (non-finite boxes excluded)      */
+  int64_t num_nodes;       /* walk records: binary tree nodes, leaves included,
+                              or the 4-wide tree's root plus every child lane */
+  int64_t device_bytes;    /* device memory held by the handle                 */
   int32_t order;
-  int32_t max_depth;
+  int32_t max_depth;       /* binary: longest root-leaf path; 4-wide: depths   */
+  int32_t tree;            /* GWN_TREE_REFERENCE or GWN_TREE_BINNED            */
+  int32_t reserved;
+  int64_t tree_nodes;      /* nodes of the tree (4-wide: the reference's count) */
 } gwn_soup_stats;
 
+/* gwn_soup_build_tree builds with the chosen tree (gwn_soup_tree);
+ * gwn_soup_build with GWN_SOUP_TREE_DEFAULT. */
+#define GWN_SOUP_TREE_DEFAULT GWN_TREE_REFERENCE
+int gwn_soup_build_tree(const double* V, int64_t nV, const int32_t* F, int64_t nF, int order,
+                        int tree, int mem, void* stream, gwn_soup** out);
 int gwn_soup_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, int order,
                    int mem, void* stream, gwn_soup** out);
+/* The 4-wide tree of a GWN_TREE_REFERENCE handle as the reference stores it
+ * (UT_BVH<4>::Node, FastWindingNumberForSoups.h:4214-4270): *num_nodes
+ * nodes in the reference's numbering (depth-first, children in lane order)
+ * and, if child is non-null, 4 entries per node: a triangle index, node |
+ * 0x80000000 for an internal child, 0xffffffff for an empty lane.  For
+ * testing and inspection. */
+int gwn_soup_tree_nodes(const gwn_soup* soup, int64_t* num_nodes, uint32_t* child);
 int gwn_soup_eval(const gwn_soup* soup, float accuracy_scale, const void* Q, int q_dtype,
                   int64_t nQ, void* W, int w_dtype, int precision, int mem, void* stream);
 int gwn_soup_stats_get(const gwn_soup* soup, gwn_soup_stats* out);

@@ -154,7 +154,11 @@ def winding_number(V, F, O, precision="mixed", out_dtype=None):
 # ---------------------------------------------------------- triangle soup --
 class _SoupStats(C.Structure):
     _fields_ = [("num_triangles", C.c_int64), ("num_nodes", C.c_int64),
-                ("device_bytes", C.c_int64), ("order", C.c_int32), ("max_depth", C.c_int32)]
+                ("device_bytes", C.c_int64), ("order", C.c_int32), ("max_depth", C.c_int32),
+                ("tree", C.c_int32), ("reserved", C.c_int32), ("tree_nodes", C.c_int64)]
+
+
+TREE_REFERENCE, TREE_BINNED = N.GWN_TREE_REFERENCE, N.GWN_TREE_BINNED
 
 
 class FastWindingNumberBVH:
@@ -162,19 +166,36 @@ class FastWindingNumberBVH:
     include/igl/fast_winding_number.h:140-147).  Built by
     ``fast_winding_number_soup_precompute``; owns device copies of V and F."""
 
-    def __init__(self, V, F, order: int = 2):
+    def __init__(self, V, F, order: int = 2, tree: str = "reference"):
+        """``tree``: "reference" -- libigl's own 4-wide SAH tree, built on the
+        GPU node for node (results equal the reference's up to its FP32
+        rounding); "binned" -- a binary tree of binned splits (a different
+        tree cut)."""
         L = N.load()
         Va = _Arg(V, np.float64)
         Fa = _Arg(F, np.int32, allowed=(np.int32,))
         mem = _same_mem(Va, Fa)
         if len(Va.shape) != 2 or Va.shape[1] != 3 or len(Fa.shape) != 2 or Fa.shape[1] != 3:
             raise ValueError("V must be #V x 3 and F #F x 3")
+        kinds = {"reference": N.GWN_TREE_REFERENCE, "binned": N.GWN_TREE_BINNED}
+        if tree not in kinds:
+            raise ValueError(f"tree must be one of {sorted(kinds)}")
         h = C.c_void_p()
         stream = _stream_ptr() if mem == N.GWN_DEVICE else None
-        N.check(L.gwn_soup_build(Va.ptr, Va.shape[0], Fa.ptr, Fa.shape[0], int(order), mem, stream,
-                                 C.byref(h)))
+        N.check(L.gwn_soup_build_tree(Va.ptr, Va.shape[0], Fa.ptr, Fa.shape[0], int(order),
+                                      kinds[tree], mem, stream, C.byref(h)))
         self._h = h
         self.order = order
+        self.tree = tree
+
+    def tree_nodes(self) -> np.ndarray:
+        """The 4-wide tree as the reference stores it (tree="reference"):
+        #nodes x 4 uint32, a triangle index, node | 2^31, or 2^32-1 (empty)."""
+        n = C.c_int64(0)
+        N.check(N.load().gwn_soup_tree_nodes(self._h, C.byref(n), None))
+        out = np.empty((n.value, 4), np.uint32)
+        N.check(N.load().gwn_soup_tree_nodes(self._h, C.byref(n), out.ctypes.data_as(C.c_void_p)))
+        return out
 
     def eval(self, Q, accuracy_scale: float = 2.0, precision="mixed", out_dtype=None):
         """W(p) = computeSolidAngle(p, accuracy_scale) / 4pi for every row of Q."""

@@ -16,6 +16,7 @@ GWN_OK = 0
 GWN_F32, GWN_F64 = 0, 1
 GWN_PLAIN_FP64, GWN_MIXED = 0, 1
 GWN_HOST, GWN_DEVICE = 0, 1
+GWN_TREE_REFERENCE, GWN_TREE_BINNED = 0, 1
 
 STATUS_NAMES = {
     1: "GWN_ERR_INVALID_ARGUMENT",
@@ -34,9 +35,12 @@ SIGNATURES = {
     "gwn_last_error": ([], C.c_char_p),
     "gwn_version": ([], _i),
     "gwn_device_status": ([_p, _i], _i),
+    "gwn_debug_fail_next_waits": ([_i], _i),
     "gwn_winding_number": ([_p, _i64, _i, _p, _i64, _p, _i, _i64, _p, _i, _i, _i, _p], _i),
     "gwn_winding_number_noalloc": ([_p, _i64, _p, _i64, _p, _i64, _p, _p, _p], _i),
     "gwn_soup_build": ([_p, _i64, _p, _i64, _i, _i, _p, _p], _i),
+    "gwn_soup_build_tree": ([_p, _i64, _p, _i64, _i, _i, _i, _p, _p], _i),
+    "gwn_soup_tree_nodes": ([_p, _p, _p], _i),
     "gwn_soup_eval": ([_p, _f, _p, _i, _i64, _p, _i, _i, _i, _p], _i),
     "gwn_soup_stats_get": ([_p, _p], _i),
     "gwn_soup_free": ([_p], None),

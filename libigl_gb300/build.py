@@ -22,6 +22,9 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
               "--expt-relaxed-constexpr", "-I", INCLUDE]
+# Per-file additions.  soup_ref.cu reproduces the reference's FP32 tree build
+# and moments bit for bit, so no multiply-add may be fused there.
+FILE_FLAGS = {"soup_ref.cu": ["--fmad=false"]}
 
 
 def nvcc() -> str:
@@ -63,7 +66,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
 
     def compile_one(job):
         s, obj = job
-        cmd = [nv, *flags, "-c", s, "-o", obj]
+        cmd = [nv, *flags, *FILE_FLAGS.get(os.path.basename(s), []), "-c", s, "-o", obj]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -26,6 +26,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstddef>
 #include <mutex>
 #include <string>
 #include <type_traits>
@@ -233,7 +234,7 @@ __global__ void __launch_bounds__(kThreads) exact3_mixed_kernel(
     const TriF* __restrict__ tris, const double* __restrict__ tris64,
     const float4* __restrict__ meta, int ntiles, const QT* __restrict__ Q, int64_t nQ,
     WT* __restrict__ W, int32_t* __restrict__ refine_list, unsigned* __restrict__ refine_count,
-    unsigned* __restrict__ status) {
+    unsigned* __restrict__ status, int withhold) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   Smem3& sm = *reinterpret_cast<Smem3*>(smem_raw);
   const int tid = threadIdx.x;
@@ -245,7 +246,9 @@ __global__ void __launch_bounds__(kThreads) exact3_mixed_kernel(
 
   constexpr uint32_t kTileBytes = sizeof(TriF) * kTile;
   if (tid == 0) {
-    for (int s = 0; s < kStages; ++s) mbar_init(&sm.bar[s], 1);
+    // withhold != 0 (failure-path tests only): stage 0 expects one more
+    // arrival than is ever made, so the first wait runs out of its budget.
+    for (int s = 0; s < kStages; ++s) mbar_init(&sm.bar[s], (withhold && s == 0) ? 2 : 1);
     fence_mbar_init();
     for (int s = 0; s < kStages && s < ntiles; ++s) {
       mbar_arrive_expect_tx(&sm.bar[s], kTileBytes);
@@ -315,6 +318,7 @@ __global__ void __launch_bounds__(kThreads) exact3_mixed_kernel(
   if (!ok) {
     if (tid == 0) {
       atomicOr(status, kStatusWaitTimeout);
+      if (withhold) mbar_arrive(&sm.bar[0]);  // the withheld arrival: stage 0 can drain
       drain_ring(sm.bar, kStages, stop_tile, ntiles);
     }
     return;
@@ -344,7 +348,8 @@ __global__ void __launch_bounds__(kThreads) exact3_fp64_kernel(const double* __r
                                                                int ntiles64,
                                                                const QT* __restrict__ Q,
                                                                int64_t nQ, WT* __restrict__ W,
-                                                               unsigned* __restrict__ status) {
+                                                               unsigned* __restrict__ status,
+                                                               int withhold) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   Smem64& sm = *reinterpret_cast<Smem64*>(smem_raw);
   const int tid = threadIdx.x;
@@ -354,7 +359,9 @@ __global__ void __launch_bounds__(kThreads) exact3_fp64_kernel(const double* __r
   if (valid) load_q3(Q, qi, qx, qy, qz);
   constexpr uint32_t kBytes = sizeof(double) * 9 * kTile64;
   if (tid == 0) {
-    for (int s = 0; s < kStages; ++s) mbar_init(&sm.bar[s], 1);
+    // withhold != 0 (failure-path tests only): stage 0 expects one more
+    // arrival than is ever made, so the first wait runs out of its budget.
+    for (int s = 0; s < kStages; ++s) mbar_init(&sm.bar[s], (withhold && s == 0) ? 2 : 1);
     fence_mbar_init();
     for (int s = 0; s < kStages && s < ntiles64; ++s) {
       mbar_arrive_expect_tx(&sm.bar[s], kBytes);
@@ -389,6 +396,7 @@ __global__ void __launch_bounds__(kThreads) exact3_fp64_kernel(const double* __r
   if (!ok) {
     if (tid == 0) {
       atomicOr(status, kStatusWaitTimeout);
+      if (withhold) mbar_arrive(&sm.bar[0]);  // the withheld arrival: stage 0 can drain
       drain_ring(sm.bar, kStages, stop_tile, ntiles64);
     }
     return;
@@ -501,7 +509,7 @@ void launch_exact3(const ExactArgs& a, cudaStream_t st) {
         PhaseTimer ph("nbody", st);
         launch_kernel(exact3_mixed_kernel<QT, WT>, grid, kThreads, smem, st, 
             tris.get(), tris64.get(), meta.get(), ntiles, Q, a.nQ, W, list.get(), count.get(),
-            status.ptr());
+            status.ptr(), take_wait_injection());
       }
       GWN_CUDA(cudaGetLastError());
       {
@@ -521,7 +529,8 @@ void launch_exact3(const ExactArgs& a, cudaStream_t st) {
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       PhaseTimer ph("nbody", st);
       launch_kernel(exact3_fp64_kernel<QT, WT>, grid, kThreads, smem, st, tris64.get(), ntiles64, Q,
-                                                                a.nQ, W, status.ptr());
+                                                                a.nQ, W, status.ptr(),
+                                                                take_wait_injection());
       GWN_CUDA(cudaGetLastError());
     }
     status.check(st, "winding_number (fp64)");
@@ -588,7 +597,10 @@ struct NoAllocScratch {
   TriF tris[kNoAllocMaxTris];          // 4 MiB
   float4 meta[kNoAllocMaxTiles];       // 8 KiB
   unsigned long long mm[6];            // bbox as ordered bits
-  unsigned status;                     // used when the caller passes no status word
+  // Failures of calls made without a status word of their own.  Never
+  // cleared by a call (zero at module load): gwn_device_status reads and
+  // clears it together with the library's other sticky word.
+  unsigned sticky_status;
 };
 static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
 
@@ -596,7 +608,6 @@ __global__ void noalloc_init_kernel(NoAllocScratch* s) {
   const int i = threadIdx.x;
   if (i < 3) s->mm[i] = ~0ull;
   else if (i < 6) s->mm[i] = 0ull;
-  else if (i == 6) s->status = 0u;
 }
 
 // FP32 packing only (near pairs read the caller's FP64 V/F directly).
@@ -651,7 +662,7 @@ __global__ void __launch_bounds__(kThreads) noalloc_mixed_kernel(
     const TriF* __restrict__ tris, const float4* __restrict__ meta, int ntiles,
     const double* __restrict__ V, int64_t nV, const int32_t* __restrict__ F,
     const double* __restrict__ Q, int64_t nQ, double* __restrict__ W,
-    unsigned* __restrict__ status) {
+    unsigned* __restrict__ status, int withhold) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   Smem3& sm = *reinterpret_cast<Smem3*>(smem_raw);
   const int tid = threadIdx.x;
@@ -662,7 +673,9 @@ __global__ void __launch_bounds__(kThreads) noalloc_mixed_kernel(
   const float fx = (float)qx, fy = (float)qy, fz = (float)qz;
   constexpr uint32_t kTileBytes = sizeof(TriF) * kTile;
   if (tid == 0) {
-    for (int s = 0; s < kStages; ++s) mbar_init(&sm.bar[s], 1);
+    // withhold != 0 (failure-path tests only): stage 0 expects one more
+    // arrival than is ever made, so the first wait runs out of its budget.
+    for (int s = 0; s < kStages; ++s) mbar_init(&sm.bar[s], (withhold && s == 0) ? 2 : 1);
     fence_mbar_init();
     for (int s = 0; s < kStages && s < ntiles; ++s) {
       mbar_arrive_expect_tx(&sm.bar[s], kTileBytes);
@@ -716,6 +729,7 @@ __global__ void __launch_bounds__(kThreads) noalloc_mixed_kernel(
   if (!ok) {
     if (tid == 0) {
       atomicOr(status, kStatusWaitTimeout);
+      if (withhold) mbar_arrive(&sm.bar[0]);  // the withheld arrival: stage 0 can drain
       drain_ring(sm.bar, kStages, stop_tile, ntiles);
     }
     return;
@@ -766,6 +780,17 @@ NoAllocScratch* noalloc_scratch_for_current_device() {
 
 int64_t noalloc_max_triangles() { return kNoAllocMaxTris; }
 
+unsigned noalloc_sticky_status(bool clear) {
+  unsigned v = 0;
+  const size_t off = offsetof(NoAllocScratch, sticky_status);
+  GWN_CUDA(cudaMemcpyFromSymbol(&v, g_noalloc_scratch, sizeof(v), off));
+  if (clear && v) {
+    const unsigned zero = 0;
+    GWN_CUDA(cudaMemcpyToSymbol(g_noalloc_scratch, &zero, sizeof(zero), off));
+  }
+  return v;
+}
+
 void run_exact_noalloc(const double* V, int64_t nV, const int32_t* F, int64_t nF, const double* Q,
                        int64_t nQ, double* W, unsigned* dev_status, cudaStream_t st) {
   GWN_REQUIRE(nF <= kNoAllocMaxTris,
@@ -773,7 +798,7 @@ void run_exact_noalloc(const double* V, int64_t nV, const int32_t* F, int64_t nF
                   " exceeds the static scratch limit of " + std::to_string(kNoAllocMaxTris) +
                   " triangles");
   NoAllocScratch* s = noalloc_scratch_for_current_device();
-  unsigned* status = dev_status ? dev_status : &s->status;
+  unsigned* status = dev_status ? dev_status : &s->sticky_status;
   launch_kernel(noalloc_init_kernel, 1, 32, 0, st, s);
   if (nQ == 0) return;
   if (nV > 0)
@@ -790,7 +815,7 @@ void run_exact_noalloc(const double* V, int64_t nV, const int32_t* F, int64_t nF
   GWN_CUDA(cudaFuncSetAttribute(noalloc_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem));
   launch_kernel(noalloc_mixed_kernel, (unsigned)((nQ + kThreads - 1) / kThreads), kThreads, smem,
-                st, s->tris, s->meta, ntiles, V, nV, F, Q, nQ, W, status);
+                st, s->tris, s->meta, ntiles, V, nV, F, Q, nQ, W, status, take_wait_injection());
   launch_kernel(noalloc_refine_kernel, num_sms() * 8, 256, 0, st, V, nV, F, nF, Q, nQ, W);
 }
 

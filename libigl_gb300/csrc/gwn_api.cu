@@ -119,6 +119,17 @@ int num_sms() {
   return g_sms[d];
 }
 
+namespace {
+std::atomic<int> g_wait_injections{0};
+}  // namespace
+
+int take_wait_injection() {
+  int n = g_wait_injections.load();
+  while (n > 0 && !g_wait_injections.compare_exchange_weak(n, n - 1)) {
+  }
+  return n > 0 ? 1 : 0;
+}
+
 unsigned int* sticky_status_word() {
   const int d = current_device();
   std::lock_guard<std::mutex> lk(g_dev_mutex);
@@ -196,6 +207,10 @@ using namespace gwn;
 
 struct gwn_soup {
   gwn_soup_impl impl;
+  // Closest-point search for a GWN_TREE_REFERENCE handle: the binned tree
+  // over the same triangles, built on the first gwn_soup_squared_distance.
+  std::mutex search_mu;
+  std::unique_ptr<gwn_soup_impl> search;
 };
 struct gwn_octree {
   gwn_octree_impl impl;
@@ -232,7 +247,15 @@ int gwn_device_status(unsigned int* flags, int clear) {
     GWN_CUDA(cudaDeviceSynchronize());
     GWN_CUDA(cudaMemcpy(&v, w, sizeof(v), cudaMemcpyDeviceToHost));
     if (clear) GWN_CUDA(cudaMemset(w, 0, sizeof(unsigned int)));
+    v |= noalloc_sticky_status(clear != 0);
     if (flags) *flags = v;
+  });
+}
+
+int gwn_debug_fail_next_waits(int n) {
+  return guarded("gwn_debug_fail_next_waits", [&] {
+    GWN_REQUIRE(n >= 0, "n must be non-negative");
+    g_wait_injections.store(n);
   });
 }
 
@@ -243,7 +266,7 @@ int gwn_winding_number(const double* V, int64_t nV, int dim, const int32_t* F, i
     profile_begin_call();
     GWN_REQUIRE(dim == 2 || dim == 3, "dim must be 2 (edges) or 3 (triangles)");
     GWN_REQUIRE(nV >= 0 && nF >= 0 && nO >= 0, "sizes must be non-negative");
-    GWN_REQUIRE(nF == 0 || (V && F), "V and F must be non-null");
+    check_mesh(V, nV, F, nF);
     GWN_REQUIRE(nO == 0 || (O && W), "O and W must be non-null");
     GWN_REQUIRE(nO < (int64_t(1) << 31), "at most 2^31-1 queries per call");
     check_dtype(o_dtype, "O");
@@ -268,13 +291,14 @@ int gwn_winding_number(const double* V, int64_t nV, int dim, const int32_t* F, i
   });
 }
 
-int gwn_soup_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, int order,
-                   int mem, void* stream, gwn_soup** out) {
+int gwn_soup_build_tree(const double* V, int64_t nV, const int32_t* F, int64_t nF, int order,
+                        int tree, int mem, void* stream, gwn_soup** out) {
   return guarded("gwn_soup_build", [&] {
     GWN_REQUIRE(out != nullptr, "out must be non-null");
     *out = nullptr;
-    GWN_REQUIRE(nV >= 0 && nF >= 0, "sizes must be non-negative");
-    GWN_REQUIRE(nF == 0 || (V && F), "V and F must be non-null");
+    check_mesh(V, nV, F, nF);
+    GWN_REQUIRE(tree == GWN_TREE_REFERENCE || tree == GWN_TREE_BINNED,
+                "tree must be GWN_TREE_REFERENCE or GWN_TREE_BINNED");
     check_mem(mem);
     ensure_device();
     cudaStream_t st = as_stream(stream);
@@ -283,13 +307,33 @@ int gwn_soup_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, in
     gwn_soup* s = new gwn_soup();
     try {
       GWN_CUDA(cudaGetDevice(&s->impl.device));
-      soup_build(s->impl, dV.dev, nV, dF.dev, nF, order, mem == GWN_HOST, st);
+      if (tree == GWN_TREE_REFERENCE)
+        soup_build_ref(s->impl, dV.dev, nV, dF.dev, nF, order, mem == GWN_HOST, st);
+      else
+        soup_build(s->impl, dV.dev, nV, dF.dev, nF, order, mem == GWN_HOST, st);
       GWN_CUDA(cudaStreamSynchronize(st));
     } catch (...) {
       delete s;
       throw;
     }
     *out = s;
+  });
+}
+
+int gwn_soup_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, int order,
+                   int mem, void* stream, gwn_soup** out) {
+  return gwn_soup_build_tree(V, nV, F, nF, order, GWN_SOUP_TREE_DEFAULT, mem, stream, out);
+}
+
+int gwn_soup_tree_nodes(const gwn_soup* soup, int64_t* num_nodes, uint32_t* child) {
+  return guarded("gwn_soup_tree_nodes", [&] {
+    GWN_REQUIRE(soup != nullptr, "soup handle is null");
+    const gwn_soup_impl& s = soup->impl;
+    GWN_REQUIRE(s.tree == GWN_TREE_REFERENCE,
+                "the handle was built with GWN_TREE_BINNED (no 4-wide node array)");
+    if (num_nodes) *num_nodes = s.ref_nodes;
+    if (child && s.ref_nodes)
+      GWN_CUDA(cudaMemcpy(child, s.ref_child.get(), s.ref_child.bytes(), cudaMemcpyDeviceToHost));
   });
 }
 
@@ -338,6 +382,9 @@ int gwn_soup_stats_get(const gwn_soup* soup, gwn_soup_stats* out) {
     GWN_REQUIRE(soup && out, "null argument");
     out->num_triangles = soup->impl.n;
     out->num_nodes = soup->impl.nnodes;
+    out->tree = soup->impl.tree;
+    out->tree_nodes = soup->impl.tree == GWN_TREE_REFERENCE ? soup->impl.ref_nodes
+                                                            : soup->impl.nnodes;
     out->device_bytes = (int64_t)soup->impl.bytes;
     out->order = soup->impl.order;
     out->max_depth = soup->impl.max_depth;
@@ -674,7 +721,24 @@ int gwn_soup_squared_distance(const gwn_soup* soup, const void* Q, int q_dtype, 
     Staged<double> dD(sqrD, (size_t)nQ, mem, st, false);
     Staged<int32_t> dI(I, (size_t)nQ, mem, st, false);
     Staged<double> dC(C, (size_t)nQ * 3, mem, st, false);
-    soup_squared_distance(soup->impl, dQ.dev, q_dtype, nQ, up_sqr_d, dD.dev, dI.dev, dC.dev, st);
+    if (soup->impl.tree == GWN_TREE_REFERENCE) {
+      gwn_soup* ms = const_cast<gwn_soup*>(soup);
+      {
+        std::lock_guard<std::mutex> lk(ms->search_mu);
+        if (!ms->search) {
+          auto srch = std::make_unique<gwn_soup_impl>();
+          srch->device = soup->impl.device;
+          soup_build_search(soup->impl, *srch, st);
+          ms->search = std::move(srch);
+        }
+      }
+      soup_squared_distance(*soup->search, dQ.dev, q_dtype, nQ, up_sqr_d, dD.dev, dI.dev, dC.dev,
+                            st);
+      soup_remap_index(soup->impl.tri_index.get(), dI.dev, nQ, st);
+    } else {
+      soup_squared_distance(soup->impl, dQ.dev, q_dtype, nQ, up_sqr_d, dD.dev, dI.dev, dC.dev,
+                            st);
+    }
     if (mem == GWN_HOST && nQ) {
       GWN_CUDA(cudaMemcpyAsync(sqrD, dD.dev, (size_t)nQ * 8, cudaMemcpyDeviceToHost, st));
       GWN_CUDA(cudaMemcpyAsync(I, dI.dev, (size_t)nQ * 4, cudaMemcpyDeviceToHost, st));
@@ -691,7 +755,7 @@ int gwn_signed_distance(const double* P, int64_t nP, const double* V, int64_t nV
   return guarded("gwn_signed_distance", [&] {
     GWN_REQUIRE(nP >= 0 && nV >= 0 && nF >= 0, "sizes must be non-negative");
     GWN_REQUIRE(nP == 0 || (P && S && I && C), "P, S, I and C must be non-null");
-    GWN_REQUIRE(nF == 0 || (V && F), "V and F must be non-null");
+    check_mesh(V, nV, F, nF);
     GWN_REQUIRE(nP < (int64_t(1) << 31), "at most 2^31-1 queries per call");
     GWN_REQUIRE(sign_type >= GWN_SD_PSEUDONORMAL && sign_type <= GWN_SD_FAST_WINDING_NUMBER,
                 "sign_type must be one of GWN_SD_*");
@@ -725,7 +789,7 @@ int gwn_winding_number_noalloc(const double* V, int64_t nV, const int32_t* F, in
                                void* stream) {
   return guarded("gwn_winding_number_noalloc", [&] {
     GWN_REQUIRE(nV >= 0 && nF >= 0 && nO >= 0, "sizes must be non-negative");
-    GWN_REQUIRE(nF == 0 || (V && F), "V and F must be non-null");
+    check_mesh(V, nV, F, nF);
     GWN_REQUIRE(nO == 0 || (O && W), "O and W must be non-null");
     GWN_REQUIRE(nO < (int64_t(1) << 31), "at most 2^31-1 queries per call");
     GWN_REQUIRE(nF <= noalloc_max_triangles(),
@@ -841,7 +905,7 @@ int gwn_swept_volume_signed_distance(const double* V, int64_t nV, const int32_t*
   return guarded("gwn_swept_volume_signed_distance", [&] {
     profile_begin_call();
     GWN_REQUIRE(nV >= 0 && nF >= 0 && nT >= 0 && nGV >= 0, "sizes must be non-negative");
-    GWN_REQUIRE(nF == 0 || (V && F), "V and F must be non-null");
+    check_mesh(V, nV, F, nF);
     GWN_REQUIRE(nT == 0 || transforms, "transforms must be non-null");
     GWN_REQUIRE(nGV == 0 || (GV && S), "GV and S must be non-null");
     GWN_REQUIRE(res != nullptr, "res must be non-null");
@@ -914,7 +978,7 @@ int gwn_wn_aabb_build(const double* V, int64_t nV, const int32_t* F, int64_t nF,
     GWN_REQUIRE(out != nullptr, "out must be non-null");
     *out = nullptr;
     GWN_REQUIRE(nV >= 0 && nF >= 0, "sizes must be non-negative");
-    GWN_REQUIRE(nF == 0 || (V && F), "V and F must be non-null");
+    check_mesh(V, nV, F, nF);
     check_mem(mem);
     ensure_device();
     cudaStream_t st = as_stream(stream);

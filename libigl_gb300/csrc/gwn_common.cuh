@@ -175,12 +175,26 @@ inline void check_dtype(int dt, const char* what) {
 inline void check_precision(int p) {
   GWN_REQUIRE(p == GWN_PLAIN_FP64 || p == GWN_MIXED, "precision must be GWN_PLAIN_FP64 or GWN_MIXED");
 }
+// Mesh arguments: F (nF rows) indexes V (nV rows).  A non-empty array needs a
+// non-null pointer and a non-empty F needs vertices to index, so no kernel
+// reads through a null V or clamps indices into an empty one.
+inline void check_mesh(const void* V, int64_t nV, const void* F, int64_t nF) {
+  GWN_REQUIRE(nV >= 0 && nF >= 0, "sizes must be non-negative");
+  GWN_REQUIRE(nV == 0 || V, "V must be non-null when nV > 0");
+  GWN_REQUIRE(nF == 0 || F, "F must be non-null when nF > 0");
+  GWN_REQUIRE(nF == 0 || nV > 0, "F has elements but V has no vertices");
+}
 inline void check_mem(int m) {
   GWN_REQUIRE(m == GWN_HOST || m == GWN_DEVICE, "mem must be GWN_HOST or GWN_DEVICE");
 }
 
 void ensure_device();
 int num_sms();
+
+// Failure-path testing (gwn_debug_fail_next_waits): 1 if the next bounded
+// bulk-copy ring launch is to withhold one mbarrier arrival (consumes one
+// pending request), else 0.
+int take_wait_injection();
 
 // Device-side status word written by kernels (atomicOr of kStatus* bits).
 // Host-memory calls get a private word that is read after the call's own
@@ -238,9 +252,14 @@ void init_minmax(unsigned long long* mm, int dim, cudaStream_t s);
 
 constexpr unsigned kStatusWaitTimeout = 1u;
 constexpr unsigned kStatusBadInput = 2u;
+constexpr unsigned kStatusInternal = 4u;  // a device-side consistency check failed
 
-// Spin limit for mbarrier waits: a bulk copy of a few KB from L2 finishes in
-// microseconds; 2^26 polls is many seconds.
+// Budget of a bounded mbarrier wait.  A bulk copy of a few KB lands within
+// microseconds; a wait gives up once 50 ms of %globaltimer have passed and it
+// has polled at least kMinPolls times (so a stale first timer read cannot end
+// it early), or after kSpinLimit polls whatever the timer says.
+constexpr uint64_t kWaitBudgetNs = 50ull * 1000 * 1000;
+constexpr uint32_t kMinPolls = 4096;
 constexpr uint32_t kSpinLimit = 1u << 26;
 
 // --------------------------------------------------------- device helpers ----
@@ -283,11 +302,23 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 // Bounded wait: returns false (and the caller reports a timeout) instead of
-// spinning forever.
+// spinning forever; see kWaitBudgetNs.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-  for (uint32_t i = 0; i < kSpinLimit; ++i)
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = globaltimer_ns();
+  for (uint32_t i = 1; i < kSpinLimit; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
+    if (i >= kMinPolls && (i & 63u) == 0 && globaltimer_ns() - t0 > kWaitBudgetNs) return false;
+  }
   return false;
 }
 

@@ -36,6 +36,9 @@ void exact_refine_listed(const double* tris64, int64_t nF, const double* Q, cons
 // No-allocation exact winding number (device pointers, mixed precision,
 // triangles); scratch in a static device array of fixed capacity.
 int64_t noalloc_max_triangles();
+// GWN_STATUS_* bits that gwn_winding_number_noalloc calls without a status
+// word of their own recorded on the current device (cleared if `clear`).
+unsigned noalloc_sticky_status(bool clear);
 void run_exact_noalloc(const double* V, int64_t nV, const int32_t* F, int64_t nF, const double* Q,
                        int64_t nQ, double* W, unsigned* dev_status, cudaStream_t st);
 

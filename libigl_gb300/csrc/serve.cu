@@ -519,7 +519,10 @@ int gwn_server::admit(SrvMesh* m, std::unique_lock<std::mutex>& lk, int& code, s
     dV.upload(m->V.data(), (size_t)nV * 3, build_st);
     dF.upload(m->F.data(), (size_t)nF * 3, build_st);
     res->device = device;
-    soup_build(*res, dV.get(), nV, dF.get(), nF, m->order, true, build_st);
+    if (GWN_SOUP_TREE_DEFAULT == GWN_TREE_REFERENCE)
+      soup_build_ref(*res, dV.get(), nV, dF.get(), nF, m->order, true, build_st);
+    else
+      soup_build(*res, dV.get(), nV, dF.get(), nF, m->order, true, build_st);
     GWN_CUDA(cudaStreamSynchronize(build_st));
   } catch (const Error& e) {
     rc = e.code;
@@ -598,6 +601,7 @@ bool gwn_server::form_and_launch(SrvSlot& s, std::unique_lock<std::mutex>& lk) {
     d.prm.eps = (float)t.eps;
     d.prm.cmax = (float)t.cmax;
     d.prm.status = nullptr;
+    d.prm.ref32 = t.tree == GWN_TREE_REFERENCE;
     for (int k = 0; k < 3; ++k) {
       // the query box: the mesh box grown by a quarter on each side
       const double e = std::max(t.hi[k] - t.lo[k], 1e-30);
@@ -827,7 +831,7 @@ int gwn_server_add_mesh(gwn_server* S, const double* V, int64_t nV, const int32_
   return guarded("gwn_server_add_mesh", [&] {
     GWN_REQUIRE(S != nullptr && mesh_id != nullptr, "server and mesh_id must be non-null");
     GWN_REQUIRE(nV >= 0 && nF >= 0, "sizes must be non-negative");
-    GWN_REQUIRE(nF == 0 || (V && F), "V and F must be non-null");
+    check_mesh(V, nV, F, nF);
     GWN_REQUIRE(nF < (int64_t(1) << 30), "at most 2^30 triangles");
     GWN_REQUIRE(order >= 0 && order <= 2, "order must be 0, 1 or 2");
     for (int64_t i = 0; i < nF * 3; ++i)

@@ -427,31 +427,7 @@ __global__ void emit_kernel(const BuildM* __restrict__ M, const int32_t* __restr
     for (int k = 0; k < 9; ++k) td[(int64_t)slot * 9 + k] = v[k];
     tf[(int64_t)slot * 3 + 0] = make_float4((float)v[0], (float)v[1], (float)v[2], (float)v[3]);
     tf[(int64_t)slot * 3 + 1] = make_float4((float)v[4], (float)v[5], (float)v[6], (float)v[7]);
-    // .y: error slack of the FP32 closest-point screen for this triangle
-    // (distance.cu): 32 u (|e1|^2 |e2|^2 / |e1 x e2|^2) L + 8 u max|v|,
-    // u = 2^-24, L the longest edge; infinite for a (near) degenerate one.
-    float slack = INFINITY;
-    {
-      double e1[3], e2[3], e3[3], cr[3];
-      double l1 = 0, l2 = 0, l3 = 0, vm = 0;
-      for (int d = 0; d < 3; ++d) {
-        e1[d] = v[3 + d] - v[d];
-        e2[d] = v[6 + d] - v[d];
-        e3[d] = v[6 + d] - v[3 + d];
-        l1 += e1[d] * e1[d];
-        l2 += e2[d] * e2[d];
-        l3 += e3[d] * e3[d];
-        vm = fmax(vm, fmax(fabs(v[d]), fmax(fabs(v[3 + d]), fabs(v[6 + d]))));
-      }
-      cr[0] = e1[1] * e2[2] - e1[2] * e2[1];
-      cr[1] = e1[2] * e2[0] - e1[0] * e2[2];
-      cr[2] = e1[0] * e2[1] - e1[1] * e2[0];
-      const double den = cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2];
-      const double cond = den > 0 ? l1 * l2 / den : INFINITY;
-      const double u = 5.9604644775390625e-08;
-      if (cond < 1e6) slack = (float)(32 * u * cond * sqrt(fmax(l1, fmax(l2, l3))) + 8 * u * vm);
-    }
-    tf[(int64_t)slot * 3 + 2] = make_float4((float)v[8], slack, 0.f, 0.f);
+    tf[(int64_t)slot * 3 + 2] = make_float4((float)v[8], tri_screen_slack(v), 0.f, 0.f);
   }
 }
 
@@ -653,6 +629,7 @@ static void soup_eval_t(const gwn_soup_impl& s, float beta, const void* Qv, int6
   prm.eps = (float)s.eps;
   prm.cmax = (float)s.cmax;
   prm.status = nullptr;
+  prm.ref32 = s.tree == GWN_TREE_REFERENCE;
   QueryOrder qo;
   {
     PhaseTimer ph("order_queries", st);
@@ -699,6 +676,7 @@ void soup_walk_stats(const gwn_soup_impl& s, float beta, const double* Q, int64_
   prm.eps = (float)s.eps;
   prm.cmax = (float)s.cmax;
   prm.status = nullptr;
+  prm.ref32 = s.tree == GWN_TREE_REFERENCE;
   QueryOrder qo;
   order_queries(Q, GWN_F64, nQ, s.lo, s.hi, qo, st);
   DevBuf<double> W((size_t)nQ, st);

@@ -30,9 +30,42 @@ struct __align__(16) SoupNodeD {
   long long link;
 };
 
+#ifdef __CUDACC__
+// Error slack of the FP32 closest-point screen for one triangle (v: three
+// FP64 corners; distance.cu): 32 u (|e1|^2 |e2|^2 / |e1 x e2|^2) L + 8 u
+// max|v|, u = 2^-24, L the longest edge; infinite for a (near) degenerate one.
+__device__ inline float tri_screen_slack(const double* v) {
+  double e1[3], e2[3], e3[3], cr[3];
+  double l1 = 0, l2 = 0, l3 = 0, vm = 0;
+  for (int d = 0; d < 3; ++d) {
+    e1[d] = v[3 + d] - v[d];
+    e2[d] = v[6 + d] - v[d];
+    e3[d] = v[6 + d] - v[3 + d];
+    l1 += e1[d] * e1[d];
+    l2 += e2[d] * e2[d];
+    l3 += e3[d] * e3[d];
+    vm = fmax(vm, fmax(fabs(v[d]), fmax(fabs(v[3 + d]), fabs(v[6 + d]))));
+  }
+  cr[0] = e1[1] * e2[2] - e1[2] * e2[1];
+  cr[1] = e1[2] * e2[0] - e1[0] * e2[2];
+  cr[2] = e1[0] * e2[1] - e1[1] * e2[0];
+  const double den = cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2];
+  const double cond = den > 0 ? l1 * l2 / den : INFINITY;
+  const double u = 5.9604644775390625e-08;
+  if (cond < 1e6) return (float)(32 * u * cond * sqrt(fmax(l1, fmax(l2, l3))) + 8 * u * vm);
+  return INFINITY;
+}
+#endif
+
 struct gwn_soup_impl {
   int device = 0;
   int order = 2;
+  // GWN_TREE_REFERENCE: the reference's 4-wide tree (soup_ref.cu), whose
+  // open test is the reference's FP32 one; GWN_TREE_BINNED: the binary
+  // tree of soup_tree.cu.
+  int tree = GWN_TREE_BINNED;
+  int64_t ref_nodes = 0;       // nodes of the 4-wide tree (reference numbering)
+  DevMem<uint32_t> ref_child;  // 4 lanes per node, the reference's encoding
   int64_t n_input = 0;   // triangles passed in
   int64_t n = 0;         // triangles kept (finite, valid)
   int64_t nnodes = 0;    // 2n-1
@@ -63,6 +96,17 @@ void soup_tree_build(const double* V, int64_t nV, const int32_t* F, int32_t* val
 
 void soup_build(gwn_soup_impl& s, const double* V, int64_t nV, const int32_t* F, int64_t nF,
                 int order, bool host_mode, cudaStream_t st);
+// The reference's own 4-wide tree and FP32 moments (soup_ref.cu); fills the
+// same walk records (slot 0 the root, then every child lane depth-first),
+// without the closest-point search nodes.
+void soup_build_ref(gwn_soup_impl& s, const double* V, int64_t nV, const int32_t* F, int64_t nF,
+                    int order, bool host_mode, cudaStream_t st);
+// The binned tree over the triangles of a GWN_TREE_REFERENCE soup (its
+// slot-ordered FP64 corners), for the closest-point search; the search
+// tree's triangle ids are the reference soup's leaf slots.
+void soup_build_search(const gwn_soup_impl& ref, gwn_soup_impl& search, cudaStream_t st);
+// I[q] <- map[I[q]] where I[q] >= 0.
+void soup_remap_index(const int32_t* map, int32_t* I, int64_t n, cudaStream_t st);
 // Instrumented mixed walk over FP64 device queries: out7 = {warp steps,
 // lane visits, far-field evaluations, FP32 exact triangles, FP64 near-field
 // triangles, FP64 decision re-checks, threshold re-evaluations}.

@@ -144,7 +144,19 @@ struct EvalParams {
   float eps;       // near-field distance (1e-3 * bbox diagonal)
   float cmax;      // max |coordinate| of any node centre
   unsigned* status;
+  int ref32;       // open test: the reference's FP32 one (GWN_TREE_REFERENCE)
 };
+
+// The reference's descend test (FWNFS.h:7176-7193) on its FP32 data: q cast
+// to float, |q - P|^2 summed as (x^2 + y^2) + z^2 and compared with
+// maxP2 * beta^2, each operation rounded on its own as in the SSE code,
+// which has no fused multiply-add.  With the reference's P and maxP2 (the
+// FP32 records of GWN_TREE_REFERENCE) it decides as the reference does.
+__device__ __forceinline__ bool ref_open32(float qx, float qy, float qz, float4 a, float beta2) {
+  const float dx = __fsub_rn(qx, a.x), dy = __fsub_rn(qy, a.y), dz = __fsub_rn(qz, a.z);
+  const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+  return r2 <= __fmul_rn(a.w, beta2);
+}
 
 // FP64 solid angle of the triangle t[0..8] (xyz of three corners) seen from
 // q, in the unnormalised van Oosterom-Strackee form of igl::solid_angle
@@ -249,12 +261,17 @@ __device__ __forceinline__ void walk_mixed(const EvalParams& prm, bool valid, do
         const float dx = fx - a.x, dy = fy - a.y, dz = fz - a.z;
         const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
         const float thr = a.w * prm.beta2f;
-        bool near = r2 <= thr;
-        if (in_guard_band(r2, thr, sigma)) {
-          const SoupNodeD* rd = prm.nd + node;
-          near = open_test64(nq.q[lane][0], nq.q[lane][1], nq.q[lane][2], rd->P[0], rd->P[1],
-                             rd->P[2], rd->maxP2, prm.beta2d);
-          if (kStats) ++c.recheck;
+        bool near;
+        if (prm.ref32) {
+          near = ref_open32(fx, fy, fz, a, prm.beta2f);
+        } else {
+          near = r2 <= thr;
+          if (in_guard_band(r2, thr, sigma)) {
+            const SoupNodeD* rd = prm.nd + node;
+            near = open_test64(nq.q[lane][0], nq.q[lane][1], nq.q[lane][2], rd->P[0], rd->P[1],
+                               rd->P[2], rd->maxP2, prm.beta2d);
+            if (kStats) ++c.recheck;
+          }
         }
         if (!near) {
           if (kStats) ++c.far;
@@ -328,7 +345,10 @@ __device__ __forceinline__ double walk_fp64(const EvalParams& prm, bool valid, d
       if (node == 0 && !leaf) {
         open = true;
       } else {
-        bool near = open_test64(qx, qy, qz, r->P[0], r->P[1], r->P[2], r->maxP2, prm.beta2d);
+        bool near = prm.ref32 ? ref_open32((float)qx, (float)qy, (float)qz,
+                                           __ldg(&prm.nf[node].a), prm.beta2f)
+                              : open_test64(qx, qy, qz, r->P[0], r->P[1], r->P[2], r->maxP2,
+                                            prm.beta2d);
         const double dx = qx - r->P[0], dy = qy - r->P[1], dz = qz - r->P[2];
         const double r2 = dx * dx + dy * dy + dz * dz;
         if (!near) {
@@ -374,7 +394,10 @@ __device__ inline double walk_fp64_lane(const EvalParams& prm, double qx, double
       ++node;
       continue;
     }
-    bool near = open_test64(qx, qy, qz, r->P[0], r->P[1], r->P[2], r->maxP2, prm.beta2d);
+    bool near = prm.ref32 ? ref_open32((float)qx, (float)qy, (float)qz, __ldg(&prm.nf[node].a),
+                                       prm.beta2f)
+                          : open_test64(qx, qy, qz, r->P[0], r->P[1], r->P[2], r->maxP2,
+                                        prm.beta2d);
     const double dx = qx - r->P[0], dy = qy - r->P[1], dz = qz - r->P[2];
     const double r2 = dx * dx + dy * dy + dz * dz;
     if (!near) {

@@ -5,9 +5,10 @@
 # Runs only where the reference tree exists; outputs never enter git history.
 # Test infrastructure only (pinning + golden-fixture generation).
 set -euo pipefail
-REF="${GWN_REFERENCE_ROOT:-/root/reference}"
+# The libigl source tree is named by GWN_REFERENCE_ROOT (no default).
+REF="${GWN_REFERENCE_ROOT:-}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
-if [ ! -f "$REF/include/igl/FastWindingNumberForSoups.h" ]; then
+if [ -z "$REF" ] || [ ! -f "$REF/include/igl/FastWindingNumberForSoups.h" ]; then
   echo "reference tree not present at $REF; skipping oracle/_ref" >&2
   exit 0
 fi

@@ -76,6 +76,8 @@ def lib():
             L.oracle_soup_free.argtypes = [p]
             L.oracle_soup_nodes.argtypes = [p]
             L.oracle_soup_nodes.restype = i64
+            L.oracle_soup_tree.argtypes = [p, p]
+            L.oracle_soup_tree.restype = i64
         if hasattr(L, "oracle_soup_tree_eval"):
             L.oracle_soup_tree_moments.argtypes = [p, p, p, i64, p, p]
             L.oracle_soup_tree_moments_flat.argtypes = [p, p, p, i64, p, p]
@@ -248,6 +250,13 @@ class SoupPort:
     def nodes(self) -> int:
         return lib().oracle_soup_nodes(self._h)
 
+    def tree(self) -> np.ndarray:
+        """The 4-wide tree, #nodes x 4 uint32 in the reference's encoding."""
+        n = lib().oracle_soup_tree(self._h, None)
+        out = np.empty((n, 4), np.uint32)
+        lib().oracle_soup_tree(self._h, _ptr(out))
+        return out
+
     def __del__(self):
         if getattr(self, "_h", None):
             lib().oracle_soup_free(self._h)
@@ -270,6 +279,8 @@ def ref_lib():
         L.ref_soup_build.restype = p
         L.ref_soup_eval.argtypes = [p, C.c_float, p, C.c_int64, p]
         L.ref_soup_free.argtypes = [p]
+        L.ref_soup_tree.argtypes = [p, p]
+        L.ref_soup_tree.restype = C.c_int64
         _ref = L
     return _ref
 
@@ -288,6 +299,13 @@ class RefSoup:
         W = np.empty(Q.shape[0], np.float64)
         ref_lib().ref_soup_eval(self._h, float(accuracy_scale), _ptr(Q), Q.shape[0], _ptr(W))
         return W
+
+    def tree(self) -> np.ndarray:
+        """The reference's own UT_BVH<4> nodes, #nodes x 4 uint32."""
+        n = ref_lib().ref_soup_tree(self._h, None)
+        out = np.empty((n, 4), np.uint32)
+        ref_lib().ref_soup_tree(self._h, _ptr(out))
+        return out
 
     def __del__(self):
         if getattr(self, "_h", None):

@@ -9,7 +9,11 @@
 // F copied to float / row-major int, init(order)) and :421-437 (evaluate:
 // query cast to float, computeSolidAngle(q, accuracy_scale) / (4 pi), in
 // igl::parallel_for(..., 1000)).
+// The tree lives in a private member of UT_SolidAngle; this test-only
+// wrapper opens it up to export the reference's own node array.
+#define private public
 #include <igl/FastWindingNumberForSoups.h>
+#undef private
 #include <igl/parallel_for.h>
 
 #include <cstdint>
@@ -49,6 +53,21 @@ void ref_soup_eval(void* h, float accuracy_scale, const double* Q, int64_t nQ, d
         W[p] = s->sa.computeSolidAngle(q, accuracy_scale) / (4.0 * 3.1415926535897932384626433832795);
       },
       1000);
+}
+
+// The reference's UT_BVH<4> nodes: returns the node count and, when `child`
+// is non-null, writes 4 entries per node (an item index, node | 2^31 for an
+// internal child, or ~0 for an empty lane), in the reference's node order.
+int64_t ref_soup_tree(void* h, uint32_t* child) {
+  RefSoup* s = (RefSoup*)h;
+  const auto& tree = s->sa.myTree;
+  const int64_t n = (int64_t)tree.getNumNodes();
+  if (child) {
+    const auto* nodes = tree.getNodes();
+    for (int64_t i = 0; i < n; ++i)
+      for (int c = 0; c < 4; ++c) child[i * 4 + c] = (uint32_t)nodes[i].child[c];
+  }
+  return n;
 }
 
 void ref_soup_free(void* h) { delete (RefSoup*)h; }

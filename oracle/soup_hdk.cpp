@@ -755,6 +755,16 @@ void oracle_soup_eval(void* h, float accuracy_scale, const double* Q, int64_t nQ
 
 int64_t oracle_soup_nodes(void* h) { return (int64_t)((Soup*)h)->nodes.size(); }
 
+// The 4-wide tree: 4 entries per node in the reference's encoding (item
+// index, node | 2^31, ~0 for an empty lane); returns the node count.
+int64_t oracle_soup_tree(void* h, uint32_t* child) {
+  const Soup* s = (const Soup*)h;
+  if (child)
+    for (size_t i = 0; i < s->nodes.size(); ++i)
+      for (int c = 0; c < 4; ++c) child[i * 4 + c] = s->nodes[i].child[c];
+  return (int64_t)s->nodes.size();
+}
+
 void oracle_soup_free(void* h) { delete (Soup*)h; }
 
 }  // extern "C"

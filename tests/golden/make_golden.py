@@ -1,16 +1,20 @@
 """Generate the committed golden fixtures from the reference's own code.
 
-Run in a checkout that has the libigl reference tree (the reference soup code
-is compiled from it into oracle/_ref/ by oracle/build_ref.sh):
+Run where the libigl reference tree is available (the reference soup code is
+compiled from it into oracle/_ref/ by oracle/build_ref.sh):
 
-    python tests/golden/make_golden.py
+    GWN_REFERENCE_ROOT=<libigl source tree> python tests/golden/make_golden.py
 
 Writes tests/golden/soup_reference.npz: for a handful of seeded meshes
 (single triangle, four triangles, a deformed icosphere with holes, a random
 soup) and seeded query sets, the reference's UT_SolidAngle winding numbers
 (order 2, accuracy_scale 2, FP32 inside, exactly as
 include/igl/fast_winding_number.cpp:383-437 calls it) and the exact FP64
-winding numbers (brute-force oracle) for the same queries.
+winding numbers (brute-force oracle) for the same queries; and for every
+mesh the reference's own UT_BVH<4> node array (<name>/tree: 4 lanes per
+node, exported from the compiled reference), including three meshes chosen
+for their trees (ties on a grid, nodes of more than 1024 boxes, degenerate
+and repeated triangles).
 """
 import os
 import sys
@@ -53,6 +57,35 @@ def cases():
     return out
 
 
+def tree_cases():
+    """Meshes whose trees exercise every split of UT_BVH<4>: exact ties
+    (a flat grid), nodes of more than 1024 boxes (span splits and their
+    partitions), and degenerate boxes."""
+    rng = np.random.default_rng(4321)
+    out = {}
+    # deformed icosphere subdiv 5 with 1% of its faces deleted (20,275 tris)
+    V, F = synth.icosphere(5)
+    V = synth.sh_deform(V, rng)
+    F = synth.delete_random_faces(F, rng, 0.01)
+    out["sphere5_holes"] = (V, F.astype(np.int32))
+    # a flat 40 x 40 grid of squares (many equal centres)
+    g = np.stack(np.meshgrid(np.arange(41.0), np.arange(41.0), [0.0], indexing="ij"),
+                 -1).reshape(-1, 3)
+    F = []
+    for i in range(40):
+        for j in range(40):
+            a = i * 41 + j
+            F += [[a, a + 1, a + 41], [a + 1, a + 42, a + 41]]
+    out["grid40"] = (g, np.array(F, np.int32))
+    # a soup with repeated and zero-area triangles
+    V = rng.normal(size=(500, 3))
+    F = rng.integers(0, 500, size=(3000, 3))
+    F[::7] = F[::7, [0, 0, 1]]          # two equal corners: zero area
+    F[1::11] = F[0:-1:11][: len(F[1::11])]  # repeats of other triangles
+    out["degenerate_soup"] = (V, F.astype(np.int32))
+    return out
+
+
 def queries(V, F, rng, n=2000):
     lo, hi = V.min(0), V.max(0)
     c, h = (lo + hi) / 2, (hi - lo) / 2 * 1.5 + 1e-3
@@ -65,7 +98,8 @@ def queries(V, F, rng, n=2000):
 
 def main():
     if O.build_ref() is None:
-        raise SystemExit("reference tree not available: cannot build oracle/_ref")
+        raise SystemExit("reference tree not available (set GWN_REFERENCE_ROOT to the libigl "
+                         "source tree): cannot build oracle/_ref")
     rng = np.random.default_rng(99)
     arrays = {}
     for name, (V, F) in cases().items():
@@ -78,8 +112,20 @@ def main():
         arrays[f"{name}/Q"] = Q
         arrays[f"{name}/W_ref"] = Wref
         arrays[f"{name}/W_exact"] = Wex
+        arrays[f"{name}/tree"] = ref.tree()
         print(f"{name}: {F.shape[0]} tris, {Q.shape[0]} queries, "
               f"max|ref-exact| = {np.abs(Wref - Wex).max():.3e}")
+    # the reference's own trees (UT_BVH<4> node arrays) and values on meshes
+    # that reach every kind of split
+    for name, (V, F) in tree_cases().items():
+        Q = queries(V, F, rng, n=4000)
+        ref = O.RefSoup(V, F, order=2)
+        arrays[f"{name}/V"] = V
+        arrays[f"{name}/F"] = F
+        arrays[f"{name}/Q"] = Q
+        arrays[f"{name}/W_ref"] = ref.eval(Q, 2.0)
+        arrays[f"{name}/tree"] = ref.tree()
+        print(f"{name}: {F.shape[0]} tris, {ref.tree().shape[0]} nodes")
     np.savez_compressed(os.path.join(HERE, "soup_reference.npz"), **arrays)
 
 

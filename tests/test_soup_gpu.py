@@ -1,4 +1,6 @@
-"""GPU parity of the triangle-soup fast winding number.
+"""GPU parity of the triangle-soup fast winding number over the binned binary
+tree (tree="binned"; the reference's own 4-wide tree is covered by
+tests/test_soup_ref_gpu.py).
 
 Checks, through the C ABI:
   * the tree's stored FP64 moments equal the HDK moments recomputed on the CPU
@@ -47,7 +49,7 @@ def mesh(cuda):
 def test_tree_moments_match_flat_recomputation(mesh):
     V, F, _ = mesh
     Vs, Fs = V, F[:3000]
-    bvh = G.FastWindingNumberBVH(Vs, Fs, order=2)
+    bvh = G.FastWindingNumberBVH(Vs, Fs, order=2, tree="binned")
     nodes, links, tri = bvh.export()
     assert sorted(tri.tolist()) == list(range(Fs.shape[0]))
     ref = O.soup_tree_moments(Vs, Fs, nodes, tri)
@@ -72,16 +74,17 @@ def test_tree_moments_match_flat_recomputation(mesh):
 
 def test_fp64_walk_matches_cpu_walk(mesh):
     V, F, Q = mesh
-    bvh = G.FastWindingNumberBVH(V, F, order=2)
+    bvh = G.FastWindingNumberBVH(V, F, order=2, tree="binned")
     nodes, links, tri = bvh.export()
     W64 = bvh.eval(Q, 2.0, precision="fp64")
     Wcpu = O.soup_tree_eval(V, F, nodes, tri, Q, 2.0, order=2)
     assert np.abs(W64 - Wcpu).max() < 1e-11
 
 
-def test_mixed_within_metric_of_fp64(mesh):
+@pytest.mark.parametrize("tree", ["binned", "reference"])
+def test_mixed_within_metric_of_fp64(mesh, tree):
     V, F, Q = mesh
-    bvh = G.FastWindingNumberBVH(V, F, order=2)
+    bvh = G.FastWindingNumberBVH(V, F, order=2, tree=tree)
     for qdt in (np.float64, np.float32):
         Qd = Q.astype(qdt)
         W64 = bvh.eval(Qd, 2.0, precision="fp64", out_dtype=np.float64)
@@ -97,7 +100,7 @@ def test_against_exact_and_orders(mesh):
     Qs = Q[:3000]
     Wex = O.winding_number(V, F, Qs)
     for order, tol in ((2, 1e-2), (1, 2e-1), (0, 5e-1)):
-        bvh = G.FastWindingNumberBVH(V, F, order=order)
+        bvh = G.FastWindingNumberBVH(V, F, order=order, tree="binned")
         W = bvh.eval(Qs, 2.0, precision="fp64")
         assert np.abs(W - Wex).max() < tol, (order, np.abs(W - Wex).max())
         nodes, links, tri = bvh.export()
@@ -107,8 +110,10 @@ def test_against_exact_and_orders(mesh):
 
 def test_against_reference_fixtures(cuda):
     for name, c in golden().items():
+        if "W_exact" not in c:
+            continue
         V, F, Q, Wref, Wex = c["V"], c["F"], c["Q"], c["W_ref"], c["W_exact"]
-        bvh = G.FastWindingNumberBVH(V, F, order=2)
+        bvh = G.FastWindingNumberBVH(V, F, order=2, tree="binned")
         W = bvh.eval(Q, 2.0, precision="mixed")
         ref_err = np.abs(Wref - Wex).max()
         if name == "one_tri":
@@ -134,6 +139,13 @@ def test_edge_cases(cuda):
     F = np.array([[0, 1, 3], [0, 2, 1], [0, 3, 2], [1, 2, 3], [4, 1, 2]], np.int32)
     Q = np.array([[0.1, 0.1, 0.1], [2, 2, 2], [0, 0, 0]])
     # a triangle with a NaN vertex is excluded from the tree (FWNFS.h:4606-4615)
+    for tree in ("binned", "reference"):
+        b = G.FastWindingNumberBVH(V, F, tree=tree)
+        assert b.stats["num_triangles"] == 4
+        Wt = b.eval(Q, 2.0, precision="mixed")
+        assert abs(Wt[0] - 1) < 1e-5 and abs(Wt[1]) < 1e-5 and np.isfinite(Wt[2])
+        with pytest.raises(G.GwnError):
+            G.FastWindingNumberBVH(V, np.array([[0, 1, 9]], np.int32), tree=tree)
     bvh = G.FastWindingNumberBVH(V, F)
     assert bvh.stats["num_triangles"] == 4
     W = bvh.eval(Q, 2.0, precision="mixed")
@@ -165,7 +177,7 @@ def test_device_tensors_and_repeatability(mesh, cuda):
 
 
 def _check_tree(V, F, Q):
-    bvh = G.FastWindingNumberBVH(V, F, order=2)
+    bvh = G.FastWindingNumberBVH(V, F, order=2, tree="binned")
     nodes, links, tri = bvh.export()
     n = F.shape[0]
     assert sorted(tri.tolist()) == list(range(n))

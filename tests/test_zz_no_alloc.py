@@ -76,3 +76,49 @@ def test_noalloc_rejects_more_than_the_static_capacity(cuda):
                                       W.data_ptr(), None, None)
     assert rc == 1  # GWN_ERR_INVALID_ARGUMENT
     assert b"65536" in L.gwn_last_error()
+
+
+def _noalloc_raw(torch, V, F, Q, status):
+    """One call with device buffers; `status` is a device int32 tensor or None."""
+    L = N.load()
+    dV = torch.from_numpy(np.ascontiguousarray(V, np.float64)).cuda()
+    dF = torch.from_numpy(np.ascontiguousarray(F, np.int32)).cuda()
+    dQ = torch.from_numpy(np.ascontiguousarray(Q, np.float64)).cuda()
+    dW = torch.zeros((Q.shape[0],), dtype=torch.float64, device="cuda")
+    N.check(L.gwn_winding_number_noalloc(
+        C.c_void_p(dV.data_ptr()), V.shape[0], C.c_void_p(dF.data_ptr()), F.shape[0],
+        C.c_void_p(dQ.data_ptr()), Q.shape[0], C.c_void_p(dW.data_ptr()),
+        C.c_void_p(status.data_ptr()) if status is not None else None,
+        C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    torch.cuda.synchronize()
+    return dW.cpu().numpy()
+
+
+def test_noalloc_reports_device_failures_with_and_without_a_status_word(cuda):
+    """A triangle index outside V is reported in the caller's status word, or,
+    when the caller passes none, in the library's static word that
+    gwn_device_status reads; so is a bulk-copy wait that runs out (made to run
+    out on purpose through gwn_debug_fail_next_waits).  Afterwards the entry
+    point still matches the allocating path."""
+    torch = cuda
+    L = N.load()
+    G.device_status(clear=True)
+    V, F, Q = synth.exact_workload(seed=8, subdiv=2, nq=1000)
+    Fbad = F.copy()
+    Fbad[7, 1] = V.shape[0] + 5  # built on the host: one index past the end of V
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    _noalloc_raw(torch, V, Fbad, Q, st)
+    assert int(st.item()) & 2  # GWN_STATUS_BAD_INPUT
+    assert G.device_status(clear=True) == 0  # nothing leaked into the sticky words
+    _noalloc_raw(torch, V, Fbad, Q, None)
+    assert G.device_status(clear=True) & 2
+    try:
+        L.gwn_debug_fail_next_waits(1)
+        _noalloc_raw(torch, V, F, Q, None)
+    finally:
+        L.gwn_debug_fail_next_waits(0)
+    assert G.device_status(clear=True) & 1  # GWN_STATUS_WAIT_TIMEOUT
+    assert G.device_status(clear=True) == 0
+    W = _noalloc_raw(torch, V, F, Q, None)
+    assert G.device_status(clear=True) == 0
+    assert np.abs(W - G.winding_number(V, F, Q, precision="mixed")).max() <= TOL
