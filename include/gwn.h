@@ -95,9 +95,10 @@ int gwn_debug_fail_next_waits(int n);
  * dim = 3: V is nV x 3, F is nF x 3 (triangles), O is nO x 3.
  * dim = 2: V is nV x 2, F is nF x 2 (edges),     O is nO x 2.
  * W (nO) receives sum over elements of solid angle / 4pi (or angle / 2pi).
- * GWN_MIXED with dim = 3, float64 O and W, at least 4096 triangles and 1024
- * queries evaluates through the cap hierarchy of gwn_wn_aabb (same value up
- * to rounding, built for the call); otherwise every pair is summed.
+ * With dim = 3, at least 4096 triangles and 1024 queries, both precisions
+ * evaluate through the cap hierarchy of gwn_wn_aabb (the reference's own
+ * algorithm, winding_number.cpp:40-53; same value up to rounding, built for
+ * the call); otherwise every pair is summed.
  * ---------------------------------------------------------------------- */
 int gwn_winding_number(const double* V, int64_t nV, int dim, const int32_t* F, int64_t nF,
                        const void* O, int o_dtype, int64_t nO, void* W, int w_dtype,
@@ -313,6 +314,11 @@ int gwn_wn_aabb_build(const double* V, int64_t nV, const int32_t* F, int64_t nF,
                       void* stream, gwn_wn_aabb** out);
 int gwn_wn_aabb_eval(const gwn_wn_aabb* tree, const double* Q, int64_t nQ, double* W, int mem,
                      void* stream);
+/* The same with a precision: GWN_PLAIN_FP64 walks as the reference does
+ * (a node's cap for a point strictly outside the node's box, every term
+ * in FP64); GWN_MIXED as gwn_wn_aabb_eval. */
+int gwn_wn_aabb_eval_precision(const gwn_wn_aabb* tree, const double* Q, int64_t nQ, double* W,
+                               int precision, int mem, void* stream);
 void gwn_wn_aabb_free(gwn_wn_aabb* tree);
 
 /* ------------------------------------------------------------------------

@@ -4,8 +4,10 @@
 //
 // set_mesh / grow / winding_number(p) as in the reference (the tree is built
 // by grow(), or at the first evaluation), plus a batched
-// winding_number(Q, W).  Evaluation is mixed precision (see gwn.h); the value
-// is the exact winding number's up to rounding.  The reference's split
+// winding_number(Q, W).  Evaluation is plain FP64 as in the reference (the
+// same walk: a node's cap for a point outside its box); define
+// IGL_GB300_WINDING_MIXED for the mixed FP32/FP64 walk (see gwn.h).  The
+// value is the exact winding number's up to rounding.  The reference's split
 // methods and approximate WindingNumberMethod modes are not provided.
 #ifndef IGL_WINDINGNUMBERAABB_H
 #define IGL_WINDINGNUMBERAABB_H
@@ -13,6 +15,14 @@
 #include <vector>
 
 #include "gwn_dropin_detail.h"
+
+#ifndef IGL_GB300_WINDING_PRECISION
+#  ifdef IGL_GB300_WINDING_MIXED
+#    define IGL_GB300_WINDING_PRECISION GWN_MIXED
+#  else
+#    define IGL_GB300_WINDING_PRECISION GWN_PLAIN_FP64
+#  endif
+#endif
 
 namespace igl {
 
@@ -56,7 +66,8 @@ class WindingNumberAABB {
     grow();
     const double q[3] = {(double)p(0), (double)p(1), (double)p(2)};
     double w = 0;
-    gwn_detail::check(gwn_wn_aabb_eval(h_, q, 1, &w, GWN_HOST, nullptr));
+    gwn_detail::check(
+        gwn_wn_aabb_eval_precision(h_, q, 1, &w, IGL_GB300_WINDING_PRECISION, GWN_HOST, nullptr));
     return (Scalar)w;
   }
   /// Winding numbers of the rows of Q (#Q x 3) into W.
@@ -66,7 +77,8 @@ class WindingNumberAABB {
     grow();
     const std::vector<double> q = gwn_detail::rows_f64(Q);
     std::vector<double> w((size_t)Q.rows());
-    gwn_detail::check(gwn_wn_aabb_eval(h_, q.data(), (int64_t)Q.rows(), w.data(), GWN_HOST, nullptr));
+    gwn_detail::check(gwn_wn_aabb_eval_precision(h_, q.data(), (int64_t)Q.rows(), w.data(),
+                                                 IGL_GB300_WINDING_PRECISION, GWN_HOST, nullptr));
     W.resize(Q.rows(), 1);
     for (Eigen::Index i = 0; i < Q.rows(); ++i) W(i) = (typename DerivedW::Scalar)w[(size_t)i];
   }

@@ -1,7 +1,9 @@
 // Drop-in replacement for include/igl/winding_number.h (libigl) running on the
 // GPU through libgwn's C ABI (gwn_winding_number).  Same signatures, same
-// argument meaning; the GPU sums every element's solid angle (the reference's
-// cap hierarchy returns the same sum up to rounding).
+// argument meaning; for 3-D meshes of at least 4096 triangles and 1024
+// points the GPU walks the reference's cap hierarchy (winding_number.cpp:
+// 40-53), otherwise it sums every element's solid angle (the same value up
+// to rounding).
 //
 // Precision: plain FP64, as the reference (set IGL_GB300_WINDING_MIXED to use
 // the mixed FP32/FP64 path).

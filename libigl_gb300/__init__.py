@@ -508,14 +508,17 @@ class WindingNumberAABB:
         N.check(N.load().gwn_wn_aabb_build(Va.ptr, Va.shape[0], Fa.ptr, Fa.shape[0], Va.mem,
                                            stream, C.byref(self._h)))
 
-    def winding_number(self, Q):
+    def winding_number(self, Q, precision="mixed"):
+        """W of every row of Q; ``precision`` "fp64" walks as the reference
+        does with every term in FP64, "mixed" takes FP32 terms away from the
+        surface (see gwn_wn_aabb_eval_precision)."""
         Qa = _Arg(Q, np.float64)
         if len(Qa.shape) != 2 or Qa.shape[1] != 3:
             raise ValueError("Q must be #Q x 3")
         W = _empty_like_mem(Qa.mem, (Qa.shape[0],), np.float64, like=Qa)
         stream = _stream_ptr() if Qa.mem == N.GWN_DEVICE else None
-        N.check(N.load().gwn_wn_aabb_eval(self._h, Qa.ptr, Qa.shape[0], _ptr_of(W), Qa.mem,
-                                          stream))
+        N.check(N.load().gwn_wn_aabb_eval_precision(self._h, Qa.ptr, Qa.shape[0], _ptr_of(W),
+                                                    _prec(precision), Qa.mem, stream))
         return W
 
     def close(self):

@@ -63,6 +63,7 @@ SIGNATURES = {
     "gwn_eytzinger_slots": ([_i64], _i64),
     "gwn_wn_aabb_build": ([_p, _i64, _p, _i64, _i, _p, _p], _i),
     "gwn_wn_aabb_eval": ([_p, _p, _i64, _p, _i, _p], _i),
+    "gwn_wn_aabb_eval_precision": ([_p, _p, _i64, _p, _i, _i, _p], _i),
     "gwn_wn_aabb_free": ([_p], None),
     "gwn_swept_volume_signed_distance": ([_p, _i64, _p, _i64, _p, _i64, _i, _p, _i64, _p, _d,
                                           _d, _p, _p, _i, _i, _p], _i),

@@ -465,17 +465,42 @@ __global__ void exact2_kernel(const double* __restrict__ V, int64_t nV,
   W[qi] = (WT)acc;
 }
 
+template <typename A, typename B>
+__global__ void convert_kernel(const A* __restrict__ in, B* __restrict__ out, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (B)in[i];
+}
+
 template <typename QT, typename WT>
 void launch_exact3(const ExactArgs& a, cudaStream_t st) {
-  // Large meshes in mixed precision: the cap hierarchy (hier.cu) gives the
-  // same value (within 4.1e-7 of the FP64 sum where the all-pairs mixed
-  // sweep reaches 3e-6) at a cost that grows far slower than #F.
-  if (a.precision == GWN_MIXED && std::is_same<QT, double>::value &&
-      std::is_same<WT, double>::value && a.nF >= kHierMinTriangles && a.nQ >= kHierMinQueries) {
+  // Large meshes: the cap hierarchy (hier.cu), the reference's own algorithm
+  // for winding_number (winding_number.cpp:40-53, WindingNumberTree.h:
+  // 261-336), gives the all-pairs value up to rounding at a cost that grows
+  // far slower than #F; in plain FP64 every term is FP64, in mixed precision
+  // the terms are FP32 with FP64 near terms and threshold re-evaluation
+  // (within 4.1e-7 of the FP64 sum where the all-pairs mixed sweep reaches
+  // 3e-6).  Float32 queries / results are widened / narrowed around it.
+  if (a.nF >= kHierMinTriangles && a.nQ >= kHierMinQueries) {
     DeviceStatus status(st, a.host_mode);
     HierTree h;
     hier_build(a.V, a.nV, a.F, a.nF, h, status.ptr(), st, true);
-    hier_eval(h, static_cast<const double*>(a.Q), a.nQ, static_cast<double*>(a.W), st);
+    const double* Qd = static_cast<const double*>(a.Q);
+    double* Wd = static_cast<double*>(a.W);
+    DevBuf<double> q64, w64;
+    if (!std::is_same<QT, double>::value) {
+      q64.alloc((size_t)a.nQ * 3, st);
+      launch_kernel(convert_kernel<QT, double>, (unsigned)((a.nQ * 3 + 255) / 256), 256, 0, st,
+                    static_cast<const QT*>(a.Q), q64.get(), a.nQ * 3);
+      Qd = q64.get();
+    }
+    if (!std::is_same<WT, double>::value) {
+      w64.alloc((size_t)a.nQ, st);
+      Wd = w64.get();
+    }
+    hier_eval(h, Qd, a.nQ, Wd, st, a.precision);
+    if (!std::is_same<WT, double>::value)
+      launch_kernel(convert_kernel<double, WT>, (unsigned)((a.nQ + 255) / 256), 256, 0, st,
+                    (const double*)w64.get(), static_cast<WT*>(a.W), a.nQ);
     status.check(st, "winding_number (hierarchy)");
     return;
   }

@@ -998,7 +998,13 @@ int gwn_wn_aabb_build(const double* V, int64_t nV, const int32_t* F, int64_t nF,
 
 int gwn_wn_aabb_eval(const gwn_wn_aabb* tree, const double* Q, int64_t nQ, double* W, int mem,
                      void* stream) {
+  return gwn_wn_aabb_eval_precision(tree, Q, nQ, W, GWN_MIXED, mem, stream);
+}
+
+int gwn_wn_aabb_eval_precision(const gwn_wn_aabb* tree, const double* Q, int64_t nQ, double* W,
+                               int precision, int mem, void* stream) {
   return guarded("gwn_wn_aabb_eval", [&] {
+    check_precision(precision);
     profile_begin_call();
     GWN_REQUIRE(tree != nullptr, "tree handle is null");
     GWN_REQUIRE(nQ >= 0, "nQ must be non-negative");
@@ -1011,7 +1017,7 @@ int gwn_wn_aabb_eval(const gwn_wn_aabb* tree, const double* Q, int64_t nQ, doubl
     cudaStream_t st = as_stream(stream);
     Staged<double> dQ(Q, (size_t)nQ * 3, mem, st);
     Staged<double> dW(W, (size_t)nQ, mem, st, false);
-    hier_eval(tree->tree, dQ.dev, nQ, dW.dev, st);
+    hier_eval(tree->tree, dQ.dev, nQ, dW.dev, st, precision);
     if (mem == GWN_HOST) {
       GWN_CUDA(cudaMemcpyAsync(W, dW.dev, (size_t)nQ * 8, cudaMemcpyDeviceToHost, st));
       GWN_CUDA(cudaStreamSynchronize(st));

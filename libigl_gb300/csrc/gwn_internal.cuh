@@ -88,6 +88,8 @@ struct HierTree {
   DevMem<float4> caps;    // 4 per cap triangle
   DevMem<float4> tris;    // 4 per leaf triangle
   DevMem<double> tris64;  // 9 per leaf triangle
+  DevMem<double> box64;   // 6 per node (pre-order): the node's FP64 box, lo then hi
+  DevMem<double> caps64;  // 9 per cap triangle (absolute FP64 corners)
 };
 // Out-of-range triangle indices set kStatusBadInput in *status.  With
 // per_call, the tree's memory is stream-ordered on `st` (a tree built and
@@ -95,8 +97,12 @@ struct HierTree {
 // ends with work still queued on `st`.
 void hier_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, HierTree& h,
                 unsigned* status, cudaStream_t st, bool per_call = false);
-// W of every query (FP64 device arrays), mixed precision, queued on `st`.
-void hier_eval(const HierTree& h, const double* Q, int64_t nQ, double* W, cudaStream_t st);
+// W of every query (FP64 device arrays), queued on `st`.  GWN_MIXED: FP32
+// caps and leaves with FP64 near terms and threshold re-evaluation;
+// GWN_PLAIN_FP64: the reference's walk (a node's cap for a point outside its
+// box, WindingNumberTree.h:261-336) with every term in FP64.
+void hier_eval(const HierTree& h, const double* Q, int64_t nQ, double* W, cudaStream_t st,
+               int precision = GWN_MIXED);
 
 // Eytzinger AABB tree of segments (eytzinger.cu); device pointers.
 int64_t eytzinger_slots(int64_t m);

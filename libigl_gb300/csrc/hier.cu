@@ -427,6 +427,8 @@ struct HierDev {
   const TriH* tris;      // leaf triangles by slot
   const double* tris64;  // leaf triangles by slot, 9 doubles
   int nnodes;
+  const double* box64;   // FP64 node boxes (pre-order), 6 doubles
+  const double* caps64;  // FP64 cap triangles, 9 doubles
 };
 
 __global__ void node_records_kernel(const double* __restrict__ box,
@@ -435,7 +437,7 @@ __global__ void node_records_kernel(const double* __restrict__ box,
                                     const uint32_t* __restrict__ cap_off,
                                     const uint32_t* __restrict__ cap_cnt, double cx, double cy,
                                     double cz, double eps, NodeH* __restrict__ nodes,
-                                    int32_t* __restrict__ capn) {
+                                    int32_t* __restrict__ capn, double* __restrict__ box64) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int nnodes = 2 * n - 1;
   if (x >= nnodes) return;
@@ -468,6 +470,7 @@ __global__ void node_records_kernel(const double* __restrict__ box,
   h.hi = make_float4(hi[0], hi[1], hi[2], __int_as_float(meta));
   nodes[p] = h;
   capn[p] = cn;
+  for (int k = 0; k < 6; ++k) box64[(int64_t)p * 6 + k] = box[(int64_t)x * 6 + k];
 }
 
 // Cap triangles of every node: for the records of node r (in node order,
@@ -483,7 +486,8 @@ __global__ void cap_tris_kernel(const double* __restrict__ V, const int32_t* __r
                                 int64_t nrec, const uint32_t* __restrict__ mult_off,
                                 const uint32_t* __restrict__ cap_off,
                                 const int32_t* __restrict__ first_rec, double cx, double cy,
-                                double cz, double eps, TriH* __restrict__ caps) {
+                                double cz, double eps, TriH* __restrict__ caps,
+                                double* __restrict__ caps64) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= nrec) return;
   const int32_t rec = order[i];
@@ -502,8 +506,14 @@ __global__ void cap_tris_kernel(const double* __restrict__ V, const int32_t* __r
   const bool degenerate = a == apex || b == apex;
   // a zero record adds atan2(0, >= 0) = 0
   const TriH t = degenerate ? zero_trih() : make_trih(p, eps, true);
+  double t64[9];
+  for (int s = 0; s < 3; ++s)
+    for (int d = 0; d < 3; ++d) t64[s * 3 + d] = degenerate ? 0.0 : V[(int64_t)vid[s] * 3 + d];
   const int reps = abs(net);
-  for (int r = 0; r < reps; ++r) caps[(int64_t)mult_off[i] + r] = t;
+  for (int r = 0; r < reps; ++r) {
+    caps[(int64_t)mult_off[i] + r] = t;
+    for (int k = 0; k < 9; ++k) caps64[((int64_t)mult_off[i] + r) * 9 + k] = t64[k];
+  }
   (void)cap_off;
 }
 
@@ -707,6 +717,84 @@ __global__ void __launch_bounds__(kT, 4) hier_walk_kernel(HierDev H, const QT* _
   if (fabs(w - 0.5) <= kBand) redo[atomicAdd(nredo, 1u)] = (int32_t)q;
 }
 
+// Plain FP64 walk, the reference's (WindingNumberTree.h:261-336): a node's
+// cap for a point strictly outside its FP64 box (the conservative test of
+// WindingNumberAABB.h:253-268) when the cap has fewer triangles than the
+// node, else its children; leaf and cap triangles in FP64 with the
+// reference's formula (solid_angle.cpp:16-54).  Same warp walk, subtree
+// split and partial sums as hier_walk_kernel.
+__global__ void __launch_bounds__(kT, 4) hier_walk64_kernel(HierDev H, const double* __restrict__ Q,
+                                                         int64_t nQ,
+                                                         const int32_t* __restrict__ perm,
+                                                         double* __restrict__ W,
+                                                         const int2* __restrict__ ranges,
+                                                         const int* __restrict__ nranges,
+                                                         double* __restrict__ part) {
+  int x0 = 0, x1 = H.nnodes;
+  if (ranges) {
+    if ((int)blockIdx.y >= *nranges) return;
+    const int2 rg = ranges[blockIdx.y];
+    x0 = rg.x;
+    x1 = rg.y;
+  }
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool valid = i < nQ;
+  const int64_t q = valid ? (perm ? perm[i] : i) : 0;
+  const double px = valid ? Q[q * 3] : 0.0, py = valid ? Q[q * 3 + 1] : 0.0,
+               pz = valid ? Q[q * 3 + 2] : 0.0;
+  auto outside = [&](int x) {
+    const double* b = H.box64 + (int64_t)x * 6;
+    return px < b[0] || px > b[3] || py < b[1] || py > b[4] || pz < b[2] || pz > b[5];
+  };
+  auto add_cap = [&](int meta, int cn, double& acc) {
+    for (int k = 0; k < cn; ++k) acc += tri64_term(H.caps64 + ((int64_t)meta + k) * 9, px, py, pz);
+  };
+  double acc = 0.0;
+  int resume = valid ? x0 : 0x7fffffff;
+  if (ranges && valid) {
+    // outside the root's box: the root's cap alone, in subtree 0
+    const int meta0 = __float_as_int(H.nodes[0].hi.w);
+    if (meta0 >= 0 && outside(0)) {
+      if (blockIdx.y == 0) add_cap(meta0, H.capn[0], acc);
+      resume = 0x7fffffff;
+    }
+  }
+  int x = x0;
+  while (x < x1) {
+    if (x >= resume) {
+      const NodeH nd = H.nodes[x];
+      const int meta = __float_as_int(nd.hi.w);
+      if (meta <= -2) {
+        acc += tri64_term(H.tris64 + (int64_t)(-2 - meta) * 9, px, py, pz);
+        resume = x + 1;
+      } else if (meta >= 0 && outside(x)) {
+        add_cap(meta, H.capn[x], acc);
+        resume = __float_as_int(nd.lo.w);
+      } else {
+        resume = x + 1;
+      }
+    }
+    x = __reduce_min_sync(0xffffffffu, resume);
+  }
+  if (!valid) return;
+  if (part) {
+    part[(int64_t)blockIdx.y * nQ + q] = acc;
+    return;
+  }
+  W[q] = acc * kInv2Pi;
+}
+
+// W from the subtrees' partial sums in a fixed order (plain FP64: no
+// re-evaluation list).
+__global__ void hier_sum64_kernel(const double* __restrict__ part, int S, int64_t nQ,
+                                  double* __restrict__ W) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= nQ) return;
+  double a = 0.0;
+  for (int y = 0; y < S; ++y) a += part[(int64_t)y * nQ + q];
+  W[q] = a * kInv2Pi;
+}
+
 // The top of the tree cut into at most S subtrees (breadth first; a leaf
 // above the cut stays whole): ranges of pre-order positions.  One thread.
 __global__ void frontier_kernel(const NodeH* __restrict__ nodes, int S, int2* __restrict__ ranges,
@@ -764,6 +852,8 @@ void hier_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, HierT
     h.caps.ordered(st);
     h.tris.ordered(st);
     h.tris64.ordered(st);
+    h.box64.ordered(st);
+    h.caps64.ordered(st);
   }
   h.V = V;
   h.nV = nV;
@@ -896,6 +986,8 @@ void hier_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, HierT
   h.caps.alloc((size_t)std::max<int64_t>(ncap, 1) * 4);
   h.tris.alloc((size_t)n * 4);
   h.tris64.alloc((size_t)n * 9);
+  h.box64.alloc((size_t)nn * 6);
+  h.caps64.alloc((size_t)std::max<int64_t>(ncap, 1) * 9);
   NodeH* nodes = reinterpret_cast<NodeH*>(h.nodes.get());
   TriH* caps = reinterpret_cast<TriH*>(h.caps.get());
   TriH* tris = reinterpret_cast<TriH*>(h.tris.get());
@@ -905,16 +997,17 @@ void hier_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, HierT
                   (const int32_t*)rnode.get(), (const int32_t*)rinc.get(),
                   (const int32_t*)rnet.get(), nrec, (const uint32_t*)mult.get(),
                   (const uint32_t*)cap_off.get(), (const int32_t*)first_rec.get(), h.c[0], h.c[1],
-                  h.c[2], h.eps, caps);
+                  h.c[2], h.eps, caps, h.caps64.get());
   launch_kernel(node_records_kernel, nblk(nn), kT, 0, st, (const double*)box.get(),
                 (const int32_t*)pre.get(), (const int32_t*)size.get(), n,
                 (const uint32_t*)cap_off.get(), (const uint32_t*)cap_cnt.get(), h.c[0], h.c[1],
-                h.c[2], h.eps, nodes, h.capn.get());
+                h.c[2], h.eps, nodes, h.capn.get(), h.box64.get());
   launch_kernel(leaf_tris_kernel, nblk(n), kT, 0, st, V, F, nV, (const int32_t*)sorted.get(), n,
                 h.c[0], h.c[1], h.c[2], h.eps, tris, h.tris64.get());
 }
 
-void hier_eval(const HierTree& h, const double* Q, int64_t nQ, double* W, cudaStream_t st) {
+void hier_eval(const HierTree& h, const double* Q, int64_t nQ, double* W, cudaStream_t st,
+               int precision) {
   if (nQ == 0) return;
   if (h.nF == 0) {
     GWN_CUDA(cudaMemsetAsync(W, 0, (size_t)nQ * 8, st));
@@ -928,13 +1021,32 @@ void hier_eval(const HierTree& h, const double* Q, int64_t nQ, double* W, cudaSt
   nredo.zero(st);
   const HierDev H{reinterpret_cast<const NodeH*>(h.nodes.get()), h.capn.get(),
                   reinterpret_cast<const TriH*>(h.caps.get()),
-                  reinterpret_cast<const TriH*>(h.tris.get()), h.tris64.get(), (int)h.nnodes};
+                  reinterpret_cast<const TriH*>(h.tris.get()), h.tris64.get(), (int)h.nnodes,
+                  h.box64.get(), h.caps64.get()};
   // Too few queries to fill the GPU: each warp of queries walks one of up to
   // 8 subtrees (blockIdx.y), and the partial sums are added in a fixed order.
   const int64_t warps = (nQ + 31) / 32;
   const int64_t want = 3 * (int64_t)num_sms() * 32;
   int S = 1;
   while (S < kMaxSplit && warps * S < want) S *= 2;
+  const int32_t* perm = qo.active ? qo.perm.get() : nullptr;
+  if (precision == GWN_PLAIN_FP64) {
+    PhaseTimer ph("hier_walk", st);
+    if (S == 1) {
+      launch_kernel(hier_walk64_kernel, nblk(nQ), kT, 0, st, H, Q, nQ, perm, W,
+                    (const int2*)nullptr, (const int*)nullptr, (double*)nullptr);
+    } else {
+      DevBuf<int2> ranges(kMaxSplit, st);
+      DevBuf<int> nranges(1, st);
+      DevBuf<double> part((size_t)S * nQ, st);
+      part.zero(st);
+      launch_kernel(frontier_kernel, 1, 1, 0, st, H.nodes, S, ranges.get(), nranges.get());
+      launch_kernel(hier_walk64_kernel, dim3(nblk(nQ), S), kT, 0, st, H, Q, nQ, perm, W,
+                    (const int2*)ranges.get(), (const int*)nranges.get(), part.get());
+      launch_kernel(hier_sum64_kernel, nblk(nQ), kT, 0, st, (const double*)part.get(), S, nQ, W);
+    }
+    return;
+  }
   {
     PhaseTimer ph("hier_walk", st);
     if (S == 1) {

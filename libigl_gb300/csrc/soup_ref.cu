@@ -170,6 +170,22 @@ struct RNode {
 };
 
 // --------------------------------------------------------------- boxes --
+// A triangle's box as UT_SolidAngle::init makes it: initBounds(v0), then
+// enlargeBounds(v1), enlargeBounds(v2) with SYSmin / SYSmax
+// (FWNFS.h:255-256, 4023-4028).  (a > b) ? b : a keeps a NaN of the first
+// vertex and drops one of a later vertex.
+template <typename T>
+__device__ __forceinline__ void tri_box(const T* a, const T* b, const T* c, T* lo, T* hi) {
+  for (int d = 0; d < 3; ++d) {
+    lo[d] = a[d];
+    hi[d] = a[d];
+    lo[d] = lo[d] > b[d] ? b[d] : lo[d];
+    hi[d] = hi[d] < b[d] ? b[d] : hi[d];
+    lo[d] = lo[d] > c[d] ? c[d] : lo[d];
+    hi[d] = hi[d] < c[d] ? c[d] : hi[d];
+  }
+}
+
 // Triangle boxes over float copies of the vertices (UT_SolidAngle::init,
 // FWNFS.h:6560-6590); a box with a non-finite bound is excluded
 // (FWNFS.h:4606-4615).  Triangles with an index outside V are reported and
@@ -192,12 +208,7 @@ __global__ void tri_box_kernel(const double* __restrict__ V, int64_t nV,
     for (int d = 0; d < 3; ++d) p[c][d] = (float)V[(int64_t)i * 3 + d];
   }
   Box b;
-  for (int a = 0; a < 3; ++a) b.lo[a] = b.hi[a] = p[0][a];
-  for (int c = 1; c < 3; ++c)
-    for (int a = 0; a < 3; ++a) {
-      b.lo[a] = b.lo[a] < p[c][a] ? b.lo[a] : p[c][a];
-      b.hi[a] = b.hi[a] > p[c][a] ? b.hi[a] : p[c][a];
-    }
+  tri_box(p[0], p[1], p[2], b.lo, b.hi);
   for (int a = 0; a < 3; ++a)
     if (!isfinite(b.lo[a]) || !isfinite(b.hi[a])) ok = false;
   box[f] = b;
@@ -1155,16 +1166,7 @@ __device__ void tri_integrals(const T* A, const T* B, const T* C, const T* P, T*
 template <typename T>
 __device__ void item_loc(const T* a, const T* b, const T* c, int order, Loc<T>& L) {
   zero_loc(L);
-  for (int d = 0; d < 3; ++d) {
-    L.lo[d] = a[d];
-    L.hi[d] = a[d];
-  }
-  for (int d = 0; d < 3; ++d) {
-    L.lo[d] = L.lo[d] < b[d] ? L.lo[d] : b[d];
-    L.hi[d] = L.hi[d] > b[d] ? L.hi[d] : b[d];
-    L.lo[d] = L.lo[d] < c[d] ? L.lo[d] : c[d];
-    L.hi[d] = L.hi[d] > c[d] ? L.hi[d] : c[d];
-  }
+  tri_box(a, b, c, L.lo, L.hi);
   T ab[3], ac[3];
   for (int d = 0; d < 3; ++d) {
     ab[d] = b[d] - a[d];
@@ -1411,6 +1413,7 @@ __global__ void moments_kernel(const RNode* __restrict__ nodes, uint32_t lb, uin
                                const double* __restrict__ V, int64_t nV,
                                const int32_t* __restrict__ F, int order,
                                const uint32_t* __restrict__ nslots,
+                               const uint32_t* __restrict__ nitems,
                                const uint32_t* __restrict__ slot,
                                const uint32_t* __restrict__ ibase, Loc<float>* __restrict__ L32,
                                Loc<double>* __restrict__ L64, SoupNodeF* __restrict__ nf,
@@ -1433,6 +1436,7 @@ __global__ void moments_kernel(const RNode* __restrict__ nodes, uint32_t lb, uin
       link = (long long)sp + nslots[y];
       write_records(c32[nch], c64[nch], link, nf + sp, nd + sp);
       sp += nslots[y];
+      ib += nitems[y];
     } else {
       double v[9];
       load_tri(V, nV, F, c, v);
@@ -1650,9 +1654,9 @@ void soup_build_ref(gwn_soup_impl& s, const double* V, int64_t nV, const int32_t
   LargeRunner large{st,        nodes.get(), idx.get(),  tmp.get(),
                     tapeE.get(), tapeG.get(), preL.get(), preE.get(),
                     cls.get(),  tb.get(),    status.ptr()};
-  std::vector<uint32_t> level = {0, 1};
+  std::vector<uint32_t> level = {0, 1};  // depth d holds nodes [level[d], level[d + 1])
   uint32_t lb = 0, le = 1;
-  while (lb < le) {
+  while (true) {
     const uint32_t nl = le - lb;
     for (int round = 0; round < 3; ++round) {
       counts.zero(st);
@@ -1681,9 +1685,9 @@ void soup_build_ref(gwn_soup_impl& s, const double* V, int64_t nV, const int32_t
     GWN_CUDA(cudaStreamSynchronize(st));
     const uint32_t added = lastc[0] + lastc[1];
     GWN_REQUIRE((size_t)le + added <= cap, "soup_build: tree larger than its bound");
-    if (added)
-      launch_kernel(make_children_kernel, blocks_for(nl), 256, 0, st, nodes.get(), lb, le,
-                    (const uint32_t*)coffs.get());
+    if (added == 0) break;
+    launch_kernel(make_children_kernel, blocks_for(nl), 256, 0, st, nodes.get(), lb, le,
+                  (const uint32_t*)coffs.get());
     lb = le;
     le += added;
     level.push_back(le);
@@ -1725,8 +1729,9 @@ void soup_build_ref(gwn_soup_impl& s, const double* V, int64_t nV, const int32_t
     for (int d = depth - 1; d >= 0; --d)
       launch_kernel(moments_kernel, blocks_for(level[d + 1] - level[d], 128), 128, 0, st,
                     (const RNode*)nodes.get(), level[d], level[d + 1], V, nV, F, order,
-                    (const uint32_t*)nslots.get(), (const uint32_t*)slot.get(),
-                    (const uint32_t*)ibase.get(), L32.get(), L64.get(), s.nf.get(), s.nd.get(),
+                    (const uint32_t*)nslots.get(), (const uint32_t*)nitems.get(),
+                    (const uint32_t*)slot.get(), (const uint32_t*)ibase.get(), L32.get(),
+                    L64.get(), s.nf.get(), s.nd.get(),
                     s.tf.get(), s.td.get(), s.tri_index.get());
     launch_kernel(export_tree_kernel, blocks_for(nn), 256, 0, st, (const RNode*)nodes.get(), nn,
                   (const uint32_t*)pre.get(), s.ref_child.get());

@@ -173,6 +173,12 @@ __device__ __forceinline__ double solid_angle_vos64(const double* __restrict__ t
   const double lb2 = bx * bx + by * by + bz * bz;
   const double lc2 = cx * cx + cy * cy + cz * cz;
   if (la2 == 0.0 || lb2 == 0.0 || lc2 == 0.0) return 0.0;
+  // two coinciding corners: the normalised form's u = b - a (or v, or
+  // u x v) is exactly zero there, so its term is 0 (FWNFS.h:6097-6101)
+  if ((t[0] == t[3] && t[1] == t[4] && t[2] == t[5]) ||
+      (t[0] == t[6] && t[1] == t[7] && t[2] == t[8]) ||
+      (t[3] == t[6] && t[4] == t[7] && t[5] == t[8]))
+    return 0.0;
   const double det = ax * (by * cz - bz * cy) + ay * (bz * cx - bx * cz) + az * (bx * cy - by * cx);
   if (det == 0.0) return 0.0;
   const double la = sqrt(la2), lb = sqrt(lb2), lc = sqrt(lc2);

@@ -589,11 +589,14 @@ struct Soup {
       Box& b = tri_boxes[(size_t)t];
       const float* p0 = vtx(F[t * 3]);
       for (int a = 0; a < 3; ++a) b.lo[a] = b.hi[a] = p0[a];
+      // enlargeBounds with SYSmin / SYSmax (FWNFS.h:255-256, 4023-4028):
+      // (a > b) ? b : a keeps a NaN of the first vertex and drops one of a
+      // later vertex, so only a non-finite first vertex excludes the box
       for (int c = 1; c < 3; ++c) {
         const float* p = vtx(F[t * 3 + c]);
         for (int a = 0; a < 3; ++a) {
-          b.lo[a] = b.lo[a] < p[a] ? b.lo[a] : p[a];
-          b.hi[a] = b.hi[a] > p[a] ? b.hi[a] : p[a];
+          b.lo[a] = b.lo[a] > p[a] ? p[a] : b.lo[a];
+          b.hi[a] = b.hi[a] < p[a] ? p[a] : b.hi[a];
         }
       }
     }

@@ -90,8 +90,12 @@ def queries(V, F, rng, n=2000):
     lo, hi = V.min(0), V.max(0)
     c, h = (lo + hi) / 2, (hi - lo) / 2 * 1.5 + 1e-3
     far = c + rng.uniform(-1, 1, size=(n // 2, 3)) * h
-    P, f = synth.sample_on_faces(V, F, rng, n - n // 2)
-    nrm = synth.face_normals(V, F[f])
+    # near-surface queries on faces of non-zero area: a point on a zero-area
+    # triangle lies exactly on the surface, where W is not defined
+    area = np.linalg.norm(np.cross(V[F[:, 1]] - V[F[:, 0]], V[F[:, 2]] - V[F[:, 0]]), axis=1)
+    Fs = F[area > 0]
+    P, f = synth.sample_on_faces(V, Fs, rng, n - n // 2)
+    nrm = synth.face_normals(V, Fs[f])
     d = 10.0 ** rng.uniform(-4, -1, size=P.shape[0]) * rng.choice([-1.0, 1.0], P.shape[0])
     return np.concatenate([far, P + nrm * d[:, None]])
 

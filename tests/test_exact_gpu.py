@@ -75,13 +75,24 @@ def test_exact_edge_cases(cuda):
     # empty mesh -> W = 0
     W = G.winding_number(V, np.zeros((0, 3), np.int32), np.array([[0.1, 0.1, 0.1]]))
     assert np.all(W == 0)
-    # query on a vertex / on a face: finite, reference-consistent
-    Q = np.array([[0, 0, 0], [0.25, 0.25, 0], [0.1, 0.1, 0.1], [0.5, 0.5, 0.5]])
+    # queries on a vertex and on a face, against the oracle.  On a vertex
+    # the incident triangles' terms are atan2(+-0, +0) = 0 in the reference's
+    # formula (no zero guards, solid_angle.cpp:21-54) and here alike, so the
+    # values agree to rounding.  On a face the triangle's determinant is
+    # zero up to rounding and its term is +-pi by the sign of that rounding:
+    # the reference's own value depends on its compiler's contraction of
+    # multiply-adds, so only W modulo 1/2 is defined there.
+    Q = np.array([[0, 0, 0], [1, 0, 0], [0, 0, 1], [0.25, 0.25, 0], [0.2, 0, 0.3],
+                  [0.1, 0.1, 0.1], [0.5, 0.5, 0.5]])
     Wref = O.winding_number(V, F, Q)
-    for prec in ("fp64", "mixed"):
+    on_vertex, on_face = slice(0, 3), slice(3, 5)
+    for prec, tol in (("fp64", 1e-12), ("mixed", 1e-6)):  # mixed: far faces in FP32
         W = G.winding_number(V, F, Q, precision=prec)
         assert np.all(np.isfinite(W))
-        assert np.abs(W[2:] - Wref[2:]).max() < 1e-6
+        assert np.abs(W[on_vertex] - Wref[on_vertex]).max() < tol
+        d = (W[on_face] - Wref[on_face]) * 2.0
+        assert np.abs(d - np.round(d)).max() < 2 * tol
+        assert np.abs(W[5:] - Wref[5:]).max() < 1e-6
     # out-of-range index -> GWN_ERR_INVALID_ARGUMENT, loudly
     with pytest.raises(G.GwnError):
         G.winding_number(V, np.array([[0, 1, 7]], np.int32), Q)
@@ -95,6 +106,22 @@ def test_exact_2d_edges(cuda):
     W = G.winding_number(V, E, Q, precision="fp64")
     Wref = O.winding_number(V, E, Q)
     assert np.abs(W - Wref).max() < 1e-12
+    # signed_angle (signed_angle.cpp:14-45) over a star polygon with 400
+    # edges, a self-overlapping loop and an open polyline, 4000 queries
+    rng = np.random.default_rng(12)
+    t = np.sort(rng.uniform(0, 2 * np.pi, 400))
+    r = 1 + 0.4 * np.sin(7 * t) + 0.05 * rng.normal(size=400)
+    star = np.stack([r * np.cos(t), r * np.sin(t)], 1)
+    loop = 0.5 * np.stack([np.cos(2 * t[::4]), np.sin(2 * t[::4])], 1) + 0.2
+    Vs = np.concatenate([star, loop])
+    Es = np.concatenate([np.stack([np.arange(400), (np.arange(400) + 1) % 400], 1),
+                         400 + np.stack([np.arange(99), np.arange(1, 100)], 1)]).astype(np.int32)
+    Qs = rng.uniform(-1.6, 1.6, (4000, 2))
+    Wref = O.winding_number(Vs, Es, Qs)
+    W64 = G.winding_number(Vs, Es, Qs, precision="fp64")
+    assert np.abs(W64 - Wref).max() < 1e-12
+    Wm = G.winding_number(Vs, Es, Qs, precision="mixed")
+    assert np.abs(Wm - Wref).max() < TOL_MIXED
 
 
 def test_exact_device_tensors(cuda):

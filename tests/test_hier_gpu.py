@@ -98,3 +98,34 @@ def test_hier_bad_index_raises(cuda):
     F[3, 1] = V.shape[0] + 4
     with pytest.raises(G.GwnError):
         G.WindingNumberAABB(V, F)
+
+
+def test_fp64_hierarchy_matches_cpu_hierarchy_and_all_pairs(cuda):
+    """The plain-FP64 walk (the reference's: a node's cap for a point
+    strictly outside its box, every term in FP64) against the CPU
+    restatement of the reference hierarchy (oracle/wn_hier.cpp) and the FP64
+    all-pairs sum: rounding only.  Uniform queries 1e-11; queries down to
+    1e-6 x the diagonal from the surface, where a triangle term itself loses
+    digits (the GPU fuses multiply-adds, the CPU does not), 1e-9."""
+    for name, (V, F) in _meshes().items():
+        h = G.WindingNumberAABB(V, F)
+        for near, tol in ((False, 1e-11), (True, 1e-9)):
+            Q = _queries(V, 1000, 67, near=near)
+            W64 = h.winding_number(Q, precision="fp64")
+            Wr = O.winding_number_hier(V, F, Q)
+            Wa = O.winding_number(V, F, Q)
+            assert np.abs(W64 - Wr).max() <= tol, (name, near, np.abs(W64 - Wr).max())
+            assert np.abs(W64 - Wa).max() <= tol, (name, near, np.abs(W64 - Wa).max())
+    # gwn_winding_number in plain FP64 takes the hierarchy from 4096 triangles
+    # and 1024 queries, with float64 or float32 queries and results
+    V, F = _meshes()["holes"]
+    Q = _queries(V, 2000, 68, near=False)
+    W = G.winding_number(V, F, Q, precision="fp64")
+    assert np.abs(W - O.winding_number(V, F, Q)).max() <= 1e-11
+    Q32 = Q.astype(np.float32)
+    W32 = G.winding_number(V, F, Q32, precision="fp64")
+    assert W32.dtype == np.float32
+    ref = O.winding_number(V, F, Q32.astype(np.float64))
+    assert np.abs(W32.astype(np.float64) - ref).max() <= 1e-6
+    Wm32 = G.winding_number(V, F, Q32, precision="mixed")
+    assert np.abs(Wm32.astype(np.float64) - ref).max() <= 1e-4

@@ -110,8 +110,12 @@ def test_lru_eviction_under_a_small_budget(cuda):
     import libigl_gb300 as G
     meshes = _meshes(4, seed=13)
     sizes = [F.shape[0] for _, F in meshes]
-    # room for about two of the largest trees
-    budget = int(2.2 * max(sizes) * 720)
+    # room for about two of the largest trees (as built by the server: the
+    # default tree of FastWindingNumberBVH)
+    Vb, Fb = meshes[int(np.argmax(sizes))]
+    big = G.FastWindingNumberBVH(Vb, Fb, 2)
+    budget = int(2.2 * big.stats["device_bytes"])
+    big.close()
     with G.Server(hbm_budget_bytes=budget, max_batch_queries=1 << 16, slots=2) as S:
         ids = [S.add_mesh(V, F) for V, F in meshes]
         refs = []

@@ -143,13 +143,16 @@ def test_edge_cases(cuda):
         b = G.FastWindingNumberBVH(V, F, tree=tree)
         assert b.stats["num_triangles"] == 4
         Wt = b.eval(Q, 2.0, precision="mixed")
-        assert abs(Wt[0] - 1) < 1e-5 and abs(Wt[1]) < 1e-5 and np.isfinite(Wt[2])
+        # within the order-2 expansion's error at accuracy 2 of the exact 1 / 0
+        assert abs(Wt[0] - 1) < 1e-4 and abs(Wt[1]) < 1e-4 and np.isfinite(Wt[2])
+        if tree == "reference":  # and the reference's own values (its tree)
+            assert np.abs(Wt[:2] - O.SoupPort(V, F).eval(Q[:2], 2.0)).max() < 1e-6
         with pytest.raises(G.GwnError):
             G.FastWindingNumberBVH(V, np.array([[0, 1, 9]], np.int32), tree=tree)
     bvh = G.FastWindingNumberBVH(V, F)
     assert bvh.stats["num_triangles"] == 4
     W = bvh.eval(Q, 2.0, precision="mixed")
-    assert abs(W[0] - 1) < 1e-5 and abs(W[1]) < 1e-5 and np.isfinite(W[2])
+    assert abs(W[0] - 1) < 1e-4 and abs(W[1]) < 1e-4 and np.isfinite(W[2])
     # empty mesh and empty queries
     e = G.FastWindingNumberBVH(V, np.zeros((0, 3), np.int32))
     assert np.all(e.eval(Q) == 0)

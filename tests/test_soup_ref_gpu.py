@@ -32,10 +32,17 @@ from oracle import oracle as O
 pytestmark = pytest.mark.gpu
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-# The reference computes in FP32 on float copies of V and Q; the FP64 walk
-# over the same tree cut differs from it by that rounding only.
-TOL_FP64_VS_REF = 1e-4
+# The reference computes in FP32 on float copies of V and Q; over the same
+# tree cut the FP64 walk differs from it by that rounding only.  On surfaces
+# (spheres, the grid) that is below 1e-5.  Soups of random triangles have a
+# boundary edge near many queries, where W turns by dW ~ dx / (2 pi d): the
+# float rounding of V and Q (~1e-7) at d = 1e-4 moves the reference's own
+# value by up to ~2e-4, so there the bound is the reference's error.
+SOUPS = {"four_tris", "random_soup", "degenerate_soup"}
+TOL_FP64_VS_REF = 1e-5
+TOL_FP64_VS_REF_SOUP = 3e-4
 P99_FP64_VS_REF = 1e-6
+P99_FP64_VS_REF_SOUP = 1e-5
 TOL_MIXED = 1e-4
 
 
@@ -72,9 +79,14 @@ def test_values_match_the_reference(cuda):
         Wm = bvh.eval(Q, 2.0, precision="mixed")
         e64 = np.abs(W64 - Wref)
         em = np.abs(Wm - Wref)
-        assert e64.max() <= TOL_FP64_VS_REF, (name, e64.max())
-        assert np.quantile(e64, 0.99) <= P99_FP64_VS_REF, (name, np.quantile(e64, 0.99))
-        assert em.max() <= TOL_MIXED, (name, em.max())
+        soup = name in SOUPS
+        tol = TOL_FP64_VS_REF_SOUP if soup else TOL_FP64_VS_REF
+        p99 = P99_FP64_VS_REF_SOUP if soup else P99_FP64_VS_REF
+        assert e64.max() <= tol, (name, e64.max())
+        assert np.quantile(e64, 0.99) <= p99, (name, np.quantile(e64, 0.99))
+        assert em.max() <= max(TOL_MIXED, tol), (name, em.max())
+        # mixed and plain FP64 take the same tree cut: arithmetic only
+        assert np.abs(Wm - W64).max() <= TOL_MIXED, name
         out = np.abs(Wref - 0.5) > 1e-3
         assert np.array_equal((W64 > 0.5)[out], (Wref > 0.5)[out]), name
         assert np.array_equal((Wm > 0.5)[out], (Wref > 0.5)[out]), name
@@ -95,7 +107,7 @@ def test_lower_orders_follow_the_reference_algorithm(cuda, order):
     V, F, Q = c["V"], c["F"], c["Q"]
     ref = O.SoupPort(V, F, order=order).eval(Q, 2.0)
     W = G.FastWindingNumberBVH(V, F, order=order).eval(Q, 2.0, precision="fp64")
-    assert np.abs(W - ref).max() <= TOL_FP64_VS_REF
+    assert np.abs(W - ref).max() <= TOL_FP64_VS_REF_SOUP
 
 
 def test_small_and_degenerate_meshes(cuda):
@@ -107,7 +119,7 @@ def test_small_and_degenerate_meshes(cuda):
         bvh = G.FastWindingNumberBVH(V, F, order=2)
         assert np.array_equal(bvh.tree_nodes(), O.SoupPort(V, F).tree()), m
         W = bvh.eval(Q, 2.0, precision="fp64")
-        assert np.abs(W - O.SoupPort(V, F).eval(Q, 2.0)).max() <= TOL_FP64_VS_REF, m
+        assert np.abs(W - O.SoupPort(V, F).eval(Q, 2.0)).max() <= TOL_FP64_VS_REF_SOUP, m
     # every triangle excluded (non-finite) and an empty mesh: W = 0
     Vn = V.copy()
     Vn[:, 0] = np.nan
