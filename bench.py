@@ -9,12 +9,18 @@ overloads), the configuration the headline metric is quoted on:
   order 2, accuracy_scale (beta) 2.
 
 A step is one evaluation of all queries on the device (mixed precision:
-FP32 bulk, FP64 near-field / decision guard band / threshold re-evaluation).
-Reported: value = queries/s of the device-resident call; e2e = the same call
-through the C ABI with host (pinned) buffers, copies included; accuracy of
-the mixed result against the plain FP64 walk of the same tree; the plain FP64
-walk's own throughput; the dominant kernel's live CUDA-event duration and
-roofline; a CPU baseline on this host's cores.
+FP32 bulk, FP64 near-field terms and threshold re-evaluation) over the
+reference's own 4-wide tree (--tree reference, the default) or the binned
+binary tree.  Reported: value = queries/s of the device-resident call; e2e =
+the same call through the C ABI with host (pinned) buffers, copies
+included; accuracy of the mixed result against the plain FP64 walk of the
+same tree and (vs_reference) against the reference's own FP32 values on the
+first 200k queries; the plain FP64 walk's own throughput; the dominant
+kernel's live CUDA-event duration and roofline; a CPU baseline on this
+host's cores.  Unless --no-extras, the line also carries the other
+configurations as sub-results, each with its own CPU baseline: exact_c1,
+cloud_c3, precision_c4, served_c5 (2 s Poisson trace, 120 GB budget) and
+served_c5_pressure (a budget below the resident set).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gwn|reference]
 
@@ -62,6 +68,15 @@ def parse():
                     help="soup = the headline line; the others are extra measurement lines")
     ap.add_argument("--served-seconds", type=float, default=4.0,
                     help="served: length of the Poisson arrival trace")
+    ap.add_argument("--tree", choices=["reference", "binned"], default="reference",
+                    help="soup tree: the reference's own 4-wide tree (default) or the "
+                         "binned binary tree")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="default line only: skip the C1/C3/C4/C5 sub-results")
+    ap.add_argument("--extras-served-seconds", type=float, default=2.0,
+                    help="trace length of the C5 sub-results of the default line")
+    ap.add_argument("--pressure-budget-gb", type=float, default=24.0,
+                    help="HBM budget of the C5 run under memory pressure")
     ap.add_argument("--served-meshes", type=int, default=256)
     ap.add_argument("--fp64-sample", type=int, default=5000,
                     help="precision study: FP64 reference queries per (decade, side)")
@@ -159,17 +174,27 @@ def make_workload(args, rank):
     return V, F, Q
 
 
-def cpu_baseline(V, F, Q, seconds: float, mesh_handle=None):
-    """CPU soup FWN (oracle restatement of the reference algorithm) on this
-    host's cores, on a bounded sample of the same queries."""
+def soup_config(args, triangles, world):
+    """The headline line's config, identical in both arms."""
+    return {"workload": WORKLOAD, "triangles": int(triangles), "queries_per_gpu": int(args.nq),
+            "qdtype": args.qdtype, "order": 2, "beta": 2.0, "tree": args.tree,
+            "l2": "inputs larger than L2 (queries+results > 126 MB per step)",
+            "parallelism": f"query shards x{world}, tree replicated"}
+
+
+def cpu_baseline(V, F, Q, seconds: float, probe_n: int = 200_000):
+    """CPU soup FWN (oracle restatement of the reference algorithm, equal to
+    the reference's own outputs bit for bit) on this host's cores, on a
+    bounded sample of the same queries.  Also returns its values on the
+    first probe_n queries (the reference's W there)."""
     from oracle import oracle as O
     nthreads = O.num_threads(0)
     t0 = time.perf_counter()
     port = O.SoupPort(V, F, order=2)
     build_s = time.perf_counter() - t0
-    probe = Q[: min(len(Q), 200_000)]
+    probe = Q[: min(len(Q), probe_n)]
     t0 = time.perf_counter()
-    port.eval(probe, 2.0, nthreads)
+    Wprobe = port.eval(probe, 2.0, nthreads)
     dt = time.perf_counter() - t0
     rate = len(probe) / max(dt, 1e-9)
     n = int(min(len(Q), max(len(probe), rate * seconds)))
@@ -180,7 +205,7 @@ def cpu_baseline(V, F, Q, seconds: float, mesh_handle=None):
     return {"value": n / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
             "sample": f"first {n} of the workload's queries (same mesh), "
                       f"precompute {build_s:.3f} s not included",
-            "precompute_s": build_s}
+            "precompute_s": build_s}, Wprobe
 
 
 def run_reference(args, rank, world):
@@ -207,14 +232,15 @@ def run_reference(args, rank, world):
         times.append(time.perf_counter() - t0)
     total = sum(times)
     value = n * args.steps / total
+    ntri = int(F.shape[0])
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic", "config": {"workload": WORKLOAD, "queries_per_step": n,
-                                        "order": 2, "beta": 2.0, "qdtype": args.qdtype},
+        "data": "synthetic", "config": soup_config(args, ntri, world),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
-                         "sample": f"{n} queries per step of the {args.nq}-query workload"},
+                         "sample": f"{n} queries per step of the {args.nq}-query workload "
+                                   "(the reference's own algorithm and tree, FP32)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -236,9 +262,18 @@ def timed_steps(fn, steps, warmup, stream):
     return ev[0].elapsed_time(ev[-1]), per
 
 
-def run_exact_line(args):
+def _line(value, ms_per_step, steps, warmup, config, **extra):
+    return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": steps,
+            "warmup": warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config, **extra}
+
+
+def exact_c1(steps, warmup):
     """Configuration C1: exact winding number, icosphere subdiv 4 (5120
-    triangles, radial noise), 100k float64 queries in [-1.5,1.5]^3."""
+    triangles, radial noise), 100k float64 queries in [-1.5,1.5]^3; mixed
+    and plain FP64 (both through the cap hierarchy), against the CPU
+    restatement of the reference's hierarchy on all queries."""
     import torch
     import libigl_gb300 as G
     from libigl_gb300 import synth
@@ -253,66 +288,71 @@ def run_exact_line(args):
         def step():
             nonlocal W
             W = G.winding_number(dV, dF, dQ, precision=prec)
-        total, per = timed_steps(step, args.steps, args.warmup, stream)
-        out[prec] = (Q.shape[0] * args.steps / (total / 1e3), total / args.steps, W.cpu().numpy())
+        total, per = timed_steps(step, steps, warmup, stream)
+        out[prec] = (Q.shape[0] * steps / (total / 1e3), total / steps, W.cpu().numpy())
     Wm, W64 = out["mixed"][2], out["fp64"][2]
     t0 = time.perf_counter()
     Wref = O.winding_number_hier(V, F, Q)
     cpu_s = time.perf_counter() - t0
     err = np.abs(Wm - Wref)
-    line = {"metric": METRIC, "value": out["mixed"][0], "unit": UNIT, "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["mixed"][1],
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic",
-            "config": {"workload": "exact_icosphere4_noise_100kq", "triangles": int(F.shape[0]),
+    return {"config": {"workload": "exact_icosphere4_noise_100kq", "triangles": int(F.shape[0]),
                        "queries": int(Q.shape[0])},
+            "mixed_qps": out["mixed"][0], "mixed_ms": out["mixed"][1],
+            "fp64_qps": out["fp64"][0], "fp64_ms": out["fp64"][1],
+            "mixed_over_fp64": out["mixed"][0] / out["fp64"][0],
             "accuracy": {"max_abs_dW_vs_cpu_fp64": float(err.max()),
                          "p99_abs_dW": float(np.quantile(err, 0.99)),
                          "labels_identical": bool(np.array_equal(Wm > 0.5, Wref > 0.5)),
                          "fp64_gpu_vs_cpu_max": float(np.abs(W64 - Wref).max())},
-            "plain_fp64": {"value": out["fp64"][0], "ms_per_step": out["fp64"][1],
-                           "mixed_speedup": out["mixed"][0] / out["fp64"][0]},
-            "cpu_baseline": {"value": Q.shape[0] / cpu_s, "unit": UNIT, "cores": O.num_threads(0),
-                             "kind": "port",
+            "cpu_baseline": {"value": Q.shape[0] / cpu_s, "unit": UNIT,
+                             "cores": O.num_threads(0), "kind": "port",
                              "sample": "all 100k queries, hierarchical exact restatement "
                                        "(oracle/wn_hier.cpp), build included"}}
-    print(json.dumps(line), flush=True)
 
 
-def run_cloud_line(args):
+def run_exact_line(args):
+    r = exact_c1(args.steps, args.warmup)
+    print(json.dumps(_line(r["mixed_qps"], r["mixed_ms"], args.steps, args.warmup, r["config"],
+                           accuracy=r["accuracy"],
+                           plain_fp64={"value": r["fp64_qps"], "ms_per_step": r["fp64_ms"],
+                                       "mixed_speedup": r["mixed_over_fp64"]},
+                           cpu_baseline=r["cpu_baseline"])), flush=True)
+
+
+def cloud_c3(steps, warmup):
     """Configuration C3: point-cloud FWN, 2M torus samples, 8M queries,
-    order 2, beta 2."""
+    order 2, beta 2; octree and precompute timed, mixed and FP64 walks,
+    the CPU restatement of the reference on a 200k-query sample."""
     import torch
     import libigl_gb300 as G
     from libigl_gb300 import synth
     from oracle import oracle as O
     P, Nn, A = synth.torus_cloud(seed=3, n=2_000_000)
     Q = synth.cloud_queries(seed=4, nq=8_000_000)
+    dP, dN, dA = (torch.from_numpy(x).cuda() for x in (P, Nn, A))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    tree = G.Octree(torch.from_numpy(P).cuda())
+    tree = G.Octree(dP)
     torch.cuda.synchronize()
     octree_s = time.perf_counter() - t0
     t0 = time.perf_counter()
-    ce = G.CloudExpansion(torch.from_numpy(P).cuda(), torch.from_numpy(Nn).cuda(),
-                          torch.from_numpy(A).cuda(), order=2, tree=tree)
+    ce = G.CloudExpansion(dP, dN, dA, order=2, tree=tree)
     torch.cuda.synchronize()
     pre_s = time.perf_counter() - t0
     dQ = torch.from_numpy(Q).cuda()
     stream = torch.cuda.current_stream()
     res = {}
-    for prec, steps in (("mixed", args.steps), ("fp64", max(1, args.steps // 5))):
+    for prec, st in (("mixed", steps), ("fp64", max(1, steps // 5))):
         W = None
 
         def step():
             nonlocal W
             W = ce.eval(dQ, 2.0, precision=prec)
-        total, per = timed_steps(step, steps, min(args.warmup, 3), stream)
-        res[prec] = (Q.shape[0] * steps / (total / 1e3), total / steps, W.cpu().numpy())
+        total, per = timed_steps(step, st, min(warmup, 3), stream)
+        res[prec] = (Q.shape[0] * st / (total / 1e3), total / st, W.cpu().numpy())
     Wm, W64 = res["mixed"][2], res["fp64"][2]
     err = np.abs(Wm - W64)
     out_band = np.abs(W64 - 0.5) > 1e-3
-    # CPU oracle (restated reference) on a sample of the queries
     nc = O.num_threads(0)
     t0 = time.perf_counter()
     ot = O.octree(P)
@@ -322,36 +362,44 @@ def run_cloud_line(args):
     t0 = time.perf_counter()
     Wc = O.cloud_eval(P, Nn, A, ot, CM, R, EC, sample, 2.0)
     cpu_s = time.perf_counter() - t0
-    line = {"metric": METRIC, "value": res["mixed"][0], "unit": UNIT, "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["mixed"][1],
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic",
-            "config": {"workload": "cloud_torus_2Mpts_8Mq", "points": int(P.shape[0]),
+    return {"config": {"workload": "cloud_torus_2Mpts_8Mq", "points": int(P.shape[0]),
                        "queries": int(Q.shape[0]), "order": 2, "beta": 2.0,
                        "cells": int(tree.sizes()[0])},
+            "mixed_qps": res["mixed"][0], "mixed_ms": res["mixed"][1],
+            "fp64_qps": res["fp64"][0], "fp64_ms": res["fp64"][1],
+            "mixed_over_fp64": res["mixed"][0] / res["fp64"][0],
+            "octree_ms": octree_s * 1e3, "precompute_ms": pre_s * 1e3,
             "accuracy": {"max_abs_dW": float(err.max()), "p99_abs_dW": float(np.quantile(err, 0.99)),
                          "label_mismatch_outside_band":
                              int(((Wm > 0.5) != (W64 > 0.5))[out_band].sum()),
                          "fp64_vs_cpu_oracle_max": float(np.abs(W64[:len(sample)] - Wc).max()),
                          "queries_compared": int(Q.shape[0])},
-            "plain_fp64": {"value": res["fp64"][0], "ms_per_step": res["fp64"][1],
-                           "mixed_speedup": res["mixed"][0] / res["fp64"][0]},
-            "octree_s": octree_s, "precompute_s": pre_s,
             "cpu_baseline": {"value": len(sample) / cpu_s, "unit": UNIT, "cores": nc,
                              "kind": "port", "precompute_s": cpu_pre,
                              "sample": f"first {len(sample)} queries (oracle restatement of "
                                        "fast_winding_number.cpp), octree+precompute timed apart"}}
-    print(json.dumps(line), flush=True)
 
 
-def run_precision_study(args):
+def run_cloud_line(args):
+    r = cloud_c3(args.steps, args.warmup)
+    print(json.dumps(_line(r["mixed_qps"], r["mixed_ms"], args.steps, args.warmup, r["config"],
+                           accuracy=r["accuracy"],
+                           plain_fp64={"value": r["fp64_qps"], "ms_per_step": r["fp64_ms"],
+                                       "mixed_speedup": r["mixed_over_fp64"]},
+                           octree_s=r["octree_ms"] / 1e3, precompute_s=r["precompute_ms"] / 1e3,
+                           cpu_baseline=r["cpu_baseline"])), flush=True)
+
+
+def precision_c4(fp64_sample):
     """Configuration C4: 500k-triangle deformed geodesic sphere (nu = 158)
     with one 2000-triangle hole; 1M queries at 10^-k (k = 1..7) along vertex
     normals, inside and outside.  Mixed vs plain FP64, exact and soup paths,
-    per decade: max / p99 |dW| and label mismatches outside 0.5 +- 1e-3."""
+    per decade: max / p99 |dW| and label mismatches outside 0.5 +- 1e-3; the
+    CPU restatement of the reference's hierarchy timed on the FP64 sample."""
     import torch
     import libigl_gb300 as G
     from libigl_gb300 import synth
+    from oracle import oracle as O
     V, F, Q, dec, side = synth.precision_workload(seed=5)
     dV, dF, dQ = (torch.from_numpy(x).cuda() for x in (V, F, Q))
     rng = np.random.default_rng(0)
@@ -360,10 +408,11 @@ def run_precision_study(args):
     for k in range(1, 8):
         for sd in (-1.0, 1.0):
             cand = np.nonzero((dec == k) & (side == sd))[0]
-            idx.append(rng.choice(cand, size=min(args.fp64_sample, cand.size), replace=False))
+            idx.append(rng.choice(cand, size=min(fp64_sample, cand.size), replace=False))
     idx = np.sort(np.concatenate(idx))
     report = {"triangles": int(F.shape[0]), "queries": int(Q.shape[0]),
               "fp64_reference_queries": int(idx.size)}
+    G.winding_number(dV, dF, dQ[:4096], precision="mixed")  # warm-up
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     We_m = G.winding_number(dV, dF, dQ, precision="mixed").cpu().numpy()
@@ -389,8 +438,27 @@ def run_precision_study(args):
                     "soup_mixed_vs_fp64": stats(Ws_m, Ws_64, m_all),
                     "soup_fp64_vs_exact_fp64": stats(Ws_64[idx], We_64, m_s)})
     report["per_decade"] = per
-    print(json.dumps({"workload": "precision_study_geodesic158_hole2000_1Mq", **report}),
-          flush=True)
+    report["worst"] = {
+        "exact_mixed_vs_fp64_max": max(d["exact_mixed_vs_fp64"]["max"] for d in per),
+        "soup_mixed_vs_fp64_max": max(d["soup_mixed_vs_fp64"]["max"] for d in per),
+        "label_mismatches": sum(d["exact_mixed_vs_fp64"]["label_mismatch_outside_band"] +
+                                d["soup_mixed_vs_fp64"]["label_mismatch_outside_band"]
+                                for d in per)}
+    sub = idx[: min(idx.size, 20_000)]
+    t0 = time.perf_counter()
+    O.winding_number_hier(V, F, Q[sub])
+    cpu_s = time.perf_counter() - t0
+    report["exact_mixed_qps"] = Q.shape[0] / report["exact_mixed_s"]
+    report["cpu_baseline"] = {"value": sub.size / cpu_s, "unit": UNIT, "cores": O.num_threads(0),
+                              "kind": "port",
+                              "sample": f"{sub.size} of the FP64 sample's queries, hierarchical "
+                                        "exact restatement (oracle/wn_hier.cpp), build included"}
+    return report
+
+
+def run_precision_study(args):
+    r = precision_c4(args.fp64_sample)
+    print(json.dumps({"workload": "precision_study_geodesic158_hole2000_1Mq", **r}), flush=True)
 
 
 def _served_mesh(spec):
@@ -399,48 +467,54 @@ def _served_mesh(spec):
     return np.ascontiguousarray(V), np.ascontiguousarray(F, np.int32)
 
 
-def run_served_line(args):
-    """Configuration C5: 256 SH-deformed geodesic spheres (F log-uniform in
-    [1e3, 2e6], 20% with a hole) resident under a 120 GB HBM budget;
-    Poisson arrivals at 2000 requests/s, each a uniform mesh with n_q
-    log-uniform in [1e3, 1e6] float32 queries uniform in that mesh's box.
-    Reports served throughput and p50/p99 submit-to-result latency, then the
-    saturated throughput of the first 1000 requests in mixed precision and in
-    plain FP64 through the same server."""
+def served_meshes(count):
+    """The served workload's meshes (256 by default), generated in parallel."""
     import multiprocessing as mp
-    import threading
-    import torch
-    import libigl_gb300 as G
     from libigl_gb300 import synth
-    specs = synth.served_meshes(seed=6, count=args.served_meshes)
-    t0 = time.perf_counter()
+    specs = synth.served_meshes(seed=6, count=count)
     order = sorted(range(len(specs)), key=lambda i: -specs[i]["nu"])
     with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
         gen = pool.map(_served_mesh, [specs[i] for i in order], chunksize=1)
     meshes = [None] * len(specs)
     for i, m in zip(order, gen):
         meshes[i] = m
-    gen_s = time.perf_counter() - t0
+    return meshes
+
+
+def served_c5(meshes, trace_s, budget_bytes, nsat=1000, nsat_fp64=1000, cpu=True, seed=7):
+    """Configuration C5 through gwn_server: the meshes resident under an HBM
+    budget (LRU eviction, trees built on the server's builder thread);
+    Poisson arrivals at 2000 requests/s, each a uniform mesh with n_q
+    log-uniform in [1e3, 1e6] float32 queries uniform in that mesh's box.
+    Served throughput, p50/p99 submit-to-result latency, builds and
+    evictions during the trace, then the saturated throughput of the first
+    nsat requests in mixed precision and in plain FP64 through the same
+    server, and the CPU soup FWN (the reference's algorithm) on a sample of
+    the trace's requests."""
+    import threading
+    import torch
+    import libigl_gb300 as G
+    from oracle import oracle as O
     torch.cuda.set_device(0)
-    S = G.Server(hbm_budget_bytes=120 << 30, max_batch_queries=1 << 22, slots=3)
+    S = G.Server(hbm_budget_bytes=budget_bytes, max_batch_queries=1 << 22, slots=3)
     ids = [S.add_mesh(V, F) for V, F in meshes]
     ntri = np.array([F.shape[0] for _, F in meshes])
-    rng = np.random.default_rng(7)
+    rng = np.random.default_rng(seed)
     pool_n = 1_000_000
     pools = []
     for V, _ in meshes:
         lo, hi = V.min(0), V.max(0)
         pools.append((lo + rng.random((pool_n, 3)) * (hi - lo)).astype(np.float32))
-    # warm-up: one small request per mesh builds every tree (admission)
+    # warm-up: one small request per mesh builds every tree (admission; under
+    # a budget below the resident set this already evicts)
     t0 = time.perf_counter()
     reqs = [S.submit(ids[k], pools[k][:256]) for k in range(len(ids))]
     for r in reqs:
         r.wait()
     warm_s = time.perf_counter() - t0
     st0 = S.stats()
-    # the trace
     rate = 2000.0
-    nreq = int(rate * args.served_seconds)
+    nreq = int(rate * trace_s)
     arr = np.cumsum(rng.exponential(1.0 / rate, nreq))
     mesh_of = rng.integers(len(ids), size=nreq)
     nq_of = np.exp(rng.uniform(np.log(1e3), np.log(1e6), nreq)).astype(np.int64)
@@ -482,41 +556,68 @@ def run_served_line(args):
             h.wait()
         wall = time.perf_counter() - t
         b = S.stats()
-        return {"qps": int(nq_of[:n].sum()) / wall, "wall_s": wall,
+        return {"requests": n, "qps": int(nq_of[:n].sum()) / wall, "wall_s": wall,
                 "walk_gpu_ms": b["walk_gpu_ms"] - a["walk_gpu_ms"],
                 "batch_gpu_ms": b["batch_gpu_ms"] - a["batch_gpu_ms"],
-                "batches": b["batches"] - a["batches"]}
-    nsat = min(1000, nreq)
-    sat_m = saturated("mixed", nsat)
-    sat_d = saturated("fp64", nsat)
-    sat_mixed, sat_fp64 = sat_m["qps"], sat_d["qps"]
-    st2 = S.stats()
+                "batches": b["batches"] - a["batches"], "builds": b["builds"] - a["builds"]}
+    sat_m = saturated("mixed", min(nsat, nreq))
+    sat_d = saturated("fp64", min(nsat_fp64, nreq))
     S.close()
-    walk_ms = st1["walk_gpu_ms"] - st0["walk_gpu_ms"]
-    line = {"metric": METRIC, "value": served_q / span, "unit": UNIT, "n_gpus": 1,
-            "steps": 1, "warmup": 1, "ms_per_step": span * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "served_256_meshes_poisson_2000rps", "meshes": len(ids),
-                       "triangles_total": int(ntri.sum()), "requests": nreq,
-                       "queries": served_q, "offered_qps": served_q / arr[-1],
-                       "qdtype": "f32", "hbm_budget_gb": 120, "slots": 3,
-                       "max_batch_queries": 1 << 22},
-            "p50_ms": float(np.percentile(lat, 50) * 1e3),
-            "p99_ms": float(np.percentile(lat, 99) * 1e3),
-            "mean_ms": float(lat.mean() * 1e3),
-            "batches": st1["batches"] - st0["batches"],
-            "walk_gpu_ms": walk_ms,
-            "batch_gpu_ms": st1["batch_gpu_ms"] - st0["batch_gpu_ms"],
-            "refined": st1["refined"] - st0["refined"],
-            "resident": {"meshes": st1["resident_meshes"], "bytes": st1["resident_bytes"],
-                         "builds": st1["builds"], "evictions": st1["evictions"],
-                         "admission_s": warm_s},
-            "saturated_first_1000": {"mixed_qps": sat_mixed, "fp64_qps": sat_fp64,
-                                     "mixed_over_fp64": sat_mixed / sat_fp64,
-                                     "mixed": sat_m, "fp64": sat_d},
-            "mesh_generation_s": gen_s, "gpu_launches": launches,
-            "kernels_per_batch": st1["kernels_per_batch"]}
-    print(json.dumps(line), flush=True)
+    out = {"config": {"workload": "served_256_meshes_poisson_2000rps", "meshes": len(ids),
+                      "triangles_total": int(ntri.sum()), "requests": nreq,
+                      "queries": served_q, "offered_qps": served_q / arr[-1],
+                      "trace_s": trace_s, "qdtype": "f32",
+                      "hbm_budget_gb": budget_bytes / 2**30, "slots": 3,
+                      "max_batch_queries": 1 << 22},
+           "qps": served_q / span, "span_s": span,
+           "p50_ms": float(np.percentile(lat, 50) * 1e3),
+           "p99_ms": float(np.percentile(lat, 99) * 1e3),
+           "mean_ms": float(lat.mean() * 1e3),
+           "batches": st1["batches"] - st0["batches"],
+           "walk_gpu_ms": st1["walk_gpu_ms"] - st0["walk_gpu_ms"],
+           "batch_gpu_ms": st1["batch_gpu_ms"] - st0["batch_gpu_ms"],
+           "refined": st1["refined"] - st0["refined"],
+           "builds_during_trace": st1["builds"] - st0["builds"],
+           "evictions_during_trace": st1["evictions"] - st0["evictions"],
+           "resident": {"meshes": st1["resident_meshes"], "bytes": st1["resident_bytes"],
+                        "peak_bytes": st1["peak_resident_bytes"], "builds": st1["builds"],
+                        "evictions": st1["evictions"], "admission_s": warm_s},
+           "saturated": {"mixed_qps": sat_m["qps"], "fp64_qps": sat_d["qps"],
+                         "mixed_over_fp64": sat_m["qps"] / sat_d["qps"],
+                         "mixed": sat_m, "fp64": sat_d},
+           "gpu_launches": launches, "kernels_per_batch": st1["kernels_per_batch"]}
+    if cpu:
+        # the reference's soup FWN on the host cores: the first 6 requests of
+        # the trace whose mesh has at most 500k triangles (precompute apart)
+        nthreads = O.num_threads(0)
+        picked = [i for i in range(nreq) if ntri[mesh_of[i]] <= 500_000][:6]
+        q_tot, t_eval, t_pre = 0, 0.0, 0.0
+        for i in picked:
+            V, F = meshes[int(mesh_of[i])]
+            t0 = time.perf_counter()
+            port = O.SoupPort(V, F, order=2)
+            t_pre += time.perf_counter() - t0
+            Qi = pools[int(mesh_of[i])][off_of[i]:off_of[i] + nq_of[i]].astype(np.float64)
+            t0 = time.perf_counter()
+            port.eval(Qi, 2.0, nthreads)
+            t_eval += time.perf_counter() - t0
+            q_tot += Qi.shape[0]
+        out["cpu_baseline"] = {"value": q_tot / max(t_eval, 1e-9), "unit": UNIT,
+                               "cores": nthreads, "kind": "port", "precompute_s": t_pre,
+                               "sample": f"{len(picked)} requests of the trace ({q_tot} queries, "
+                                         "meshes <= 500k triangles), oracle/soup_hdk.cpp, "
+                                         "precompute timed apart"}
+    return out
+
+
+def run_served_line(args):
+    t0 = time.perf_counter()
+    meshes = served_meshes(args.served_meshes)
+    gen_s = time.perf_counter() - t0
+    r = served_c5(meshes, args.served_seconds, 120 << 30)
+    print(json.dumps(_line(r["qps"], r["span_s"] * 1e3, 1, 1, r["config"],
+                           **{k: v for k, v in r.items() if k not in ("config", "qps")},
+                           mesh_generation_s=gen_s)), flush=True)
 
 
 def run_signed_distance_line(args):
@@ -876,11 +977,11 @@ def main():
     # precompute (tree + moments), timed on the device
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    bvh = G.FastWindingNumberBVH(V, F, order=2)
+    bvh = G.FastWindingNumberBVH(V, F, order=2, tree=args.tree)
     torch.cuda.synchronize()
     build_s_first = time.perf_counter() - t0
     t0 = time.perf_counter()
-    bvh2 = G.FastWindingNumberBVH(V, F, order=2)
+    bvh2 = G.FastWindingNumberBVH(V, F, order=2, tree=args.tree)
     torch.cuda.synchronize()
     build_s = time.perf_counter() - t0
     bvh2.close()
@@ -989,8 +1090,22 @@ def main():
                 "kernel_ms": walk, "kernel_share_of_step": walk / ms_per_step}
 
     cpu = None
+    vs_reference = None
     if rank == 0 and not args.skip_cpu:
-        cpu = cpu_baseline(V, F, Q, args.cpu_seconds)
+        cpu, Wref = cpu_baseline(V, F, Q, args.cpu_seconds)
+        # against the reference's own W (its algorithm and tree, FP32, as
+        # restated bit for bit by the oracle) on the first queries
+        n = Wref.shape[0]
+        e = np.abs(Wm[:n] - Wref)
+        out_ref = np.abs(Wref - 0.5) > 1e-3
+        vs_reference = {"max_abs_dW": float(e.max()), "p99_abs_dW": float(np.quantile(e, 0.99)),
+                        "p999_abs_dW": float(np.quantile(e, 0.999)),
+                        "label_mismatch_outside_band":
+                            int(((Wm[:n] > 0.5) != (Wref > 0.5))[out_ref].sum()),
+                        "queries_compared": int(n),
+                        "note": "mixed GPU result vs the reference's FP32 soup algorithm "
+                                "(oracle/soup_hdk.cpp, bit-exact restatement) on the first "
+                                f"{n} queries; tree={args.tree}"}
 
     # kernels launched per step by the library (counted in the library's launch sites)
     launches_per_step = G.launch_count_of(lambda: step())
@@ -1000,11 +1115,9 @@ def main():
         "p50_ms": float(np.percentile(step_ms, 50)), "p99_ms": float(np.percentile(step_ms, 99)),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "triangles": int(nt), "queries_per_gpu": int(nq),
-                   "qdtype": args.qdtype, "order": 2, "beta": 2.0, "precision": "mixed",
-                   "l2": "inputs larger than L2 (queries+results > 126 MB per step)",
-                   "parallelism": f"query shards x{world}, tree replicated"},
-        "accuracy": accuracy,
+        "config": soup_config(args, nt, world),
+        "precision": "mixed",
+        "accuracy": dict(accuracy, vs_reference=vs_reference),
         "plain_fp64": {"value": plain_fp64_qps, "unit": UNIT, "ms_per_step": fp64_ms,
                        "mixed_speedup": value / world / plain_fp64_qps},
         "precompute_s": build_s, "precompute_first_call_s": build_s_first,
@@ -1012,10 +1125,50 @@ def main():
         "roofline": roofline, "clocks": clocks, "e2e": e2e, "cpu_baseline": cpu,
         "gpu_launches": int(launches_per_step * args.steps),
     }
+    if rank == 0 and world == 1 and not args.no_extras:
+        line.update(run_extras(args))
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def run_extras(args):
+    """The other configurations as sub-results of the default line, each
+    with its own CPU baseline: exact_c1, cloud_c3, precision_c4, served_c5
+    (120 GB budget, every tree resident) and served_c5_pressure (a budget
+    below the resident set: builds and evictions during the trace).  A
+    failing sub-result records its error instead of ending the run."""
+    import torch
+    out = {}
+    t_all = time.perf_counter()
+
+    def guard(name, fn):
+        t0 = time.perf_counter()
+        try:
+            out[name] = fn()
+        except Exception as e:  # recorded in the line, the headline stands
+            out[name] = {"error": f"{type(e).__name__}: {e}"}
+        out[name]["wall_s"] = time.perf_counter() - t0
+        torch.cuda.empty_cache()
+    guard("exact_c1", lambda: exact_c1(5, 3))
+    guard("cloud_c3", lambda: cloud_c3(3, 2))
+    guard("precision_c4", lambda: precision_c4(2000))
+    meshes = []
+
+    def gen():
+        meshes.extend(served_meshes(256))
+        return {"meshes": len(meshes)}
+    guard("served_meshes", gen)
+    if meshes:
+        guard("served_c5", lambda: served_c5(meshes, args.extras_served_seconds, 120 << 30,
+                                              nsat=500, nsat_fp64=150))
+        guard("served_c5_pressure",
+              lambda: served_c5(meshes, args.extras_served_seconds,
+                                int(args.pressure_budget_gb * 2**30), nsat=200,
+                                nsat_fp64=50, cpu=False, seed=8))
+    out["extras_wall_s"] = time.perf_counter() - t_all
+    return out
 
 
 if __name__ == "__main__":

@@ -349,6 +349,8 @@ struct SrvMesh {
   uint64_t last_use = 0;
   int pending = 0;        // submitted, not yet in a batch
   int inflight = 0;       // in a batch on the device
+  bool building = false;  // queued for, or being built by, the builder thread
+  int64_t reserved = 0;   // bytes of the budget held for it while it builds
 };
 
 struct SrvReq {
@@ -393,8 +395,16 @@ struct gwn_server {
 
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
-  bool stop = false;
+  bool stop = false, stop_builder = false;
   std::thread worker;
+  // Tree builds run on their own thread and stream: the worker keeps
+  // completing and launching batches while a mesh builds, and a request
+  // whose mesh is building waits in `pending` while later ones go ahead.
+  std::thread builder;
+  std::condition_variable cv_build;
+  std::deque<SrvMesh*> build_q;
+  int building = 0;       // meshes queued or being built
+  uint64_t events = 0;    // bumped by submissions and finished builds
 
   int64_t next_mesh = 1, next_req = 1;
   uint64_t tick = 0;
@@ -412,7 +422,8 @@ struct gwn_server {
   void run();
   void finish(SrvSlot& s, std::unique_lock<std::mutex>& lk);
   bool form_and_launch(SrvSlot& s, std::unique_lock<std::mutex>& lk);
-  int admit(SrvMesh* m, std::unique_lock<std::mutex>& lk, int& code, std::string& err);
+  int admit(SrvMesh* m, bool room_may_free, int& code, std::string& err);
+  void build_loop();
   void evict(SrvMesh* m);
   void complete(SrvReq* r, int status, const std::string& err);
 };
@@ -487,11 +498,15 @@ void gwn_server::evict(SrvMesh* m) {
   ++stats.evictions;
 }
 
-// Make mesh m resident.  Returns 0 (resident), 1 (wait: room is held by
-// batches in flight) or 2 (cannot be served; code and err say why).  Called
-// with the lock held; releases it while building.
-int gwn_server::admit(SrvMesh* m, std::unique_lock<std::mutex>& lk, int& code, std::string& err) {
+// Make mesh m resident.  Returns 0 (resident), 1 (its tree is queued or
+// building), 3 (room is held by batches in flight or by other builds) or 2
+// (cannot be served; code and err say why).  Called with the lock held; a
+// build is queued for the builder thread with its bytes reserved, never run
+// here.  room_may_free: some batch or build still holds budget that will
+// come free.
+int gwn_server::admit(SrvMesh* m, bool room_may_free, int& code, std::string& err) {
   if (m->res) return 0;
+  if (m->building) return 1;
   const int64_t need = estimate_bytes((int64_t)m->F.size() / 3);
   if (need > budget) {
     code = GWN_ERR_OUT_OF_MEMORY;
@@ -506,42 +521,87 @@ int gwn_server::admit(SrvMesh* m, std::unique_lock<std::mutex>& lk, int& code, s
       if (c->res && c->inflight == 0 && c != m && (!victim || c->last_use < victim->last_use))
         victim = c;
     }
-    if (!victim) return 1;
+    if (!victim) {
+      if (room_may_free || building > 0) return 3;
+      code = GWN_ERR_OUT_OF_MEMORY;
+      err = "mesh " + std::to_string(m->id) + " does not fit in the HBM budget";
+      return 2;
+    }
     evict(victim);
   }
-  lk.unlock();
-  std::unique_ptr<gwn_soup_impl> res(new gwn_soup_impl());
-  int rc = GWN_OK;
-  try {
-    const int64_t nF = (int64_t)m->F.size() / 3, nV = (int64_t)m->V.size() / 3;
-    DevBuf<double> dV((size_t)nV * 3, build_st);
-    DevBuf<int32_t> dF((size_t)nF * 3, build_st);
-    dV.upload(m->V.data(), (size_t)nV * 3, build_st);
-    dF.upload(m->F.data(), (size_t)nF * 3, build_st);
-    res->device = device;
-    if (GWN_SOUP_TREE_DEFAULT == GWN_TREE_REFERENCE)
-      soup_build_ref(*res, dV.get(), nV, dF.get(), nF, m->order, true, build_st);
-    else
-      soup_build(*res, dV.get(), nV, dF.get(), nF, m->order, true, build_st);
-    GWN_CUDA(cudaStreamSynchronize(build_st));
-  } catch (const Error& e) {
-    rc = e.code;
-    err = std::string("building mesh ") + std::to_string(m->id) + ": " + e.what();
-  } catch (const std::exception& e) {
-    rc = GWN_ERR_INTERNAL;
-    err = std::string("building mesh ") + std::to_string(m->id) + ": " + e.what();
-  }
-  lk.lock();
-  if (rc != GWN_OK) {
-    code = rc;
-    return 2;
-  }
-  m->bytes = res->bytes;
-  m->res = std::move(res);
-  resident_bytes += (int64_t)m->bytes;
+  m->building = true;
+  m->reserved = need;
+  resident_bytes += need;
   stats.peak_resident_bytes = std::max<int64_t>(stats.peak_resident_bytes, resident_bytes);
-  ++stats.builds;
-  return 0;
+  ++building;
+  build_q.push_back(m);
+  cv_build.notify_one();
+  return 1;
+}
+
+// The builder thread: one tree at a time on build_st, the lock released
+// while it builds.  A failed build completes the mesh's pending requests
+// with the error.
+void gwn_server::build_loop() {
+  cudaSetDevice(device);
+  std::unique_lock<std::mutex> lk(mu);
+  for (;;) {
+    cv_build.wait(lk, [&] { return stop_builder || !build_q.empty(); });
+    if (build_q.empty()) {
+      if (stop_builder) return;
+      continue;
+    }
+    SrvMesh* m = build_q.front();
+    build_q.pop_front();
+    lk.unlock();
+    std::unique_ptr<gwn_soup_impl> res(new gwn_soup_impl());
+    int rc = GWN_OK;
+    std::string err;
+    try {
+      const int64_t nF = (int64_t)m->F.size() / 3, nV = (int64_t)m->V.size() / 3;
+      DevBuf<double> dV((size_t)nV * 3, build_st);
+      DevBuf<int32_t> dF((size_t)nF * 3, build_st);
+      dV.upload(m->V.data(), (size_t)nV * 3, build_st);
+      dF.upload(m->F.data(), (size_t)nF * 3, build_st);
+      res->device = device;
+      if (GWN_SOUP_TREE_DEFAULT == GWN_TREE_REFERENCE)
+        soup_build_ref(*res, dV.get(), nV, dF.get(), nF, m->order, true, build_st);
+      else
+        soup_build(*res, dV.get(), nV, dF.get(), nF, m->order, true, build_st);
+      GWN_CUDA(cudaStreamSynchronize(build_st));
+    } catch (const Error& e) {
+      rc = e.code;
+      err = std::string("building mesh ") + std::to_string(m->id) + ": " + e.what();
+    } catch (const std::exception& e) {
+      rc = GWN_ERR_INTERNAL;
+      err = std::string("building mesh ") + std::to_string(m->id) + ": " + e.what();
+    }
+    lk.lock();
+    resident_bytes -= m->reserved;
+    m->reserved = 0;
+    m->building = false;
+    --building;
+    if (rc == GWN_OK) {
+      m->bytes = res->bytes;
+      m->res = std::move(res);
+      resident_bytes += (int64_t)m->bytes;
+      stats.peak_resident_bytes = std::max<int64_t>(stats.peak_resident_bytes, resident_bytes);
+      ++stats.builds;
+    } else {
+      for (auto it = pending.begin(); it != pending.end();) {
+        if ((*it)->mesh == m) {
+          m->pending--;
+          complete(*it, rc, err);
+          it = pending.erase(it);
+        } else {
+          ++it;
+        }
+      }
+      cv_done.notify_all();
+    }
+    ++events;
+    cv_work.notify_all();
+  }
 }
 
 bool gwn_server::form_and_launch(SrvSlot& s, std::unique_lock<std::mutex>& lk) {
@@ -549,28 +609,30 @@ bool gwn_server::form_and_launch(SrvSlot& s, std::unique_lock<std::mutex>& lk) {
   int64_t aligned = 0;
   bool any_busy = false;
   for (auto& o : slots) any_busy |= o->busy;
-  while (!pending.empty() && (int)take.size() < max_reqs) {
-    SrvReq* r = pending.front();
+  // In submission order, every request whose tree is resident joins the
+  // batch; one whose tree is building (or waits for room) stays pending
+  // without holding back the requests behind it.
+  for (auto it = pending.begin(); it != pending.end() && (int)take.size() < max_reqs;) {
+    SrvReq* r = *it;
     const int64_t al = (r->nq + 31) / 32 * 32;
     if (aligned + al > cap) break;
     std::string err;
     int code = GWN_ERR_OUT_OF_MEMORY;
-    const int a = admit(r->mesh, lk, code, err);
+    const int a = admit(r->mesh, any_busy || !take.empty(), code, err);
     if (a == 1) {
-      // room is held by meshes of requests in flight (or of this batch):
-      // launch what there is and admit this one when they finish
-      if (!take.empty() || any_busy) break;
-      err = "mesh " + std::to_string(r->mesh->id) + " does not fit in the HBM budget";
+      ++it;
+      continue;
     }
-    if (a != 0) {
-      pending.pop_front();
-      r->mesh->pending--;
+    // no room yet: launch what there is and admit this one when batches
+    // finish (no later request may overtake it for the room)
+    if (a == 3) break;
+    it = pending.erase(it);
+    r->mesh->pending--;
+    if (a == 2) {
       complete(r, code, err);
       cv_done.notify_all();
       continue;
     }
-    pending.pop_front();
-    r->mesh->pending--;
     r->mesh->inflight++;
     r->mesh->last_use = ++tick;
     take.push_back(r);
@@ -705,6 +767,7 @@ void gwn_server::run() {
   cudaSetDevice(device);
   std::unique_lock<std::mutex> lk(mu);
   for (;;) {
+    const uint64_t seen = events;
     bool progressed = false, any_busy = false;
     for (auto& sp : slots) {
       SrvSlot& s = *sp;
@@ -736,7 +799,7 @@ void gwn_server::run() {
         break;
       }
     }
-    if (stop && pending.empty()) {
+    if (stop && pending.empty() && building == 0) {
       bool busy = false;
       for (auto& sp : slots) busy |= sp->busy;
       if (!busy) break;
@@ -744,9 +807,9 @@ void gwn_server::run() {
     if (!progressed) {
       if (any_busy)
         cv_work.wait_for(lk, std::chrono::microseconds(20));
-      else
+      else  // until a submission, a finished build or stop
         cv_work.wait_for(lk, std::chrono::milliseconds(50),
-                         [&] { return stop || !pending.empty(); });
+                         [&] { return stop || events != seen; });
     }
   }
 }
@@ -757,7 +820,13 @@ gwn_server::~gwn_server() {
     stop = true;
   }
   cv_work.notify_all();
-  if (worker.joinable()) worker.join();
+  if (worker.joinable()) worker.join();  // the builder serves it until it ends
+  {
+    std::lock_guard<std::mutex> g(mu);
+    stop_builder = true;
+  }
+  cv_build.notify_all();
+  if (builder.joinable()) builder.join();
   for (auto& sp : slots) {
     if (sp->exec) cudaGraphExecDestroy(sp->exec);
     if (sp->ev_start) cudaEventDestroy(sp->ev_start);
@@ -822,6 +891,7 @@ int gwn_server_create(int64_t hbm_budget_bytes, int64_t max_batch_queries, int32
     }
     gwn_server* raw = S.get();
     S->worker = std::thread([raw] { raw->run(); });
+    S->builder = std::thread([raw] { raw->build_loop(); });
     *out = S.release();
   });
 }
@@ -855,8 +925,8 @@ int gwn_server_remove_mesh(gwn_server* S, int64_t mesh_id) {
     auto it = S->meshes.find(mesh_id);
     GWN_REQUIRE(it != S->meshes.end(), "unknown mesh id");
     SrvMesh* m = it->second.get();
-    if (m->pending || m->inflight)
-      throw Error(GWN_ERR_BUSY, "mesh has requests pending or in flight");
+    if (m->pending || m->inflight || m->building)
+      throw Error(GWN_ERR_BUSY, "mesh has requests pending or in flight, or is building");
     if (m->res) {
       S->resident_bytes -= (int64_t)m->bytes;
       m->res.reset();
@@ -910,6 +980,7 @@ int gwn_server_submit(gwn_server* S, int64_t mesh_id, const void* Q, int q_dtype
       }
       raw->mesh->pending++;
       S->pending.push_back(raw);
+      ++S->events;
     }
     S->cv_work.notify_one();
   });

@@ -159,3 +159,45 @@ def test_server_errors(cuda):
         S.remove_mesh(small)
         with pytest.raises(GwnError):
             S.submit(small, np.zeros((3, 3), np.float32))
+
+
+@pytest.mark.gpu
+def test_cold_build_does_not_block_resident_meshes(cuda):
+    """A request whose mesh is not resident waits for its tree, which builds
+    on the server's builder thread; requests for resident meshes submitted
+    after it keep being batched and finish first.  Every result still equals
+    the single-mesh path."""
+    import time
+    import libigl_gb300 as G
+    rng = np.random.default_rng(21)
+    Vb, Fb = synth.icosphere(8)  # 1.3M triangles: a build of tens of ms
+    Vb = synth.sh_deform(Vb, rng)
+    small = _meshes(2, seed=23)
+    with G.Server(hbm_budget_bytes=16 << 30, max_batch_queries=1 << 18, slots=2) as S:
+        sid = [S.add_mesh(V, F) for V, F in small]
+        for k, (V, _) in enumerate(small):  # make the small meshes resident
+            S.submit(sid[k], _queries(V, 64, seed=5 + k)).wait(60)
+        bid = S.add_mesh(Vb, Fb)
+        builds0 = S.stats()["builds"]
+        Qb = _queries(Vb, 2000, seed=31)
+        t_big = time.perf_counter()
+        big = S.submit(bid, Qb, 2.0, "mixed", np.float64)
+        subs = []
+        for i in range(16):
+            k = i % 2
+            Q = _queries(small[k][0], 500, seed=40 + i)
+            subs.append((k, Q, time.perf_counter(), S.submit(sid[k], Q, 2.0, "mixed", np.float64)))
+        done_small = []
+        for k, Q, t0, r in subs:
+            W, lat = r.wait(60)
+            done_small.append(t0 + lat)
+            bvh = G.FastWindingNumberBVH(*small[k], 2)
+            assert np.abs(W - bvh.eval(Q, 2.0, "mixed", out_dtype=np.float64)).max() <= TOL_SAME
+            bvh.close()
+        Wb, lat_b = big.wait(120)
+        assert S.stats()["builds"] == builds0 + 1
+        # the small requests did not wait for the build
+        assert max(done_small) < t_big + lat_b
+        bvh = G.FastWindingNumberBVH(Vb, Fb, 2)
+        assert np.abs(Wb - bvh.eval(Qb, 2.0, "mixed", out_dtype=np.float64)).max() <= TOL_SAME
+        bvh.close()
