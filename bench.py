@@ -63,7 +63,8 @@ def parse():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--workload", choices=["soup", "exact", "cloud", "precision", "served",
-                                           "signed_distance", "knn", "eytzinger2d", "swept"],
+                                           "signed_distance", "knn", "eytzinger2d", "swept",
+                                           "point_areas"],
                     default="soup",
                     help="soup = the headline line; the others are extra measurement lines")
     ap.add_argument("--served-seconds", type=float, default=4.0,
@@ -75,7 +76,7 @@ def parse():
                     help="default line only: skip the C1/C3/C4/C5 sub-results")
     ap.add_argument("--extras-served-seconds", type=float, default=2.0,
                     help="trace length of the C5 sub-results of the default line")
-    ap.add_argument("--pressure-budget-gb", type=float, default=24.0,
+    ap.add_argument("--pressure-budget-gb", type=float, default=36.0,
                     help="HBM budget of the C5 run under memory pressure")
     ap.add_argument("--served-meshes", type=int, default=256)
     ap.add_argument("--fp64-sample", type=int, default=5000,
@@ -620,6 +621,66 @@ def run_served_line(args):
                            mesh_generation_s=gen_s)), flush=True)
 
 
+def run_point_areas_line(args):
+    """Per-point areas (igl::copyleft::cgal::point_areas) of the C3 torus
+    cloud (2M points) from its 21 nearest points, as
+    copyleft/cgal/fast_winding_number.cpp:36-38 computes them; then the
+    whole points-only winding number (octree, knn, areas, expansions, 8M
+    queries).  CPU baseline: the oracle restatement (brute-force Delaunay,
+    not CGAL: CGAL is not in the image) on a sample of points."""
+    import torch
+    import libigl_gb300 as G
+    from libigl_gb300 import synth
+    from oracle import oracle as O
+    P, Nn, _ = synth.torus_cloud(seed=3, n=2_000_000)
+    dP, dN = torch.from_numpy(P).cuda(), torch.from_numpy(Nn).cuda()
+    stream = torch.cuda.current_stream()
+    I = None
+
+    def knn_step():
+        nonlocal I
+        I = G.knn(dP, dP, 21)
+    knn_total, _ = timed_steps(knn_step, max(1, args.steps // 2), 2, stream)
+    A = None
+
+    def step():
+        nonlocal A
+        A = G.point_areas(dP, I, dN)
+    total, per = timed_steps(step, args.steps, args.warmup, stream)
+    n = P.shape[0]
+    Ah, Ih = A.cpu().numpy(), I.cpu().numpy()
+    sample = 20_000
+    t0 = time.perf_counter()
+    Ao, _ = O.point_areas(P, Ih[:sample], Nn)
+    cpu_s = time.perf_counter() - t0
+    rel = np.abs(Ah[:sample] - Ao) / np.maximum(np.abs(Ao), 1e-300)
+    Q = synth.cloud_queries(seed=4, nq=8_000_000)
+    dQ = torch.from_numpy(Q).cuda()
+    W = None
+
+    def full():
+        nonlocal W
+        W = G.fast_winding_number_cloud_points(dP, dN, dQ, 2, 2.0, precision="mixed")
+    full_total, _ = timed_steps(full, 2, 1, stream)
+    line = _line(n * args.steps / (total / 1e3), total / args.steps, args.steps, args.warmup,
+                 {"workload": "point_areas_torus_2Mpts_k21", "points": n, "k": 21},
+                 metric_note="points/s of gwn_point_areas (unit below is per point)",
+                 knn_ms=knn_total / max(1, args.steps // 2),
+                 accuracy={"vs_cpu_restatement_rel_max": float(rel.max()),
+                           "vs_cpu_restatement_rel_p999": float(np.quantile(rel, 0.999)),
+                           "points_compared": sample,
+                           "area_sum_over_torus_area":
+                               float(Ah.sum() / (4 * np.pi ** 2 * 1.0 * 0.35))},
+                 points_only_fwn={"queries": int(Q.shape[0]), "ms_per_call": full_total / 2,
+                                  "qps_including_precompute": Q.shape[0] / (full_total / 2e3)},
+                 cpu_baseline={"value": sample / cpu_s, "unit": "points/s",
+                               "cores": O.num_threads(0), "kind": "port",
+                               "sample": f"first {sample} points, oracle/point_areas.cpp "
+                                         "(brute-force Delaunay, not CGAL)"})
+    line["unit"] = "points/s"
+    print(json.dumps(line), flush=True)
+
+
 def run_signed_distance_line(args):
     """igl::signed_distance with the fast-winding-number sign on the C2 mesh
     (1,297,489 triangles), 1M float64 queries of the C2 distribution.
@@ -957,7 +1018,8 @@ def main():
         {"exact": run_exact_line, "cloud": run_cloud_line, "precision": run_precision_study,
          "served": run_served_line,
          "signed_distance": run_signed_distance_line, "knn": run_knn_line,
-         "eytzinger2d": run_eytzinger_line, "swept": run_swept_line}[args.workload](args)
+         "eytzinger2d": run_eytzinger_line, "swept": run_swept_line,
+         "point_areas": run_point_areas_line}[args.workload](args)
         return
     import torch
     import libigl_gb300 as G

@@ -235,6 +235,33 @@ int gwn_octree_knn(const gwn_octree* tree, const void* Q, int q_dtype, int64_t n
 int gwn_knn(const double* P, int64_t nP, const double* V, int64_t nV, int64_t k, int32_t* I,
             int mem, void* stream);
 
+/* Per-point areas of a point cloud: igl::copyleft::cgal::point_areas(P,I,N,A,T)
+ *   (include/igl/copyleft/cgal/point_areas.h:40-53, point_areas.cpp:60-160).
+ * P, N: nP x 3 points and normals; I: nP x k neighbour indices (e.g. from
+ * gwn_knn / gwn_octree_knn), the first normally the point itself.  A (nP)
+ * receives each point's Voronoi area in its local Delaunay triangulation
+ * (the neighbours whose normal agrees with the first neighbour's, projected
+ * on their principal plane); T (nP x 3, optional: NULL skips it) the plane
+ * normal turned towards N.  A point with two or fewer agreeing neighbours
+ * gets A = 0, T = 0; a non-finite area gives 0.  k <= GWN_POINT_AREAS_MAX_K.
+ * The triangulation is computed directly for each point (no CGAL); for four
+ * or more cocircular plane points at the point it is not unique, and values
+ * there may differ from CGAL's. */
+#define GWN_POINT_AREAS_MAX_K 128
+int gwn_point_areas(const double* P, int64_t nP, const int32_t* I, int64_t k, const double* N,
+                    double* A, double* T, int mem, void* stream);
+
+/* Winding number of an oriented point cloud without areas:
+ * igl::copyleft::cgal::fast_winding_number(P,N,Q,expansion_order,beta,WN)
+ *   (include/igl/copyleft/cgal/fast_winding_number.h:20-36, .cpp:9-44):
+ *   octree of P, its 21 nearest points per point, gwn_point_areas, the
+ *   order-`order` expansions and their evaluation at Q (beta as for
+ *   gwn_cloud_eval; the reference's short overload uses order 2, beta 2).
+ * P, N nP x 3 float64; Q nQ x 3 and W nQ in their dtypes. */
+int gwn_cloud_winding_number_points(const double* P, const double* N, int64_t nP, const void* Q,
+                                    int q_dtype, int64_t nQ, int order, double beta, void* W,
+                                    int w_dtype, int precision, int mem, void* stream);
+
 typedef struct gwn_cloud gwn_cloud;
 
 int gwn_cloud_build(const gwn_octree* tree, const double* P, const double* N, const double* A,

@@ -25,6 +25,7 @@ import ctypes as C
 import numpy as np
 
 from . import _native as N
+from . import _native as NV  # for functions whose arguments are named N
 from ._native import GwnError
 from .serve import Server
 
@@ -35,7 +36,7 @@ __all__ = [
     "fast_winding_number_cloud", "fast_winding_number_cloud_oneshot", "device_status",
     "Server", "signed_distance", "knn", "eytzinger_aabb", "eytzinger_aabb_winding_number_tree",
     "eytzinger_aabb_winding_number", "swept_volume_signed_distance", "flood_fill",
-    "WindingNumberAABB",
+    "WindingNumberAABB", "point_areas", "fast_winding_number_cloud_points",
 ]
 
 _PREC = {"fp64": N.GWN_PLAIN_FP64, "plain": N.GWN_PLAIN_FP64, "mixed": N.GWN_MIXED}
@@ -474,6 +475,47 @@ def fast_winding_number_cloud_oneshot(P, Nrm, A, Q, order: int = 2, beta: float 
     finally:
         ce.close()
         ce.tree.close()
+
+
+def point_areas(P, I, N, return_T: bool = False):
+    """igl::copyleft::cgal::point_areas(P,I,N,A[,T])
+    (include/igl/copyleft/cgal/point_areas.h:40-53): per-point Voronoi
+    areas from the neighbour lists I (#P x k, e.g. ``knn(P, P, k)``).
+    Returns A (#P,), and T (#P x 3) too when return_T."""
+    L = NV.load()
+    Pa = _Arg(P, np.float64)
+    Ia = _Arg(I, np.int32, allowed=(np.int32,))
+    Na = _Arg(N, np.float64)
+    mem = _same_mem(Pa, Ia, Na)
+    if len(Ia.shape) != 2 or Ia.shape[0] != Pa.shape[0]:
+        raise ValueError("I must be #P x k")
+    n, k = Ia.shape
+    A = _empty_like_mem(mem, (n,), np.float64, like=Pa)
+    T = _empty_like_mem(mem, (n, 3), np.float64, like=Pa) if return_T else None
+    stream = _stream_ptr() if mem == NV.GWN_DEVICE else None
+    NV.check(L.gwn_point_areas(Pa.ptr, n, Ia.ptr, k, Na.ptr, _ptr_of(A),
+                               _ptr_of(T) if return_T else None, mem, stream))
+    return (A, T) if return_T else A
+
+
+def fast_winding_number_cloud_points(P, Nrm, Q, order: int = 2, beta: float = 2.0,
+                                     precision="mixed", out_dtype=None):
+    """igl::copyleft::cgal::fast_winding_number(P,N,Q,expansion_order,beta,WN)
+    (include/igl/copyleft/cgal/fast_winding_number.h:20-36): the areas come
+    from the 21 nearest points of each point (point_areas)."""
+    L = NV.load()
+    Pa = _Arg(P, np.float64)
+    Na = _Arg(Nrm, np.float64)
+    Qa = _Arg(Q)
+    mem = _same_mem(Pa, Na, Qa)
+    wdt = np.dtype(out_dtype) if out_dtype is not None else Qa.np_dtype
+    W = _empty_like_mem(mem, (Qa.shape[0],), wdt, like=Qa)
+    stream = _stream_ptr() if mem == NV.GWN_DEVICE else None
+    NV.check(L.gwn_cloud_winding_number_points(
+        Pa.ptr, Na.ptr, Pa.shape[0], Qa.ptr, Qa.code, Qa.shape[0], int(order), float(beta),
+        _ptr_of(W), NV.GWN_F64 if wdt == np.float64 else NV.GWN_F32, _prec(precision), mem,
+        stream))
+    return W
 
 
 def knn(P, V, k: int):

@@ -60,6 +60,9 @@ SIGNATURES = {
     "gwn_soup_squared_distance": ([_p, _p, _i, _i64, _d, _p, _p, _p, _i, _p], _i),
     "gwn_octree_knn": ([_p, _p, _i, _i64, _i64, _p, _i, _p], _i),
     "gwn_knn": ([_p, _i64, _p, _i64, _i64, _p, _i, _p], _i),
+    "gwn_point_areas": ([_p, _i64, _p, _i64, _p, _p, _p, _i, _p], _i),
+    "gwn_cloud_winding_number_points": ([_p, _p, _i64, _p, _i, _i64, _i, _d, _p, _i, _i, _i,
+                                         _p], _i),
     "gwn_eytzinger_slots": ([_i64], _i64),
     "gwn_wn_aabb_build": ([_p, _i64, _p, _i64, _i, _p, _p], _i),
     "gwn_wn_aabb_eval": ([_p, _p, _i64, _p, _i, _p], _i),

@@ -704,6 +704,78 @@ int gwn_knn(const double* P, int64_t nP, const double* V, int64_t nV, int64_t k,
   });
 }
 
+int gwn_point_areas(const double* P, int64_t nP, const int32_t* I, int64_t k, const double* N,
+                    double* A, double* T, int mem, void* stream) {
+  return guarded("gwn_point_areas", [&] {
+    GWN_REQUIRE(nP >= 0, "nP must be non-negative");
+    GWN_REQUIRE(k >= 1 && k <= GWN_POINT_AREAS_MAX_K,
+                "k must be in [1, " + std::to_string(GWN_POINT_AREAS_MAX_K) + "]");
+    GWN_REQUIRE(nP == 0 || (P && I && N && A), "P, I, N and A must be non-null");
+    check_mem(mem);
+    ensure_device();
+    if (nP == 0) return;
+    cudaStream_t st = as_stream(stream);
+    Staged<double> dP(P, (size_t)nP * 3, mem, st);
+    Staged<int32_t> dI(I, (size_t)(nP * k), mem, st);
+    Staged<double> dN(N, (size_t)nP * 3, mem, st);
+    Staged<double> dA(A, (size_t)nP, mem, st, false);
+    Staged<double> dT(T, T ? (size_t)nP * 3 : 0, mem, st, false);
+    DeviceStatus status(st, mem == GWN_HOST);
+    point_areas_run(dP.dev, nP, dI.dev, (int)k, dN.dev, dA.dev, T ? dT.dev : nullptr,
+                    status.ptr(), st);
+    status.check(st, "point_areas");
+    if (mem == GWN_HOST) {
+      GWN_CUDA(cudaMemcpyAsync(A, dA.dev, (size_t)nP * 8, cudaMemcpyDeviceToHost, st));
+      if (T) GWN_CUDA(cudaMemcpyAsync(T, dT.dev, (size_t)nP * 24, cudaMemcpyDeviceToHost, st));
+      GWN_CUDA(cudaStreamSynchronize(st));
+    }
+  });
+}
+
+int gwn_cloud_winding_number_points(const double* P, const double* N, int64_t nP, const void* Q,
+                                    int q_dtype, int64_t nQ, int order, double beta, void* W,
+                                    int w_dtype, int precision, int mem, void* stream) {
+  return guarded("gwn_cloud_winding_number_points", [&] {
+    GWN_REQUIRE(nP >= 0 && nQ >= 0, "sizes must be non-negative");
+    GWN_REQUIRE(nP == 0 || (P && N), "P and N must be non-null");
+    GWN_REQUIRE(nQ == 0 || (Q && W), "Q and W must be non-null");
+    GWN_REQUIRE(nQ < (int64_t(1) << 31) && nP < (int64_t(1) << 31), "at most 2^31-1 points");
+    GWN_REQUIRE(order >= 0 && order <= 2, "order must be 0, 1 or 2");
+    check_dtype(q_dtype, "Q");
+    check_dtype(w_dtype, "W");
+    check_precision(precision);
+    check_mem(mem);
+    ensure_device();
+    cudaStream_t st = as_stream(stream);
+    StagedBytes dQ(Q, (size_t)nQ * 3 * dtype_size(q_dtype), mem, st);
+    StagedBytes dW(W, (size_t)nQ * dtype_size(w_dtype), mem, st, false);
+    Staged<double> dP(P, (size_t)nP * 3, mem, st);
+    Staged<double> dN(N, (size_t)nP * 3, mem, st);
+    // copyleft/cgal/fast_winding_number.cpp:25-43: octree, 21 nearest
+    // points, areas, order-`order` expansions, Barnes-Hut evaluation
+    gwn_octree_impl tree;
+    GWN_CUDA(cudaGetDevice(&tree.device));
+    octree_build(tree, dP.dev, nP, true, st);
+    const int64_t k = knn_columns(nP, 21);
+    DevBuf<int32_t> I((size_t)std::max<int64_t>(nP * k, 1), st);
+    DevBuf<double> A((size_t)std::max<int64_t>(nP, 1), st);
+    DeviceStatus status(st, true);
+    if (nP > 0 && k > 0) {
+      octree_knn(tree, dP.dev, GWN_F64, nP, 21, I.get(), st);
+      point_areas_run(dP.dev, nP, I.get(), (int)k, dN.dev, A.get(), nullptr, status.ptr(), st);
+    }
+    status.check(st, "cloud_winding_number_points (areas)");
+    gwn_cloud_impl c;
+    c.device = tree.device;
+    cloud_build(c, tree, dN.dev, A.get(), order, st);
+    cloud_eval(c, beta, dQ.dev, q_dtype, nQ, dW.dev, w_dtype, precision, st);
+    if (mem == GWN_HOST && nQ)
+      GWN_CUDA(cudaMemcpyAsync(W, dW.dev, (size_t)nQ * dtype_size(w_dtype),
+                               cudaMemcpyDeviceToHost, st));
+    GWN_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
 int gwn_soup_squared_distance(const gwn_soup* soup, const void* Q, int q_dtype, int64_t nQ,
                               double up_sqr_d, double* sqrD, int32_t* I, double* C, int mem,
                               void* stream) {

@@ -72,6 +72,12 @@ void swept_volume_run(const double* V, int64_t nV, const int32_t* F, int64_t nF,
 // igl::flood_fill (swept.cu) over a res[0] x res[1] x res[2] grid (x fastest).
 void flood_fill_run(const int32_t res[3], double* S, cudaStream_t st);
 
+// igl::copyleft::cgal::point_areas (point_areas.cu): A (nP) and, when T is
+// non-null, T (nP x 3) from the nP x k neighbour lists I; device pointers.
+constexpr int kPointAreasMaxK = 128;
+void point_areas_run(const double* P, int64_t nP, const int32_t* I, int k, const double* N,
+                     double* A, double* T, unsigned* status, cudaStream_t st);
+
 // Hierarchical exact winding number of a triangle mesh (hier.cu): the
 // caller's V / F stay referenced (device pointers) for the FP64 re-checks.
 struct HierTree {

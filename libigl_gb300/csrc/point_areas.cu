@@ -1,0 +1,286 @@
+// Per-point Voronoi areas of a point cloud from its k nearest neighbours:
+// igl::copyleft::cgal::point_areas(P,I,N,A,T)
+// (include/igl/copyleft/cgal/point_areas.cpp:60-160), the step that gives the
+// point-cloud winding number its areas A from a raw scan
+// (copyleft/cgal/fast_winding_number.cpp:30-38).
+//
+// Per point i (one warp; lane j holds neighbours j, j + 32, ...), as the
+// reference:
+//   * the neighbours I(i,:) whose normal has a positive dot product with the
+//     first neighbour's normal are kept, in order (no filter for k = 1);
+//     two or fewer kept: A = 0, T = 0;
+//   * their mean and principal directions: the reference takes the SVD of
+//     the centred neighbours; here the eigenvectors of their 3 x 3 scatter
+//     matrix (cyclic Jacobi, FP64), the same right singular vectors up to
+//     sign.  T = the least direction, turned towards N(i); the kept points'
+//     coordinates along the two largest are the plane (the reference's
+//     scores U S, up to signs that move no distance);
+//   * the Delaunay triangles of the plane points that have the first kept
+//     point (vertex 0) as a corner.  The reference triangulates everything
+//     with CGAL and keeps those; here they come directly: inverting the
+//     other points about vertex 0 (q -> q / |q|^2) maps the circle through
+//     vertex 0, a and b to the line through the images of a and b and its
+//     inside to the side away from vertex 0, so triangle (0, a, b) has an
+//     empty circumcircle exactly when (a', b') is an edge of the convex hull
+//     of the images with vertex 0 strictly on the hull's side.  Each lane
+//     finds its point's hull successor (one gift-wrapping step, then a check
+//     that no image lies right of the edge).  Coinciding points are counted
+//     once, as CGAL keeps the first of equal points;
+//   * each such triangle adds the reference's share of its area to vertex 0
+//     (the circumcentric split for an acute triangle, half or a quarter of
+//     it when obtuse at vertex 0 or elsewhere), summed in FP64; a non-finite
+//     sum gives 0.
+// Neighbours are summed in a fixed warp order, so results are deterministic.
+// In degenerate configurations (four or more cocircular plane points at
+// vertex 0) the triangulation is not unique and CGAL's depends on its
+// insertion order; results there may differ.
+#include <cuda_runtime.h>
+
+#include <cmath>
+
+#include "gwn_common.cuh"
+#include "gwn_internal.cuh"
+
+namespace gwn {
+namespace {
+
+constexpr int kWarps = 4;  // points per CTA
+
+struct PaShared {
+  double p[kPointAreasMaxK][3];  // kept neighbours, in order
+  double u[kPointAreasMaxK], w[kPointAreasMaxK];    // plane coordinates
+  double su[kPointAreasMaxK], sw[kPointAreasMaxK];  // images under inversion about vertex 0
+  unsigned char ok[kPointAreasMaxK];                // image usable (distinct, not vertex 0)
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Eigen-decomposition of the symmetric 3 x 3 matrix a (cyclic Jacobi);
+// returns eigenvalues d and eigenvectors as the columns of v, sorted by
+// decreasing eigenvalue.
+__device__ void sym3_eigen(double a[3][3], double d[3], double v[3][3]) {
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) v[r][c] = r == c ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 32; ++sweep) {
+    const double off = fabs(a[0][1]) + fabs(a[0][2]) + fabs(a[1][2]);
+    const double scale = fabs(a[0][0]) + fabs(a[1][1]) + fabs(a[2][2]);
+    if (off == 0.0 || off <= 1e-300 + scale * 1e-17) break;
+    for (int p = 0; p < 2; ++p) {
+      for (int q = p + 1; q < 3; ++q) {
+        if (a[p][q] == 0.0) continue;
+        const double theta = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+        const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < 3; ++k) {  // a <- a J
+          const double akp = a[k][p], akq = a[k][q];
+          a[k][p] = c * akp - s * akq;
+          a[k][q] = s * akp + c * akq;
+        }
+        for (int k = 0; k < 3; ++k) {  // a <- J^T a
+          const double apk = a[p][k], aqk = a[q][k];
+          a[p][k] = c * apk - s * aqk;
+          a[q][k] = s * apk + c * aqk;
+        }
+        for (int k = 0; k < 3; ++k) {  // v <- v J
+          const double vkp = v[k][p], vkq = v[k][q];
+          v[k][p] = c * vkp - s * vkq;
+          v[k][q] = s * vkp + c * vkq;
+        }
+      }
+    }
+  }
+  for (int k = 0; k < 3; ++k) d[k] = a[k][k];
+  // sort descending (three elements)
+  for (int x = 0; x < 2; ++x)
+    for (int y = 0; y < 2 - x; ++y)
+      if (d[y] < d[y + 1]) {
+        const double t = d[y];
+        d[y] = d[y + 1];
+        d[y + 1] = t;
+        for (int r = 0; r < 3; ++r) {
+          const double tv = v[r][y];
+          v[r][y] = v[r][y + 1];
+          v[r][y + 1] = tv;
+        }
+      }
+}
+
+// The reference's share of triangle (X, Y, Z) for vertex X
+// (point_areas.cpp:122-150), plane coordinates.
+__device__ double voronoi_share(double xx, double xy, double yx, double yy, double zx,
+                                double zy) {
+  const double x = hypot(yx - zx, yy - zy);
+  const double y = hypot(xx - zx, xy - zy);
+  const double z = hypot(yx - xx, yy - xy);
+  const double cosX = (z * z + y * y - x * x) / (2 * y * z);
+  const double cosY = (z * z + x * x - y * y) / (2 * x * z);
+  const double cosZ = (x * x + y * y - z * z) / (2 * y * x);
+  double b0 = x * cosX, b1 = y * cosY, b2 = z * cosZ;
+  const double bs = b0 + b1 + b2;
+  b0 /= bs;
+  b1 /= bs;
+  b2 /= bs;
+  const double full = 0.25 * sqrt((x + (y + z)) * (z - (x - y)) * (z + (x - y)) * (x + (y - z)));
+  if (cosX < 0) return 0.5 * full;
+  if (cosY < 0 || cosZ < 0) return 0.25 * full;
+  return (b1 * full + b2 * full) / 2;
+}
+
+// orientation of (b - a) x (c - a): > 0 when c is left of a -> b
+__device__ __forceinline__ double orient(double ax, double ay, double bx, double by, double cx,
+                                         double cy) {
+  return (bx - ax) * (cy - ay) - (by - ay) * (cx - ax);
+}
+
+__global__ void __launch_bounds__(32 * kWarps) point_areas_kernel(
+    const double* __restrict__ P, int64_t nP, const int32_t* __restrict__ I, int k,
+    const double* __restrict__ N, double* __restrict__ A, double* __restrict__ T,
+    unsigned* __restrict__ status) {
+  __shared__ PaShared sh_all[kWarps];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  PaShared& S = sh_all[wib];
+  const unsigned full = 0xffffffffu;
+  const unsigned lt = (1u << lane) - 1u;
+  for (int64_t i = (int64_t)blockIdx.x * kWarps + wib; i < nP; i += (int64_t)gridDim.x * kWarps) {
+    const int32_t* row = I + i * k;
+    const int32_t i0 = row[0];
+    const bool bad0 = i0 < 0 || i0 >= nP;
+    // ---- kept neighbours, in order
+    double n0[3] = {0, 0, 0};
+    if (!bad0)
+      for (int d = 0; d < 3; ++d) n0[d] = N[(int64_t)i0 * 3 + d];
+    int m = 0;
+    bool any_bad = bad0;
+    for (int j0 = 0; j0 < k; j0 += 32) {
+      const int j = j0 + lane;
+      int32_t idx = j < k ? row[j] : -1;
+      const bool bad = j < k && (idx < 0 || idx >= nP);
+      bool keep = j < k && !bad && !bad0;
+      if (keep && k > 1) {
+        const double* nj = N + (int64_t)idx * 3;
+        keep = n0[0] * nj[0] + n0[1] * nj[1] + n0[2] * nj[2] > 0;
+      }
+      any_bad |= __any_sync(full, bad);
+      const unsigned b = __ballot_sync(full, keep);
+      if (keep) {
+        const int pos = m + __popc(b & lt);
+        for (int d = 0; d < 3; ++d) S.p[pos][d] = P[(int64_t)idx * 3 + d];
+      }
+      m += __popc(b);
+    }
+    if (any_bad && lane == 0) atomicOr(status, kStatusBadInput);
+    __syncwarp();
+    if (m <= 2 || any_bad) {
+      if (lane == 0) {
+        A[i] = 0.0;
+        if (T)
+          for (int d = 0; d < 3; ++d) T[i * 3 + d] = 0.0;
+      }
+      __syncwarp();
+      continue;
+    }
+    // ---- mean and scatter matrix (fixed warp order)
+    double s0 = 0, s1 = 0, s2 = 0;
+    for (int j = lane; j < m; j += 32) {
+      s0 += S.p[j][0];
+      s1 += S.p[j][1];
+      s2 += S.p[j][2];
+    }
+    const double mean[3] = {warp_sum(s0) / m, warp_sum(s1) / m, warp_sum(s2) / m};
+    double c00 = 0, c01 = 0, c02 = 0, c11 = 0, c12 = 0, c22 = 0;
+    for (int j = lane; j < m; j += 32) {
+      const double x = S.p[j][0] - mean[0], y = S.p[j][1] - mean[1], z = S.p[j][2] - mean[2];
+      c00 += x * x;
+      c01 += x * y;
+      c02 += x * z;
+      c11 += y * y;
+      c12 += y * z;
+      c22 += z * z;
+    }
+    double a[3][3];
+    a[0][0] = warp_sum(c00);
+    a[0][1] = a[1][0] = warp_sum(c01);
+    a[0][2] = a[2][0] = warp_sum(c02);
+    a[1][1] = warp_sum(c11);
+    a[1][2] = a[2][1] = warp_sum(c12);
+    a[2][2] = warp_sum(c22);
+    double ev[3], V[3][3];
+    sym3_eigen(a, ev, V);  // every lane alike
+    // ---- T: the least direction, turned towards N(i)
+    if (lane == 0 && T) {
+      const double* ni = N + i * 3;
+      double t[3] = {V[0][2], V[1][2], V[2][2]};
+      if (t[0] * ni[0] + t[1] * ni[1] + t[2] * ni[2] < 0)
+        for (int d = 0; d < 3; ++d) t[d] = -t[d];
+      for (int d = 0; d < 3; ++d) T[i * 3 + d] = t[d];
+    }
+    // ---- plane coordinates
+    for (int j = lane; j < m; j += 32) {
+      const double x = S.p[j][0] - mean[0], y = S.p[j][1] - mean[1], z = S.p[j][2] - mean[2];
+      S.u[j] = x * V[0][0] + y * V[1][0] + z * V[2][0];
+      S.w[j] = x * V[0][1] + y * V[1][1] + z * V[2][1];
+    }
+    __syncwarp();
+    const double u0 = S.u[0], w0 = S.w[0];
+    // ---- images about vertex 0; a point equal to vertex 0 or to an
+    // earlier point is left out (CGAL keeps the first of equal points)
+    for (int j = lane; j < m; j += 32) {
+      bool ok = j > 0 && !(S.u[j] == u0 && S.w[j] == w0);
+      for (int l = 1; ok && l < j; ++l)
+        if (S.u[l] == S.u[j] && S.w[l] == S.w[j]) ok = false;
+      const double qx = S.u[j] - u0, qy = S.w[j] - w0, r2 = qx * qx + qy * qy;
+      S.ok[j] = ok ? 1 : 0;
+      S.su[j] = ok ? qx / r2 : 0.0;
+      S.sw[j] = ok ? qy / r2 : 0.0;
+    }
+    __syncwarp();
+    // ---- hull edges of the images facing vertex 0 -> Delaunay triangles
+    double acc = 0.0;
+    for (int j = lane; j < m; j += 32) {
+      if (!S.ok[j]) continue;
+      const double jx = S.su[j], jy = S.sw[j];
+      int c = -1;
+      for (int l = 1; l < m; ++l) {  // most clockwise image seen from j
+        if (l == j || !S.ok[l]) continue;
+        if (c < 0) {
+          c = l;
+          continue;
+        }
+        const double o = orient(jx, jy, S.su[c], S.sw[c], S.su[l], S.sw[l]);
+        if (o < 0) {
+          c = l;
+        } else if (o == 0) {  // collinear: the farther one
+          const double dc = (S.su[c] - jx) * (S.su[c] - jx) + (S.sw[c] - jy) * (S.sw[c] - jy);
+          const double dl = (S.su[l] - jx) * (S.su[l] - jx) + (S.sw[l] - jy) * (S.sw[l] - jy);
+          if (dl > dc) c = l;
+        }
+      }
+      if (c < 0) continue;
+      bool edge = true;  // no image strictly right of j -> c
+      for (int l = 1; edge && l < m; ++l)
+        if (S.ok[l] && l != j && l != c &&
+            orient(jx, jy, S.su[c], S.sw[c], S.su[l], S.sw[l]) < 0)
+          edge = false;
+      if (!edge || !(orient(jx, jy, S.su[c], S.sw[c], 0.0, 0.0) > 0)) continue;
+      acc += voronoi_share(u0, w0, S.u[j], S.w[j], S.u[c], S.w[c]);
+    }
+    const double area = warp_sum(acc);
+    if (lane == 0) A[i] = isfinite(area) ? area : 0.0;
+    __syncwarp();
+  }
+}
+
+}  // namespace
+
+void point_areas_run(const double* P, int64_t nP, const int32_t* I, int k, const double* N,
+                     double* A, double* T, unsigned* status, cudaStream_t st) {
+  if (nP == 0) return;
+  const int64_t blocks = std::min<int64_t>((nP + kWarps - 1) / kWarps, (int64_t)num_sms() * 64);
+  launch_kernel(point_areas_kernel, (unsigned)blocks, 32 * kWarps, 0, st, P, nP, I, k, N, A, T,
+                status);
+}
+
+}  // namespace gwn

@@ -64,6 +64,7 @@ namespace {
 using soupwalk::EvalParams;
 
 constexpr int kMaxReqs = 256;  // the request index occupies 8 key bits
+constexpr int kBuilders = 4;   // tree builder threads (and streams) per server
 
 struct __align__(16) ServeReq {
   EvalParams prm;     // the request's tree and beta
@@ -391,7 +392,6 @@ struct gwn_server {
   int64_t cap = 0;  // key positions per batch (multiple of 32)
   int max_reqs = kMaxReqs;
   std::vector<std::unique_ptr<SrvSlot>> slots;
-  cudaStream_t build_st = nullptr;
 
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
@@ -400,7 +400,8 @@ struct gwn_server {
   // Tree builds run on their own thread and stream: the worker keeps
   // completing and launching batches while a mesh builds, and a request
   // whose mesh is building waits in `pending` while later ones go ahead.
-  std::thread builder;
+  std::vector<std::thread> builders;  // kBuilders threads, one stream each
+  std::vector<cudaStream_t> build_streams;
   std::condition_variable cv_build;
   std::deque<SrvMesh*> build_q;
   int building = 0;       // meshes queued or being built
@@ -423,17 +424,21 @@ struct gwn_server {
   void finish(SrvSlot& s, std::unique_lock<std::mutex>& lk);
   bool form_and_launch(SrvSlot& s, std::unique_lock<std::mutex>& lk);
   int admit(SrvMesh* m, bool room_may_free, int& code, std::string& err);
-  void build_loop();
+  void build_loop(cudaStream_t st);
   void evict(SrvMesh* m);
   void complete(SrvReq* r, int status, const std::string& err);
 };
 
-// A resident tree's device bytes, estimated before the first build from the
-// node and triangle records (2n-1 nodes of 96 + 192 + 32 bytes, 124 bytes
-// per triangle).
+// A resident tree's device bytes, bounded before its build: at most 2n-1
+// walk records of 96 + 192 bytes, 124 bytes per triangle, and for the
+// 4-wide tree at most n-1 nodes of 16 bytes (the binary tree: 2 search
+// records of 16 bytes per node instead).
 static int64_t estimate_bytes(int64_t nF) {
-  return std::max<int64_t>(1, 2 * nF - 1) *
-             (int64_t)(sizeof(SoupNodeF) + sizeof(SoupNodeD) + 2 * sizeof(float4)) +
+  const int64_t recs = std::max<int64_t>(1, 2 * nF - 1);
+  const int64_t tree = GWN_SOUP_TREE_DEFAULT == GWN_TREE_REFERENCE
+                           ? std::max<int64_t>(1, nF - 1) * 16
+                           : recs * (int64_t)(2 * sizeof(float4));
+  return recs * (int64_t)(sizeof(SoupNodeF) + sizeof(SoupNodeD)) + tree +
          nF * (int64_t)(3 * sizeof(float4) + 9 * sizeof(double) + sizeof(int32_t));
 }
 
@@ -539,10 +544,11 @@ int gwn_server::admit(SrvMesh* m, bool room_may_free, int& code, std::string& er
   return 1;
 }
 
-// The builder thread: one tree at a time on build_st, the lock released
-// while it builds.  A failed build completes the mesh's pending requests
-// with the error.
-void gwn_server::build_loop() {
+// A builder thread: one tree at a time on its own stream, the lock
+// released while it builds (small trees are latency-bound, so several
+// builders overlap on the device).  A failed build completes the mesh's
+// pending requests with the error.
+void gwn_server::build_loop(cudaStream_t build_st) {
   cudaSetDevice(device);
   std::unique_lock<std::mutex> lk(mu);
   for (;;) {
@@ -826,7 +832,9 @@ gwn_server::~gwn_server() {
     stop_builder = true;
   }
   cv_build.notify_all();
-  if (builder.joinable()) builder.join();
+  for (auto& b : builders)
+    if (b.joinable()) b.join();
+  for (cudaStream_t bs : build_streams) cudaStreamDestroy(bs);
   for (auto& sp : slots) {
     if (sp->exec) cudaGraphExecDestroy(sp->exec);
     if (sp->ev_start) cudaEventDestroy(sp->ev_start);
@@ -835,7 +843,6 @@ gwn_server::~gwn_server() {
     if (sp->ev_walk1) cudaEventDestroy(sp->ev_walk1);
     if (sp->st) cudaStreamDestroy(sp->st);
   }
-  if (build_st) cudaStreamDestroy(build_st);
 }
 
 extern "C" {
@@ -855,7 +862,6 @@ int gwn_server_create(int64_t hbm_budget_bytes, int64_t max_batch_queries, int32
     S->budget = hbm_budget_bytes;
     S->cap = max_batch_queries / 32 * 32;
     S->stats.budget_bytes = hbm_budget_bytes;
-    GWN_CUDA(cudaStreamCreateWithFlags(&S->build_st, cudaStreamNonBlocking));
     {
       const unsigned hc = std::thread::hardware_concurrency();
       S->pool.reset(new CopyPool((int)std::min(7u, std::max(1u, hc / 2))));
@@ -891,7 +897,12 @@ int gwn_server_create(int64_t hbm_budget_bytes, int64_t max_batch_queries, int32
     }
     gwn_server* raw = S.get();
     S->worker = std::thread([raw] { raw->run(); });
-    S->builder = std::thread([raw] { raw->build_loop(); });
+    for (int b = 0; b < kBuilders; ++b) {
+      cudaStream_t bs = nullptr;
+      GWN_CUDA(cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking));
+      S->build_streams.push_back(bs);
+      S->builders.emplace_back([raw, bs] { raw->build_loop(bs); });
+    }
     *out = S.release();
   });
 }

@@ -20,7 +20,8 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "liboracle.so")
 REF_SOUP_PATH = os.path.join(HERE, "_ref", "libref_soup.so")
 
-_SOURCES = ["gwn_oracle.cpp", "soup_port.cpp", "soup_hdk.cpp", "wn_hier.cpp", "distance.cpp", "aabb.cpp", "knn.cpp", "eytzinger.cpp", "swept.cpp"]
+_SOURCES = ["gwn_oracle.cpp", "soup_port.cpp", "soup_hdk.cpp", "wn_hier.cpp", "distance.cpp", "aabb.cpp", "knn.cpp", "eytzinger.cpp", "swept.cpp",
+            "point_areas.cpp"]
 
 
 def build(force: bool = False) -> str:
@@ -109,6 +110,8 @@ def lib():
             L.oracle_segments_wn.argtypes = [p, i64, p, p, i64, p]
         if hasattr(L, "oracle_flood_fill"):
             L.oracle_flood_fill.argtypes = [p, p]
+        if hasattr(L, "oracle_point_areas"):
+            L.oracle_point_areas.argtypes = [p, i64, p, C.c_int, p, p, p, C.c_int]
         if hasattr(L, "oracle_winding_number_hier"):
             L.oracle_winding_number_hier.argtypes = [p, i64, p, i64, p, i64, p, C.c_int]
             L.oracle_winding_number_hier.restype = C.c_int
@@ -565,3 +568,15 @@ def swept_volume_signed_distance(V, F, transforms, sign_type, GV, res, h, isolev
     if finite:
         S = flood_fill(res, S)
     return S
+
+
+def point_areas(P, I, N, nthreads: int = 0):
+    """igl::copyleft::cgal::point_areas restated (oracle/point_areas.cpp):
+    returns (A, T)."""
+    P, N = _d(P), _d(N)
+    I = np.ascontiguousarray(I, np.int32)
+    n, k = I.shape
+    A = np.empty(n, np.float64)
+    T = np.empty((n, 3), np.float64)
+    lib().oracle_point_areas(_ptr(P), n, _ptr(I), k, _ptr(N), _ptr(A), _ptr(T), nthreads)
+    return A, T

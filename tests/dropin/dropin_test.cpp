@@ -21,6 +21,8 @@
 #include <igl/signed_distance.h>
 #include <igl/swept_volume_signed_distance.h>
 #include <igl/winding_number.h>
+#include <igl/copyleft/cgal/fast_winding_number.h>
+#include <igl/copyleft/cgal/point_areas.h>
 
 static int failures = 0;
 static void check_near(const char* what, double a, double b, double tol) {
@@ -197,6 +199,41 @@ int main() {
     pout.set({2, 2, 2});
     check_near("wn_aabb_inside", hier.winding_number(pin), 1.0, 1e-6);
     check_near("wn_aabb_outside", hier.winding_number(pout), 0.0, 1e-6);
+  }
+  // copyleft::cgal::point_areas on a 7 x 7 hexagonal patch: the centre point
+  // owns its hexagonal Voronoi cell, (sqrt(3)/2) h^2; then the point-cloud
+  // winding number of the CGAL module from points and normals alone
+  {
+    const double h = 0.1;
+    Eigen::MatrixXd Ph(49, 3), Nh(49, 3);
+    int c = 0, centre = 0;
+    for (int j = -3; j <= 3; ++j)
+      for (int i = -3; i <= 3; ++i, ++c) {
+        Ph(c, 0) = h * (i + 0.5 * (j & 1));
+        Ph(c, 1) = h * j * std::sqrt(3.0) / 2;
+        Ph(c, 2) = 1e-7 * ((c * 37) % 11);  // tiny relief: no exact cocircularity
+        Nh(c, 0) = 0;
+        Nh(c, 1) = 0;
+        Nh(c, 2) = 1;
+        if (i == 0 && j == 0) centre = c;
+      }
+    std::vector<std::vector<int>> PIh;
+    Eigen::MatrixXi CHh;
+    Eigen::MatrixXd CNh;
+    Eigen::VectorXd Wh;
+    igl::octree(Ph, PIh, CHh, CNh, Wh);
+    Eigen::MatrixXi Ih;
+    igl::knn(Ph, 13, PIh, CHh, CNh, Wh, Ih);
+    Eigen::VectorXd Ah;
+    Eigen::MatrixXd Th;
+    igl::copyleft::cgal::point_areas(Ph, Ih, Nh, Ah, Th);
+    check_near("point_areas_hex", Ah(centre), std::sqrt(3.0) / 2 * h * h, 1e-6);
+    check_near("point_areas_normal", Th(centre, 2), 1.0, 1e-6);
+    Eigen::MatrixXd Qh(1, 3);
+    Qh.set({0.0, 0.0, 5.0});
+    Eigen::VectorXd WNh;
+    igl::copyleft::cgal::fast_winding_number(Ph, Nh, Qh, WNh);
+    check_near("cgal_fwn_far", WNh(0), 0.0, 1e-2);
   }
   std::printf("failures %d\n", failures);
   return failures ? 1 : 0;
