@@ -4,7 +4,12 @@
 // point-cloud winding number its areas A from a raw scan
 // (copyleft/cgal/fast_winding_number.cpp:30-38).
 //
-// Per point i (one warp; lane j holds neighbours j, j + 32, ...), as the
+// A warp takes 32 points: their kept neighbours' mean and scatter matrix
+// point by point (lane j holds neighbours j, j + 32, ...), the 3 x 3
+// eigenproblems lane by lane (one point each), then point by point the
+// plane and the triangulation.  GB300 runs FP64 far slower than FP32, so
+// the hull's orientation tests run in FP32 with an error bound and fall
+// back to FP64 only where the sign is not certain.  Per point, as the
 // reference:
 //   * the neighbours I(i,:) whose normal has a positive dot product with the
 //     first neighbour's normal are kept, in order (no filter for k = 1);
@@ -50,6 +55,7 @@ struct PaShared {
   double p[kPointAreasMaxK][3];  // kept neighbours, in order
   double u[kPointAreasMaxK], w[kPointAreasMaxK];    // plane coordinates
   double su[kPointAreasMaxK], sw[kPointAreasMaxK];  // images under inversion about vertex 0
+  float fu[kPointAreasMaxK], fw[kPointAreasMaxK];   // the images rounded to FP32
   unsigned char ok[kPointAreasMaxK];                // image usable (distinct, not vertex 0)
 };
 
@@ -135,6 +141,53 @@ __device__ __forceinline__ double orient(double ax, double ay, double bx, double
   return (bx - ax) * (cy - ay) - (by - ay) * (cx - ax);
 }
 
+// Kept neighbours of point i into S.p (the reference's normal filter);
+// returns their number (-1 when an index lies outside P).  Warp-uniform.
+__device__ int gather_kept(const double* __restrict__ P, int64_t nP, const int32_t* __restrict__ row,
+                           int k, const double* __restrict__ N, PaShared& S) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const int32_t i0 = row[0];
+  if (i0 < 0 || i0 >= nP) return -1;
+  const double n0x = N[(int64_t)i0 * 3], n0y = N[(int64_t)i0 * 3 + 1], n0z = N[(int64_t)i0 * 3 + 2];
+  int m = 0;
+  bool any_bad = false;
+  for (int j0 = 0; j0 < k; j0 += 32) {
+    const int j = j0 + lane;
+    const int32_t idx = j < k ? row[j] : -1;
+    const bool bad = j < k && (idx < 0 || idx >= nP);
+    bool keep = j < k && !bad;
+    if (keep && k > 1) {
+      const double* nj = N + (int64_t)idx * 3;
+      keep = n0x * nj[0] + n0y * nj[1] + n0z * nj[2] > 0;
+    }
+    any_bad |= __any_sync(full, bad);
+    const unsigned b = __ballot_sync(full, keep);
+    if (keep) {
+      const int pos = m + __popc(b & lt);
+      for (int d = 0; d < 3; ++d) S.p[pos][d] = P[(int64_t)idx * 3 + d];
+    }
+    m += __popc(b);
+  }
+  __syncwarp();
+  return any_bad ? -1 : m;
+}
+
+// Sign of orient(a, b, c) for the images: FP32 when its error bound
+// (input rounding of the FP64 images and the FP32 operations, a generous
+// 16 u) leaves the sign certain, else FP64.
+__device__ __forceinline__ int orient_sign(const PaShared& S, int a, int b, int c) {
+  const float ax = S.fu[a], ay = S.fw[a], bx = S.fu[b], by = S.fw[b], cx = S.fu[c], cy = S.fw[c];
+  const float o = (bx - ax) * (cy - ay) - (by - ay) * (cx - ax);
+  const float bound = 9.6e-7f * ((fabsf(bx) + fabsf(ax)) * (fabsf(cy) + fabsf(ay)) +
+                                 (fabsf(by) + fabsf(ay)) * (fabsf(cx) + fabsf(ax)));
+  if (o > bound) return 1;
+  if (o < -bound) return -1;
+  const double od = orient(S.su[a], S.sw[a], S.su[b], S.sw[b], S.su[c], S.sw[c]);
+  return od > 0 ? 1 : (od < 0 ? -1 : 0);
+}
+
 __global__ void __launch_bounds__(32 * kWarps) point_areas_kernel(
     const double* __restrict__ P, int64_t nP, const int32_t* __restrict__ I, int k,
     const double* __restrict__ N, double* __restrict__ A, double* __restrict__ T,
@@ -142,134 +195,142 @@ __global__ void __launch_bounds__(32 * kWarps) point_areas_kernel(
   __shared__ PaShared sh_all[kWarps];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   PaShared& S = sh_all[wib];
-  const unsigned full = 0xffffffffu;
-  const unsigned lt = (1u << lane) - 1u;
-  for (int64_t i = (int64_t)blockIdx.x * kWarps + wib; i < nP; i += (int64_t)gridDim.x * kWarps) {
-    const int32_t* row = I + i * k;
-    const int32_t i0 = row[0];
-    const bool bad0 = i0 < 0 || i0 >= nP;
-    // ---- kept neighbours, in order
-    double n0[3] = {0, 0, 0};
-    if (!bad0)
-      for (int d = 0; d < 3; ++d) n0[d] = N[(int64_t)i0 * 3 + d];
-    int m = 0;
-    bool any_bad = bad0;
-    for (int j0 = 0; j0 < k; j0 += 32) {
-      const int j = j0 + lane;
-      int32_t idx = j < k ? row[j] : -1;
-      const bool bad = j < k && (idx < 0 || idx >= nP);
-      bool keep = j < k && !bad && !bad0;
-      if (keep && k > 1) {
-        const double* nj = N + (int64_t)idx * 3;
-        keep = n0[0] * nj[0] + n0[1] * nj[1] + n0[2] * nj[2] > 0;
+  const int64_t nwarps = (int64_t)gridDim.x * kWarps;
+  for (int64_t base = ((int64_t)blockIdx.x * kWarps + wib) * 32; base < nP; base += nwarps * 32) {
+    const int np = (int)(nP - base < 32 ? nP - base : 32);
+    // ---- stage A, point by point: kept count, mean and scatter matrix;
+    // lane t keeps point base + t's
+    int my_m = 0;
+    double my_mean[3] = {0, 0, 0}, my_c[6] = {0, 0, 0, 0, 0, 0};
+    for (int t = 0; t < np; ++t) {
+      const int m = gather_kept(P, nP, I + (base + t) * k, k, N, S);
+      if (m <= 2) {
+        if (lane == t) my_m = m;
+        __syncwarp();
+        continue;
       }
-      any_bad |= __any_sync(full, bad);
-      const unsigned b = __ballot_sync(full, keep);
-      if (keep) {
-        const int pos = m + __popc(b & lt);
-        for (int d = 0; d < 3; ++d) S.p[pos][d] = P[(int64_t)idx * 3 + d];
+      double s0 = 0, s1 = 0, s2 = 0;
+      for (int j = lane; j < m; j += 32) {
+        s0 += S.p[j][0];
+        s1 += S.p[j][1];
+        s2 += S.p[j][2];
       }
-      m += __popc(b);
-    }
-    if (any_bad && lane == 0) atomicOr(status, kStatusBadInput);
-    __syncwarp();
-    if (m <= 2 || any_bad) {
-      if (lane == 0) {
-        A[i] = 0.0;
-        if (T)
-          for (int d = 0; d < 3; ++d) T[i * 3 + d] = 0.0;
+      const double mean[3] = {warp_sum(s0) / m, warp_sum(s1) / m, warp_sum(s2) / m};
+      double c[6] = {0, 0, 0, 0, 0, 0};
+      for (int j = lane; j < m; j += 32) {
+        const double x = S.p[j][0] - mean[0], y = S.p[j][1] - mean[1], z = S.p[j][2] - mean[2];
+        c[0] += x * x;
+        c[1] += x * y;
+        c[2] += x * z;
+        c[3] += y * y;
+        c[4] += y * z;
+        c[5] += z * z;
+      }
+      for (int q = 0; q < 6; ++q) c[q] = warp_sum(c[q]);
+      if (lane == t) {
+        my_m = m;
+        for (int d = 0; d < 3; ++d) my_mean[d] = mean[d];
+        for (int q = 0; q < 6; ++q) my_c[q] = c[q];
       }
       __syncwarp();
-      continue;
     }
-    // ---- mean and scatter matrix (fixed warp order)
-    double s0 = 0, s1 = 0, s2 = 0;
-    for (int j = lane; j < m; j += 32) {
-      s0 += S.p[j][0];
-      s1 += S.p[j][1];
-      s2 += S.p[j][2];
+    // ---- stage B, lane per point: principal directions, T, A for the
+    // degenerate cases
+    double V[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    if (lane < np && my_m > 2) {
+      double a[3][3] = {{my_c[0], my_c[1], my_c[2]},
+                        {my_c[1], my_c[3], my_c[4]},
+                        {my_c[2], my_c[4], my_c[5]}};
+      double ev[3];
+      sym3_eigen(a, ev, V);
     }
-    const double mean[3] = {warp_sum(s0) / m, warp_sum(s1) / m, warp_sum(s2) / m};
-    double c00 = 0, c01 = 0, c02 = 0, c11 = 0, c12 = 0, c22 = 0;
-    for (int j = lane; j < m; j += 32) {
-      const double x = S.p[j][0] - mean[0], y = S.p[j][1] - mean[1], z = S.p[j][2] - mean[2];
-      c00 += x * x;
-      c01 += x * y;
-      c02 += x * z;
-      c11 += y * y;
-      c12 += y * z;
-      c22 += z * z;
-    }
-    double a[3][3];
-    a[0][0] = warp_sum(c00);
-    a[0][1] = a[1][0] = warp_sum(c01);
-    a[0][2] = a[2][0] = warp_sum(c02);
-    a[1][1] = warp_sum(c11);
-    a[1][2] = a[2][1] = warp_sum(c12);
-    a[2][2] = warp_sum(c22);
-    double ev[3], V[3][3];
-    sym3_eigen(a, ev, V);  // every lane alike
-    // ---- T: the least direction, turned towards N(i)
-    if (lane == 0 && T) {
-      const double* ni = N + i * 3;
-      double t[3] = {V[0][2], V[1][2], V[2][2]};
-      if (t[0] * ni[0] + t[1] * ni[1] + t[2] * ni[2] < 0)
-        for (int d = 0; d < 3; ++d) t[d] = -t[d];
-      for (int d = 0; d < 3; ++d) T[i * 3 + d] = t[d];
-    }
-    // ---- plane coordinates
-    for (int j = lane; j < m; j += 32) {
-      const double x = S.p[j][0] - mean[0], y = S.p[j][1] - mean[1], z = S.p[j][2] - mean[2];
-      S.u[j] = x * V[0][0] + y * V[1][0] + z * V[2][0];
-      S.w[j] = x * V[0][1] + y * V[1][1] + z * V[2][1];
-    }
-    __syncwarp();
-    const double u0 = S.u[0], w0 = S.w[0];
-    // ---- images about vertex 0; a point equal to vertex 0 or to an
-    // earlier point is left out (CGAL keeps the first of equal points)
-    for (int j = lane; j < m; j += 32) {
-      bool ok = j > 0 && !(S.u[j] == u0 && S.w[j] == w0);
-      for (int l = 1; ok && l < j; ++l)
-        if (S.u[l] == S.u[j] && S.w[l] == S.w[j]) ok = false;
-      const double qx = S.u[j] - u0, qy = S.w[j] - w0, r2 = qx * qx + qy * qy;
-      S.ok[j] = ok ? 1 : 0;
-      S.su[j] = ok ? qx / r2 : 0.0;
-      S.sw[j] = ok ? qy / r2 : 0.0;
-    }
-    __syncwarp();
-    // ---- hull edges of the images facing vertex 0 -> Delaunay triangles
-    double acc = 0.0;
-    for (int j = lane; j < m; j += 32) {
-      if (!S.ok[j]) continue;
-      const double jx = S.su[j], jy = S.sw[j];
-      int c = -1;
-      for (int l = 1; l < m; ++l) {  // most clockwise image seen from j
-        if (l == j || !S.ok[l]) continue;
-        if (c < 0) {
-          c = l;
-          continue;
+    if (lane < np) {
+      const int64_t i = base + lane;
+      if (my_m < 0) atomicOr(status, kStatusBadInput);
+      if (my_m <= 2) A[i] = 0.0;
+      if (T) {
+        double t[3] = {0, 0, 0};
+        if (my_m > 2) {
+          const double* ni = N + i * 3;
+          t[0] = V[0][2];
+          t[1] = V[1][2];
+          t[2] = V[2][2];
+          if (t[0] * ni[0] + t[1] * ni[1] + t[2] * ni[2] < 0)
+            for (int d = 0; d < 3; ++d) t[d] = -t[d];
         }
-        const double o = orient(jx, jy, S.su[c], S.sw[c], S.su[l], S.sw[l]);
-        if (o < 0) {
-          c = l;
-        } else if (o == 0) {  // collinear: the farther one
-          const double dc = (S.su[c] - jx) * (S.su[c] - jx) + (S.sw[c] - jy) * (S.sw[c] - jy);
-          const double dl = (S.su[l] - jx) * (S.su[l] - jx) + (S.sw[l] - jy) * (S.sw[l] - jy);
-          if (dl > dc) c = l;
-        }
+        for (int d = 0; d < 3; ++d) T[i * 3 + d] = t[d];
       }
-      if (c < 0) continue;
-      bool edge = true;  // no image strictly right of j -> c
-      for (int l = 1; edge && l < m; ++l)
-        if (S.ok[l] && l != j && l != c &&
-            orient(jx, jy, S.su[c], S.sw[c], S.su[l], S.sw[l]) < 0)
-          edge = false;
-      if (!edge || !(orient(jx, jy, S.su[c], S.sw[c], 0.0, 0.0) > 0)) continue;
-      acc += voronoi_share(u0, w0, S.u[j], S.w[j], S.u[c], S.w[c]);
     }
-    const double area = warp_sum(acc);
-    if (lane == 0) A[i] = isfinite(area) ? area : 0.0;
-    __syncwarp();
+    // ---- stage C, point by point: plane, Delaunay star, area
+    for (int t = 0; t < np; ++t) {
+      const int m = __shfl_sync(0xffffffffu, my_m, t);
+      if (m <= 2) continue;
+      double mean[3], e1[3], e2[3];
+      for (int d = 0; d < 3; ++d) {
+        mean[d] = __shfl_sync(0xffffffffu, my_mean[d], t);
+        e1[d] = __shfl_sync(0xffffffffu, V[d][0], t);
+        e2[d] = __shfl_sync(0xffffffffu, V[d][1], t);
+      }
+      gather_kept(P, nP, I + (base + t) * k, k, N, S);
+      for (int j = lane; j < m; j += 32) {
+        const double x = S.p[j][0] - mean[0], y = S.p[j][1] - mean[1], z = S.p[j][2] - mean[2];
+        S.u[j] = x * e1[0] + y * e1[1] + z * e1[2];
+        S.w[j] = x * e2[0] + y * e2[1] + z * e2[2];
+      }
+      __syncwarp();
+      const double u0 = S.u[0], w0 = S.w[0];
+      const long long bu0 = __double_as_longlong(u0), bw0 = __double_as_longlong(w0);
+      // images about vertex 0; a point equal to vertex 0 or to an earlier
+      // point is left out (CGAL keeps the first of equal points)
+      for (int j = lane; j < m; j += 32) {
+        const long long bu = __double_as_longlong(S.u[j]), bw = __double_as_longlong(S.w[j]);
+        bool ok = j > 0 && !(bu == bu0 && bw == bw0);
+        for (int l = 1; ok && l < j; ++l)
+          if (__double_as_longlong(S.u[l]) == bu && __double_as_longlong(S.w[l]) == bw) ok = false;
+        const double qx = S.u[j] - u0, qy = S.w[j] - w0;
+        const double inv = ok ? 1.0 / (qx * qx + qy * qy) : 0.0;
+        S.ok[j] = ok ? 1 : 0;
+        S.su[j] = qx * inv;
+        S.sw[j] = qy * inv;
+        S.fu[j] = (float)(qx * inv);
+        S.fw[j] = (float)(qy * inv);
+      }
+      __syncwarp();
+      double acc = 0.0;
+      for (int j = lane; j < m; j += 32) {
+        if (!S.ok[j]) continue;
+        int c = -1;
+        for (int l = 1; l < m; ++l) {  // most clockwise image seen from j
+          if (l == j || !S.ok[l]) continue;
+          if (c < 0) {
+            c = l;
+            continue;
+          }
+          const int o = orient_sign(S, j, c, l);
+          if (o < 0) {
+            c = l;
+          } else if (o == 0) {  // collinear: the farther one
+            const double dc = (S.su[c] - S.su[j]) * (S.su[c] - S.su[j]) +
+                              (S.sw[c] - S.sw[j]) * (S.sw[c] - S.sw[j]);
+            const double dl = (S.su[l] - S.su[j]) * (S.su[l] - S.su[j]) +
+                              (S.sw[l] - S.sw[j]) * (S.sw[l] - S.sw[j]);
+            if (dl > dc) c = l;
+          }
+        }
+        if (c < 0) continue;
+        bool edge = true;  // no image strictly right of j -> c
+        for (int l = 1; edge && l < m; ++l)
+          if (S.ok[l] && l != j && l != c && orient_sign(S, j, c, l) < 0) edge = false;
+        if (!edge) continue;
+        // vertex 0 (the origin of the images) strictly left of j -> c
+        const double o0 = orient(S.su[j], S.sw[j], S.su[c], S.sw[c], 0.0, 0.0);
+        if (!(o0 > 0)) continue;
+        acc += voronoi_share(u0, w0, S.u[j], S.w[j], S.u[c], S.w[c]);
+      }
+      const double area = warp_sum(acc);
+      if (lane == 0) A[base + t] = isfinite(area) ? area : 0.0;
+      __syncwarp();
+    }
   }
 }
 
@@ -278,7 +339,8 @@ __global__ void __launch_bounds__(32 * kWarps) point_areas_kernel(
 void point_areas_run(const double* P, int64_t nP, const int32_t* I, int k, const double* N,
                      double* A, double* T, unsigned* status, cudaStream_t st) {
   if (nP == 0) return;
-  const int64_t blocks = std::min<int64_t>((nP + kWarps - 1) / kWarps, (int64_t)num_sms() * 64);
+  const int64_t blocks =
+      std::min<int64_t>((nP + 32 * kWarps - 1) / (32 * kWarps), (int64_t)num_sms() * 16);
   launch_kernel(point_areas_kernel, (unsigned)blocks, 32 * kWarps, 0, st, P, nP, I, k, N, A, T,
                 status);
 }

@@ -111,7 +111,7 @@ def lib():
         if hasattr(L, "oracle_flood_fill"):
             L.oracle_flood_fill.argtypes = [p, p]
         if hasattr(L, "oracle_point_areas"):
-            L.oracle_point_areas.argtypes = [p, i64, p, C.c_int, p, p, p, C.c_int]
+            L.oracle_point_areas.argtypes = [p, i64, i64, p, C.c_int, p, p, p, C.c_int]
         if hasattr(L, "oracle_winding_number_hier"):
             L.oracle_winding_number_hier.argtypes = [p, i64, p, i64, p, i64, p, C.c_int]
             L.oracle_winding_number_hier.restype = C.c_int
@@ -572,11 +572,13 @@ def swept_volume_signed_distance(V, F, transforms, sign_type, GV, res, h, isolev
 
 def point_areas(P, I, N, nthreads: int = 0):
     """igl::copyleft::cgal::point_areas restated (oracle/point_areas.cpp):
-    returns (A, T)."""
+    returns (A, T) for the points of I's rows (the first I.shape[0] points
+    of P; I may hold a leading block of the rows)."""
     P, N = _d(P), _d(N)
     I = np.ascontiguousarray(I, np.int32)
     n, k = I.shape
     A = np.empty(n, np.float64)
     T = np.empty((n, 3), np.float64)
-    lib().oracle_point_areas(_ptr(P), n, _ptr(I), k, _ptr(N), _ptr(A), _ptr(T), nthreads)
+    lib().oracle_point_areas(_ptr(P), P.shape[0], n, _ptr(I), k, _ptr(N), _ptr(A), _ptr(T),
+                             nthreads)
     return A, T

@@ -179,14 +179,15 @@ void one_point(const double* P, int64_t nP, const int32_t* I, int k, const doubl
 
 extern "C" {
 
-void oracle_point_areas(const double* P, int64_t nP, const int32_t* I, int k, const double* N,
-                        double* A, double* T, int nthreads) {
+// Rows 0 .. nI-1 of I are points 0 .. nI-1 of P (nP points in all).
+void oracle_point_areas(const double* P, int64_t nP, int64_t nI, const int32_t* I, int k,
+                        const double* N, double* A, double* T, int nthreads) {
   unsigned nt = nthreads > 0 ? (unsigned)nthreads : std::thread::hardware_concurrency();
   if (nt == 0) nt = 8;
   std::vector<std::thread> pool;
   for (unsigned t = 0; t < nt; ++t)
     pool.emplace_back([=] {
-      for (int64_t i = t; i < nP; i += nt) one_point(P, nP, I, k, N, i, A, T);
+      for (int64_t i = t; i < nI; i += nt) one_point(P, nP, I, k, N, i, A, T);
     });
   for (auto& th : pool) th.join();
 }
