@@ -76,7 +76,7 @@ def parse():
                     help="default line only: skip the C1/C3/C4/C5 sub-results")
     ap.add_argument("--extras-served-seconds", type=float, default=2.0,
                     help="trace length of the C5 sub-results of the default line")
-    ap.add_argument("--pressure-budget-gb", type=float, default=36.0,
+    ap.add_argument("--pressure-budget-gb", type=float, default=40.0,
                     help="HBM budget of the C5 run under memory pressure")
     ap.add_argument("--served-meshes", type=int, default=256)
     ap.add_argument("--fp64-sample", type=int, default=5000,
