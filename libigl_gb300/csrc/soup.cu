@@ -413,11 +413,7 @@ __global__ void emit_kernel(const BuildM* __restrict__ M, const int32_t* __restr
   nd[p] = D;
   SoupNodeF Fr;
   Fr.a = make_float4((float)D.P[0], (float)D.P[1], (float)D.P[2], (float)maxP2);
-  Fr.b = make_float4((float)D.N[0], (float)D.N[1], (float)D.N[2], (float)D.Nii[0]);
-  Fr.c = make_float4((float)D.Nii[1], (float)D.Nii[2], (float)D.Nxy_yx, (float)D.Nyz_zy);
-  Fr.d = make_float4((float)D.Nzx_xz, (float)D.Niii[0], (float)D.Niii[1], (float)D.Niii[2]);
-  Fr.e = make_float4((float)D.perm, (float)D.c2[0], (float)D.c2[1], (float)D.c2[2]);
-  Fr.f = make_float4((float)D.c2[3], (float)D.c2[4], (float)D.c2[5], __int_as_float((int)link));
+  pack_far32(Fr, D.N, D.Nii, D.Nxy_yx, D.Nyz_zy, D.Nzx_xz, D.Niii, D.perm, D.c2, (int)link);
   nf[p] = Fr;
   if (leaf) {
     const int32_t f = sorted_tri[slot];

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstring>
 
 #include "gwn_common.cuh"
 
@@ -11,15 +12,48 @@ namespace gwn {
 
 // 96-byte FP32 node record, read by the mixed-precision walk.
 //   a: P (average point) xyz, maxPDist2
-//   b: N xyz, Nxx          c: Nyy, Nzz, Nxy+Nyx, Nyz+Nzy
-//   d: Nzx+Nxz, Nxxx, Nyyy, Nzzz
-//   e: 2(Nxyz+Nyzx+Nzxy), 2Nxxy+Nyxx, 2Nxxz+Nzxx, 2Nyyz+Nzyy
-//   f: 2Nyyx+Nxyy, 2Nzzx+Nxzz, 2Nzzy+Nyzz, link (int bits)
+//   b: N xyz, A_xx     c: A_yy, A_zz, A_xy, A_xz     d: A_yz, K_xxx, K_yyy, K_zzz
+//   e: K_xxy, K_xxz, K_xyy, K_yyz     f: K_xzz, K_yzz, K_xyz, link (int bits)
+// A and K are the coefficients of the far field's order-1 quadratic and
+// order-2 cubic forms in the unit direction (pack_far32 below).
 // link >= 0: internal node, index one past its subtree (pre-order);
 // link < 0: leaf, triangle slot ~link.
 struct __align__(16) SoupNodeF {
   float4 a, b, c, d, e, f;
 };
+
+// The far field of FWNFS.h:7195-7251 with q = (x - P)/|x - P|,
+// m1 = 1/|x - P|, m2 = m1^2:
+//   omega = -m2 q.N
+//         + m2 m1 (S - 3 (sum_i q_i^2 Nii + q_x q_y Nxy_yx + ...))          (order 1)
+//         + m2 m1^2 (1.5 q.L - 7.5 (sum_i q_i^3 Niii + q_x q_y q_z perm + ...)) (order 2)
+// with S = Nxx + Nyy + Nzz and L_i = 3 Niii + the two c2 sums of FWNFS.h:
+// 7228-7233.  Since |q| = 1, S = S |q|^2 and q.L = (q.L)|q|^2, so the order-1
+// bracket is a quadratic form A(q) and the order-2 bracket a cubic form K(q):
+//   omega = m2 (m1 (A(q) + m1 K(q)) - q.N),
+// 6 + 10 coefficients in place of the 9 + 10 moments, and about half the
+// operations per evaluation.  The coefficients are formed here in FP64 from
+// the node's moments and rounded once.
+__host__ __device__ inline void pack_far32(SoupNodeF& R, const double N[3], const double Nii[3],
+                                           double Nxy_yx, double Nyz_zy, double Nzx_xz,
+                                           const double Niii[3], double perm, const double c2[6],
+                                           int link) {
+  const double S = Nii[0] + Nii[1] + Nii[2];
+  const double Lx = 3 * Niii[0] + (c2[3] + c2[4]);
+  const double Ly = 3 * Niii[1] + (c2[5] + c2[0]);
+  const double Lz = 3 * Niii[2] + (c2[1] + c2[2]);
+  R.b = make_float4((float)N[0], (float)N[1], (float)N[2], (float)(S - 3 * Nii[0]));
+  R.c = make_float4((float)(S - 3 * Nii[1]), (float)(S - 3 * Nii[2]), (float)(-3 * Nxy_yx),
+                    (float)(-3 * Nzx_xz));
+  R.d = make_float4((float)(-3 * Nyz_zy), (float)(1.5 * Lx - 7.5 * Niii[0]),
+                    (float)(1.5 * Ly - 7.5 * Niii[1]), (float)(1.5 * Lz - 7.5 * Niii[2]));
+  R.e = make_float4((float)(1.5 * Ly - 7.5 * c2[0]), (float)(1.5 * Lz - 7.5 * c2[1]),
+                    (float)(1.5 * Lx - 7.5 * c2[3]), (float)(1.5 * Lz - 7.5 * c2[2]));
+  float lf;
+  memcpy(&lf, &link, sizeof(float));
+  R.f = make_float4((float)(1.5 * Lx - 7.5 * c2[4]), (float)(1.5 * Ly - 7.5 * c2[5]),
+                    (float)(-7.5 * perm), lf);
+}
 
 // 192-byte FP64 node record (plain FP64 walk, FP64 re-checks).
 struct __align__(16) SoupNodeD {

@@ -1383,11 +1383,19 @@ __device__ void write_records(const Loc<float>& C32, const Loc<double>& C64, lon
   const float m32 = lane_maxP2(C32);
   SoupNodeF R;
   R.a = make_float4(C32.P[0], C32.P[1], C32.P[2], m32);
-  R.b = make_float4(C32.N[0], C32.N[1], C32.N[2], C32.Nii[0]);
-  R.c = make_float4(C32.Nii[1], C32.Nii[2], C32.Nxy + C32.Nyx, C32.Nyz + C32.Nzy);
-  R.d = make_float4(C32.Nzx + C32.Nxz, C32.Niii[0], C32.Niii[1], C32.Niii[2]);
-  R.e = make_float4(C32.perm, C32.c2[0], C32.c2[1], C32.c2[2]);
-  R.f = make_float4(C32.c2[3], C32.c2[4], C32.c2[5], __int_as_float((int)link));
+  {
+    // the reference's FP32 moments (with its FP32 sums of the mixed terms),
+    // packed into the walk's far-field forms
+    double N[3], Nii[3], Niii[3], c2[6];
+    for (int d = 0; d < 3; ++d) {
+      N[d] = C32.N[d];
+      Nii[d] = C32.Nii[d];
+      Niii[d] = C32.Niii[d];
+    }
+    for (int k = 0; k < 6; ++k) c2[k] = C32.c2[k];
+    pack_far32(R, N, Nii, (double)(C32.Nxy + C32.Nyx), (double)(C32.Nyz + C32.Nzy),
+               (double)(C32.Nzx + C32.Nxz), Niii, (double)C32.perm, c2, (int)link);
+  }
   *nf = R;
   SoupNodeD D;
   for (int d = 0; d < 3; ++d) {

@@ -24,7 +24,7 @@ constexpr float kInv4PiF = 0.079577471545947667884f;
 constexpr double kInv4Pi = 0.079577471545947667884;
 
 // Far field of one node about its average point, FWNFS.h:7195-7251, with
-// (dx,dy,dz) = q - P and r2 = |q - P|^2.  T is float or double.
+// (dx,dy,dz) = q - P and r2 = |q - P|^2, on the FP64 records.
 template <typename T>
 struct Far {
   T N[3], Nii[3], Nxy_yx, Nyz_zy, Nzx_xz, Niii[3], perm, c2[6];
@@ -94,17 +94,28 @@ __device__ __forceinline__ T tri_solid_angle(T ax, T ay, T az, T bx, T by, T bz,
   return T(2) * g_atan2(num, den);
 }
 
-__device__ __forceinline__ Far<float> load_far(const SoupNodeF* r) {
-  const float4 b = __ldg(&r->b), c = __ldg(&r->c), d = __ldg(&r->d), e = __ldg(&r->e),
-               f = __ldg(&r->f);
-  Far<float> m;
-  m.N[0] = b.x; m.N[1] = b.y; m.N[2] = b.z;
-  m.Nii[0] = b.w; m.Nii[1] = c.x; m.Nii[2] = c.y;
-  m.Nxy_yx = c.z; m.Nyz_zy = c.w; m.Nzx_xz = d.x;
-  m.Niii[0] = d.y; m.Niii[1] = d.z; m.Niii[2] = d.w;
-  m.perm = e.x; m.c2[0] = e.y; m.c2[1] = e.z; m.c2[2] = e.w;
-  m.c2[3] = f.x; m.c2[4] = f.y; m.c2[5] = f.z;
-  return m;
+// FP32 far field of a packed record (pack_far32): omega = m2 (m1 (A(q) +
+// m1 K(q)) - q.N) with q = (x - P) m1, (dx,dy,dz) = x - P, r2 = |x - P|^2.
+__device__ __forceinline__ float far_field32(const SoupNodeF* r, float dx, float dy, float dz,
+                                             float r2, int order) {
+  const float4 b = __ldg(&r->b);
+  const float m1 = g_rsqrt(r2), m2 = m1 * m1;
+  const float qx = dx * m1, qy = dy * m1, qz = dz * m1;
+  const float lin = fmaf(qx, b.x, fmaf(qy, b.y, qz * b.z));
+  if (order == 0) return -m2 * lin;
+  const float4 c = __ldg(&r->c), d = __ldg(&r->d);
+  const float x2 = qx * qx, y2 = qy * qy, z2 = qz * qz, yz = qy * qz;
+  const float a = fmaf(qx, fmaf(b.w, qx, fmaf(c.z, qy, c.w * qz)),
+                       fmaf(c.x, y2, fmaf(c.y, z2, d.x * yz)));
+  float s = a;
+  if (order >= 2) {
+    const float4 e = __ldg(&r->e), f = __ldg(&r->f);
+    const float kx = fmaf(d.y, x2, fmaf(e.z, y2, fmaf(f.x, z2, f.z * yz)));
+    const float ky = fmaf(e.x, x2, fmaf(d.z, y2, f.y * z2));
+    const float kz = fmaf(e.y, x2, fmaf(e.w, y2, d.w * z2));
+    s = fmaf(m1, fmaf(qx, kx, fmaf(qy, ky, qz * kz)), a);
+  }
+  return m2 * fmaf(m1, s, -lin);
 }
 
 __device__ __forceinline__ Far<double> load_far(const SoupNodeD* r) {
@@ -281,7 +292,7 @@ __device__ __forceinline__ void walk_mixed(const EvalParams& prm, bool valid, do
         }
         if (!near) {
           if (kStats) ++c.far;
-          const float om = far_field<float>(load_far(r), dx, dy, dz, r2, prm.order);
+          const float om = far_field32(r, dx, dy, dz, r2, prm.order);
           if (isfinite(om)) {
             acc += om;
             resume = leaf ? node + 1 : link;
