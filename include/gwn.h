@@ -15,7 +15,9 @@
  * Precision modes:
  *   GWN_PLAIN_FP64 -- every term, sum and far-field expansion in FP64.
  *   GWN_MIXED      -- FP32 bulk arithmetic; FP64 for (i) exact terms of
- *                     queries within 1e-3 * bbox-diagonal of a primitive,
+ *                     queries within 1e-3 * bbox-diagonal of a primitive
+ *                     (for triangle soups: FP64 corner vectors, determinant
+ *                     and denominator, the angle itself from FP32 atan2),
  *                     (ii) moment accumulation, (iii) full re-evaluation of
  *                     any query whose FP32 result lies within 1e-3 of 0.5.
  *

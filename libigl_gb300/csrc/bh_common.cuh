@@ -53,6 +53,14 @@ __device__ __forceinline__ float g_rsqrt(float x) { return rsqrtf(x); }
 __device__ __forceinline__ double g_rsqrt(double x) { return 1.0 / sqrt(x); }
 __device__ __forceinline__ float g_atan2(float y, float x) { return atan2f(y, x); }
 __device__ __forceinline__ double g_atan2(double y, double x) { return atan2(y, x); }
+// 256-bit read-only global load (ld.global.nc.v8, sm_100 and later) of the
+// 32 bytes at p, which must be 32-byte aligned.
+__device__ __forceinline__ void ldg256(const void* p, float4& lo, float4& hi) {
+  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(lo.x), "=f"(lo.y), "=f"(lo.z), "=f"(lo.w), "=f"(hi.x), "=f"(hi.y), "=f"(hi.z),
+        "=f"(hi.w)
+      : "l"(p));
+}
 __device__ __forceinline__ float g_rcp(float x) { return __frcp_rn(x); }
 __device__ __forceinline__ double g_rcp(double x) { return 1.0 / x; }
 

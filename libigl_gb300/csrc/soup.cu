@@ -39,9 +39,10 @@
 //   * mixed precision: FP32 records and arithmetic; the open test is redone
 //     in FP64 whenever the FP32 margin is inside a proven error band, so the
 //     mixed walk makes exactly the plain FP64 walk's decisions; exact
-//     triangle terms within 1e-3 * bbox diagonal of the query are computed in
-//     FP64 from the original vertices; results within 1e-3 of 0.5 are
-//     recomputed by the plain FP64 walk.
+//     triangle terms within 1e-3 * bbox diagonal of the query are computed
+//     from the original vertices with FP64 corner vectors, determinant and
+//     denominator (the angle from FP32 atan2 of the scaled pair); results
+//     within 1e-3 of 0.5 are recomputed by the plain FP64 walk.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -441,7 +442,7 @@ __device__ __forceinline__ void read_query(const QT* Q, const int32_t* perm, con
 // Mixed-precision warp-coherent walk.  One query per lane.  kStats builds
 // an instrumented copy that counts its work into `stats` (see
 // gwn_soup_walk_stats); the timed kernel is the kStats = false instance.
-template <typename QT, typename WT, bool kStats = false>
+template <typename QT, typename WT, bool kStats = false, int kTree = -1>
 __global__ void __launch_bounds__(128, 8) soup_eval_mixed_kernel(EvalParams prm, const QT* __restrict__ Q,
                                                               const int32_t* __restrict__ perm,
                                                               int64_t nQ, WT* __restrict__ W,
@@ -457,7 +458,8 @@ __global__ void __launch_bounds__(128, 8) soup_eval_mixed_kernel(EvalParams prm,
   float acc;
   double acc64;
   soupwalk::WalkCounters c;
-  soupwalk::walk_mixed<kStats>(prm, valid, qx, qy, qz, acc, acc64, c, near_q[threadIdx.x >> 5]);
+  soupwalk::walk_mixed<kStats, kTree>(prm, valid, qx, qy, qz, acc, acc64, c,
+                                      near_q[threadIdx.x >> 5]);
   if (kStats) {
     if ((threadIdx.x & 31) == 0) atomicAdd(&stats[0], c.steps);
     atomicAdd(&stats[1], c.visits);
@@ -570,6 +572,9 @@ void soup_build(gwn_soup_impl& s, const double* V, int64_t nV, const int32_t* F,
   GWN_CUDA(cudaMemcpyAsync(s.tri_index.get(), vals.get(), (size_t)n * sizeof(int32_t),
                            cudaMemcpyDeviceToDevice, st));
   s.nf.alloc((size_t)nnodes);
+  // the walk reads records with 256-bit loads
+  if (reinterpret_cast<uintptr_t>(s.nf.get()) % 32)
+    throw Error(GWN_ERR_INTERNAL, "node records are not 32-byte aligned");
   s.nd.alloc((size_t)nnodes);
   s.tf.alloc((size_t)n * 3);
   s.td.alloc((size_t)n * 9);
@@ -639,8 +644,16 @@ static void soup_eval_t(const gwn_soup_impl& s, float beta, const void* Qv, int6
     count.zero(st);
     {
       PhaseTimer ph("walk", st);
-      launch_kernel(soup_eval_mixed_kernel<QT, WT>, grid, 128, 0, st, prm, Q, perm, nQ, W, list.get(),
-                                                           count.get(), (unsigned long long*)nullptr);
+      // the tree kind is fixed per launch: the reference tree's instance
+      // carries no FP64 re-check code
+      if (prm.ref32)
+        launch_kernel(soup_eval_mixed_kernel<QT, WT, false, GWN_TREE_REFERENCE>, grid, 128, 0, st,
+                      prm, Q, perm, nQ, W, list.get(), count.get(),
+                      (unsigned long long*)nullptr);
+      else
+        launch_kernel(soup_eval_mixed_kernel<QT, WT, false, GWN_TREE_BINNED>, grid, 128, 0, st,
+                      prm, Q, perm, nQ, W, list.get(), count.get(),
+                      (unsigned long long*)nullptr);
     }
     GWN_CUDA(cudaGetLastError());
     {

@@ -18,9 +18,10 @@ namespace gwn {
 // order-2 cubic forms in the unit direction (pack_far32 below).
 // link >= 0: internal node, index one past its subtree (pre-order);
 // link < 0: leaf, triangle slot ~link.
-struct __align__(16) SoupNodeF {
+struct __align__(32) SoupNodeF {
   float4 a, b, c, d, e, f;
 };
+static_assert(sizeof(SoupNodeF) == 96, "96-byte records: a..b, c..d, e..f are 32-byte aligned");
 
 // The far field of FWNFS.h:7195-7251 with q = (x - P)/|x - P|,
 // m1 = 1/|x - P|, m2 = m1^2:

@@ -1727,6 +1727,9 @@ void soup_build_ref(gwn_soup_impl& s, const double* V, int64_t nV, const int32_t
   s.max_depth = depth;
   s.tri_index.alloc(m);
   s.nf.alloc(total_slots);
+  // the walk reads records with 256-bit loads
+  if (reinterpret_cast<uintptr_t>(s.nf.get()) % 32)
+    throw Error(GWN_ERR_INTERNAL, "node records are not 32-byte aligned");
   s.nd.alloc(total_slots);
   s.tf.alloc((size_t)m * 3);
   s.td.alloc((size_t)m * 9);

@@ -94,22 +94,19 @@ __device__ __forceinline__ T tri_solid_angle(T ax, T ay, T az, T bx, T by, T bz,
   return T(2) * g_atan2(num, den);
 }
 
-// FP32 far field of a packed record (pack_far32): omega = m2 (m1 (A(q) +
+// FP32 far field of a packed record (pack_far32; b..f its float4s): omega = m2 (m1 (A(q) +
 // m1 K(q)) - q.N) with q = (x - P) m1, (dx,dy,dz) = x - P, r2 = |x - P|^2.
-__device__ __forceinline__ float far_field32(const SoupNodeF* r, float dx, float dy, float dz,
-                                             float r2, int order) {
-  const float4 b = __ldg(&r->b);
+__device__ __forceinline__ float far_field32(float4 b, float4 c, float4 d, float4 e, float4 f,
+                                             float dx, float dy, float dz, float r2, int order) {
   const float m1 = g_rsqrt(r2), m2 = m1 * m1;
   const float qx = dx * m1, qy = dy * m1, qz = dz * m1;
   const float lin = fmaf(qx, b.x, fmaf(qy, b.y, qz * b.z));
   if (order == 0) return -m2 * lin;
-  const float4 c = __ldg(&r->c), d = __ldg(&r->d);
   const float x2 = qx * qx, y2 = qy * qy, z2 = qz * qz, yz = qy * qz;
   const float a = fmaf(qx, fmaf(b.w, qx, fmaf(c.z, qy, c.w * qz)),
                        fmaf(c.x, y2, fmaf(c.y, z2, d.x * yz)));
   float s = a;
   if (order >= 2) {
-    const float4 e = __ldg(&r->e), f = __ldg(&r->f);
     const float kx = fmaf(d.y, x2, fmaf(e.z, y2, fmaf(f.x, z2, f.z * yz)));
     const float ky = fmaf(e.x, x2, fmaf(d.z, y2, f.y * z2));
     const float kz = fmaf(e.y, x2, fmaf(e.w, y2, d.w * z2));
@@ -175,6 +172,12 @@ __device__ __forceinline__ bool ref_open32(float qx, float qy, float qz, float4 
 // q, tan(Omega/2) = A.(B x C) / (|A||B||C| + (A.B)|C| + (A.C)|B| + (B.C)|A|).
 // Equal to the normalised form of tri_solid_angle up to rounding, without
 // its nine divisions.  A corner at q or a zero determinant gives 0, as there.
+// The corner vectors, the determinant and the denominator -- where the
+// cancellation near the triangle is -- are FP64; the angle is FP32 atan2 of
+// the pair scaled by a power of two, so that the pair's rounding to FP32
+// moves it by at most 2^-24 rad besides atan2f's own error (a few 1e-7 rad):
+// FP64 atan2 would cost as much as the rest of the term at this part's FP64
+// rate.
 __device__ __forceinline__ double solid_angle_vos64(const double* __restrict__ t, double qx,
                                                     double qy, double qz) {
   const double ax = t[0] - qx, ay = t[1] - qy, az = t[2] - qz;
@@ -195,7 +198,12 @@ __device__ __forceinline__ double solid_angle_vos64(const double* __restrict__ t
   const double la = sqrt(la2), lb = sqrt(lb2), lc = sqrt(lc2);
   const double den = la * lb * lc + (ax * bx + ay * by + az * bz) * lc +
                      (ax * cx + ay * cy + az * cz) * lb + (bx * cx + by * cy + bz * cz) * la;
-  return 2.0 * atan2(det, den);
+  // s = 2^-e, e = the binary exponent of max(|det|, |den|), clamped so that
+  // s is a normal double
+  const int hi = __double2hiint(fmax(fabs(det), fabs(den)));
+  const int e = min(max(((hi >> 20) & 0x7ff) - 1023, -1022), 1022);
+  const double s = __hiloint2double((1023 - e) << 20, 0);
+  return 2.0 * (double)atan2f((float)(det * s), (float)(den * s));
 }
 
 // Per-warp queue of FP64 near-field terms (triangle slot, owning lane).
@@ -209,25 +217,26 @@ __device__ __forceinline__ double solid_angle_vos64(const double* __restrict__ t
 // read only at the rare FP64 open-test re-checks and at the flushes, and
 // the six registers they would hold cost the walk spills (9.60 -> 9.25 ms
 // per 10M-query launch with them parked here).
+// Each lane keeps the queue positions of its own terms as a bit mask and adds
+// their values (v, written by the lanes that evaluated them) in queue order.
 struct NearQueue {
   int2 e[32];
   double q[32][3];  // each lane's FP64 query
+  double v[32];     // the evaluated terms of one flush
 };
 
-__device__ __forceinline__ void flush_near64(const double* __restrict__ td, const NearQueue& q,
-                                             int n, double& acc64) {
-  const unsigned full = 0xffffffffu;
+__device__ __forceinline__ void flush_near64(const double* __restrict__ td, NearQueue& q, int n,
+                                             unsigned mine, double& acc64) {
   const int lane = threadIdx.x & 31;
   __syncwarp();
-  int2 e = make_int2(0, lane);
-  if (lane < n) e = q.e[lane];
-  const double ox = q.q[e.y][0], oy = q.q[e.y][1], oz = q.q[e.y][2];
-  double v = 0.0;
-  if (lane < n) v = solid_angle_vos64(td + (int64_t)e.x * 9, ox, oy, oz);
-  for (int k = 0; k < n; ++k) {
-    const double vk = __shfl_sync(full, v, k);
-    const int ok = __shfl_sync(full, e.y, k);
-    if (ok == lane) acc64 += vk;
+  if (lane < n) {
+    const int2 e = q.e[lane];
+    q.v[lane] = solid_angle_vos64(td + (int64_t)e.x * 9, q.q[e.y][0], q.q[e.y][1], q.q[e.y][2]);
+  }
+  __syncwarp();
+  while (mine) {
+    acc64 += q.v[__ffs(mine) - 1];
+    mine &= mine - 1;
   }
   __syncwarp();
 }
@@ -242,8 +251,10 @@ struct WalkCounters {
 // records and arithmetic; the open test is redone in FP64 inside the guard
 // band; exact triangle terms within eps of the query are taken in FP64
 // through the warp's NearQueue `nq` (shared memory).  Returns the
-// solid-angle sum as an FP32 part and an FP64 part.
-template <bool kStats>
+// solid-angle sum as an FP32 part and an FP64 part.  kTree: the tree kind
+// (GWN_TREE_REFERENCE / GWN_TREE_BINNED) when known at compile time, -1 to
+// read it from prm.ref32.
+template <bool kStats, int kTree = -1>
 __device__ __forceinline__ void walk_mixed(const EvalParams& prm, bool valid, double qx, double qy,
                                            double qz, float& acc, double& acc64,
                                            WalkCounters& c, NearQueue& nq) {
@@ -252,7 +263,9 @@ __device__ __forceinline__ void walk_mixed(const EvalParams& prm, bool valid, do
   nq.q[lane][1] = qy;
   nq.q[lane][2] = qz;
   const unsigned lt_mask = (1u << lane) - 1u;
-  int nqueued = 0;  // warp-uniform
+  int nqueued = 0;    // warp-uniform
+  unsigned mine = 0;  // this lane's queue positions
+  const bool ref = kTree < 0 ? prm.ref32 != 0 : kTree == GWN_TREE_REFERENCE;
   const float fx = (float)qx, fy = (float)qy, fz = (float)qz;
   const float S = fmaxf(fabsf(fx), fmaxf(fabsf(fy), fabsf(fz))) + prm.cmax;
   const float sigma = guard_sigma(S);
@@ -262,9 +275,15 @@ __device__ __forceinline__ void walk_mixed(const EvalParams& prm, bool valid, do
   int node = 0;
   const unsigned full = 0xffffffffu;
   while (node < prm.nnodes) {
+    // the whole record at once, in three 256-bit loads (records are 96
+    // bytes from a 32-byte aligned base): the far field's coefficients
+    // arrive with the open test's data instead of one load latency after it
     const SoupNodeF* r = prm.nf + node;
-    const float4 a = __ldg(&r->a);
-    const int link = __float_as_int(__ldg(&r->f).w);
+    float4 a, rb, rc, rd, re, rf;
+    ldg256(&r->a, a, rb);
+    ldg256(&r->c, rc, rd);
+    ldg256(&r->e, re, rf);
+    const int link = __float_as_int(rf.w);
     bool open = false;
     bool want64 = false;
     int slot64 = 0;
@@ -276,23 +295,26 @@ __device__ __forceinline__ void walk_mixed(const EvalParams& prm, bool valid, do
         open = true;
       } else {
         const float dx = fx - a.x, dy = fy - a.y, dz = fz - a.z;
-        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-        const float thr = a.w * prm.beta2f;
+        float r2;
         bool near;
-        if (prm.ref32) {
-          near = ref_open32(fx, fy, fz, a, prm.beta2f);
+        if (ref) {
+          // ref_open32's own |q - P|^2, reused by the far field below
+          r2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+          near = r2 <= __fmul_rn(a.w, prm.beta2f);
         } else {
+          r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+          const float thr = a.w * prm.beta2f;
           near = r2 <= thr;
           if (in_guard_band(r2, thr, sigma)) {
-            const SoupNodeD* rd = prm.nd + node;
-            near = open_test64(nq.q[lane][0], nq.q[lane][1], nq.q[lane][2], rd->P[0], rd->P[1],
-                               rd->P[2], rd->maxP2, prm.beta2d);
+            const SoupNodeD* r64 = prm.nd + node;
+            near = open_test64(nq.q[lane][0], nq.q[lane][1], nq.q[lane][2], r64->P[0],
+                               r64->P[1], r64->P[2], r64->maxP2, prm.beta2d);
             if (kStats) ++c.recheck;
           }
         }
         if (!near) {
           if (kStats) ++c.far;
-          const float om = far_field32(r, dx, dy, dz, r2, prm.order);
+          const float om = far_field32(rb, rc, rd, re, rf, dx, dy, dz, r2, prm.order);
           if (isfinite(om)) {
             acc += om;
             resume = leaf ? node + 1 : link;
@@ -327,17 +349,22 @@ __device__ __forceinline__ void walk_mixed(const EvalParams& prm, bool valid, do
     if (m64) {
       const int k = __popc(m64);
       if (nqueued + k > 32) {
-        flush_near64(prm.td, nq, nqueued, acc64);
+        flush_near64(prm.td, nq, nqueued, mine, acc64);
         nqueued = 0;
+        mine = 0;
       }
-      if (want64) nq.e[nqueued + __popc(m64 & lt_mask)] = make_int2(slot64, lane);
+      if (want64) {
+        const int pos = nqueued + __popc(m64 & lt_mask);
+        nq.e[pos] = make_int2(slot64, lane);
+        mine |= 1u << pos;
+      }
       nqueued += k;
     }
     // a lane that opens the node wants node + 1, every other lane is past
     // the node (resume > node): the warp goes to the smallest of them
     node = __reduce_min_sync(full, open ? node + 1 : resume);
   }
-  if (nqueued) flush_near64(prm.td, nq, nqueued, acc64);
+  if (nqueued) flush_near64(prm.td, nq, nqueued, mine, acc64);
 }
 
 // Winding number from the two parts of walk_mixed.
