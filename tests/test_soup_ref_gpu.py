@@ -142,3 +142,21 @@ def test_closest_triangle_on_a_reference_handle(cuda):
     for i in range(0, Q.shape[0], 97):
         Dd, _, _ = O.squared_distance(V, F[[Ir[i]]], Q[[i]])
         assert abs(Dd[0] - Dr[i]) <= 1e-12 * max(1.0, float(Dr[i]))
+
+
+def test_host_buffers_equal_the_device_call(cuda):
+    """A 4.5M-query host-buffer call (staged copies in and out) equals the
+    device-buffer call exactly, in both precisions and for FP32 queries."""
+    torch = cuda
+    V, F = synth.soup_mesh(seed=1, subdiv=5)
+    rng = np.random.default_rng(4)
+    Q = rng.uniform(-1.5, 1.5, (4_500_001, 3))
+    bvh = G.FastWindingNumberBVH(V, F, order=2)
+    for prec in ("mixed", "fp64"):
+        Wh = bvh.eval(Q, 2.0, precision=prec)
+        Wd = bvh.eval(torch.from_numpy(Q).cuda(), 2.0, precision=prec).cpu().numpy()
+        assert np.array_equal(Wh, Wd), prec
+    Wh32 = bvh.eval(Q.astype(np.float32), 2.0, precision="mixed")
+    Wd32 = bvh.eval(torch.from_numpy(Q.astype(np.float32)).cuda(), 2.0,
+                    precision="mixed").cpu().numpy()
+    assert np.array_equal(Wh32, Wd32)
