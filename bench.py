@@ -166,6 +166,36 @@ def ncu_traffic(name: str):
     return None
 
 
+# FP32 operations of the mixed walk (a fused multiply-add counts 2): the
+# reference's open test |q - P|^2 <= maxP2 beta^2 (3 sub, 4 mul, 2 add), the
+# packed order-2 far field (soup.cuh pack_far32: rsqrt, 27 mul/add, 13 fma,
+# the sum), one FP32 exact triangle term (corner vectors, normalisation,
+# triple product, denominator, atan2f).
+FLOPS_OPEN_TEST = 9
+FLOPS_FAR_FIELD = 54
+FLOPS_EXACT_TRI = 100
+
+
+def walk_compute(bvh, dQ, nq, walk_ms, clocks, peaks):
+    """Compute side of the walk's roofline: FP32 FLOPs per query from the
+    instrumented walk's counters over the same queries, achieved FLOP/s in
+    the timed launches, against the nominal FP32 rate at the sampled clock
+    (152 SMs x 128 lanes x 2 x MHz; no measured FP32 peak exists)."""
+    c = bvh.walk_stats(dQ, 2.0)
+    per_q = {k: c[k] / nq for k in ("node_visits", "far_field", "exact_fp32", "exact_fp64_near")}
+    flops_q = (per_q["node_visits"] * FLOPS_OPEN_TEST + per_q["far_field"] * FLOPS_FAR_FIELD
+               + per_q["exact_fp32"] * FLOPS_EXACT_TRI)
+    mhz = (clocks or {}).get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+    peak = 152 * 128 * 2 * mhz * 1e6 / 1e12
+    achieved = flops_q * nq / (walk_ms / 1e3) / 1e12
+    warps = (nq + 31) // 32
+    return {"unit": "TFLOP/s", "achieved": achieved, "peak": peak, "frac": achieved / peak,
+            "peak_source": f"nominal FP32 at the sampled {mhz:.0f} MHz",
+            "flops_per_query": flops_q, "per_query": per_q,
+            "warp_steps_per_warp": c["warp_steps"] / warps,
+            "lane_utilisation": c["node_visits"] / max(1, c["warp_steps"] * 32)}
+
+
 def make_workload(args, rank):
     from libigl_gb300 import synth
     V, F = synth.soup_mesh(seed=1, subdiv=args.subdiv)
@@ -1149,7 +1179,8 @@ def main():
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
                 "peak_source": peak_kind, "kernel": "soup_eval_mixed_kernel",
-                "kernel_ms": walk, "kernel_share_of_step": walk / ms_per_step}
+                "kernel_ms": walk, "kernel_share_of_step": walk / ms_per_step,
+                "compute": walk_compute(bvh, dQ, nq, walk, clocks, peaks)}
 
     cpu = None
     vs_reference = None

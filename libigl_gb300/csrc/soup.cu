@@ -428,16 +428,6 @@ __global__ void emit_kernel(const BuildM* __restrict__ M, const int32_t* __restr
   }
 }
 
-template <typename QT>
-__device__ __forceinline__ void read_query(const QT* Q, const int32_t* perm, const int32_t* list,
-                                           int64_t i, int64_t& qi, double& x, double& y,
-                                           double& z) {
-  qi = list ? (int64_t)list[i] : (perm ? (int64_t)perm[i] : i);
-  x = (double)Q[qi * 3 + 0];
-  y = (double)Q[qi * 3 + 1];
-  z = (double)Q[qi * 3 + 2];
-}
-
 // --------------------------------------------------------------- evaluate --
 // Mixed-precision warp-coherent walk.  One query per lane.  kStats builds
 // an instrumented copy that counts its work into `stats` (see
@@ -453,7 +443,7 @@ __global__ void __launch_bounds__(128, 8) soup_eval_mixed_kernel(EvalParams prm,
   const bool valid = i < nQ;
   int64_t qi = 0;
   double qx = 0, qy = 0, qz = 0;
-  if (valid) read_query(Q, perm, (const int32_t*)nullptr, i, qi, qx, qy, qz);
+  if (valid) soupwalk::read_query(Q, perm, (const int32_t*)nullptr, i, qi, qx, qy, qz);
   __shared__ soupwalk::NearQueue near_q[4];
   float acc;
   double acc64;
@@ -470,7 +460,7 @@ __global__ void __launch_bounds__(128, 8) soup_eval_mixed_kernel(EvalParams prm,
   }
   if (!valid) return;
   const double w = soupwalk::mixed_result(acc, acc64);
-  W[qi] = (WT)w;
+  __stcs(&W[qi], (WT)w);  // written once, read by no later warp: evict first
   if (fabs(w - 0.5) <= kBand) {
     const unsigned s = atomicAdd(refine_count, 1u);
     refine_list[s] = (int32_t)qi;
@@ -490,7 +480,7 @@ __global__ void __launch_bounds__(128) soup_eval_fp64_kernel(EvalParams prm, con
   const bool valid = i < n;
   int64_t qi = 0;
   double qx = 0, qy = 0, qz = 0;
-  if (valid) read_query(Q, perm, list, i, qi, qx, qy, qz);
+  if (valid) soupwalk::read_query(Q, perm, list, i, qi, qx, qy, qz);
   const double acc = soupwalk::walk_fp64(prm, valid, qx, qy, qz);
   if (valid) W[qi] = (WT)(acc * kInv4Pi);
 }
@@ -646,14 +636,10 @@ static void soup_eval_t(const gwn_soup_impl& s, float beta, const void* Qv, int6
       PhaseTimer ph("walk", st);
       // the tree kind is fixed per launch: the reference tree's instance
       // carries no FP64 re-check code
-      if (prm.ref32)
-        launch_kernel(soup_eval_mixed_kernel<QT, WT, false, GWN_TREE_REFERENCE>, grid, 128, 0, st,
-                      prm, Q, perm, nQ, W, list.get(), count.get(),
-                      (unsigned long long*)nullptr);
-      else
-        launch_kernel(soup_eval_mixed_kernel<QT, WT, false, GWN_TREE_BINNED>, grid, 128, 0, st,
-                      prm, Q, perm, nQ, W, list.get(), count.get(),
-                      (unsigned long long*)nullptr);
+      auto kernel = prm.ref32 ? soup_eval_mixed_kernel<QT, WT, false, GWN_TREE_REFERENCE>
+                              : soup_eval_mixed_kernel<QT, WT, false, GWN_TREE_BINNED>;
+      launch_kernel(kernel, grid, 128, 0, st, prm, Q, perm, nQ, W, list.get(), count.get(),
+                    (unsigned long long*)nullptr);
     }
     GWN_CUDA(cudaGetLastError());
     {

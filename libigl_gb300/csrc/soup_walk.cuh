@@ -130,14 +130,17 @@ __device__ __forceinline__ Far<double> load_far(const SoupNodeD* r) {
   return m;
 }
 
+// Query i of a launch (through the spatial order perm, or a re-evaluation
+// list).  Streaming loads: each query is read once, so its cache lines go
+// first and L2 keeps the node records the walks share.
 template <typename QT>
 __device__ __forceinline__ void read_query(const QT* Q, const int32_t* perm, const int32_t* list,
                                            int64_t i, int64_t& qi, double& x, double& y,
                                            double& z) {
-  qi = list ? (int64_t)list[i] : (perm ? (int64_t)perm[i] : i);
-  x = (double)Q[qi * 3 + 0];
-  y = (double)Q[qi * 3 + 1];
-  z = (double)Q[qi * 3 + 2];
+  qi = list ? (int64_t)__ldcs(list + i) : (perm ? (int64_t)__ldcs(perm + i) : i);
+  x = (double)__ldcs(Q + qi * 3 + 0);
+  y = (double)__ldcs(Q + qi * 3 + 1);
+  z = (double)__ldcs(Q + qi * 3 + 2);
 }
 
 struct EvalParams {
