@@ -717,12 +717,76 @@ __global__ void __launch_bounds__(kT, 4) hier_walk_kernel(HierDev H, const QT* _
   if (fabs(w - 0.5) <= kBand) redo[atomicAdd(nredo, 1u)] = (int32_t)q;
 }
 
+// Per-warp queue of the plain FP64 walk's triangle terms.  Every leaf and
+// cap triangle a lane needs is appended as (triangle, lane): triangle >= 0 a
+// cap triangle (caps64), < 0 the leaf ~triangle (tris64).  Whenever 32 are
+// queued (and at the end) the warp evaluates them, one per lane, so each
+// FP64 instruction serves the whole warp instead of the lanes that happen to
+// leave a node at the same step (a warp instruction costs the narrow FP64
+// pipe the same with 1 or 32 lanes).  A lane adds its own values by its bit
+// mask of queue positions, in queue order, which is its walk order: its sum
+// is the one it would form alone.
+struct Hier64Queue {
+  int2 e[32];
+  double q[32][3];  // each lane's query
+  double v[32];     // the values of one flush
+};
+
+__device__ __forceinline__ void flush_queue64(const HierDev& H, Hier64Queue& hq, int n,
+                                              unsigned mine, double& acc) {
+  const int lane = threadIdx.x & 31;
+  __syncwarp();
+  if (lane < n) {
+    const int2 e = hq.e[lane];
+    const double* t = e.x >= 0 ? H.caps64 + (int64_t)e.x * 9 : H.tris64 + (int64_t)(~e.x) * 9;
+    hq.v[lane] = tri64_term(t, hq.q[e.y][0], hq.q[e.y][1], hq.q[e.y][2]);
+  }
+  __syncwarp();
+  while (mine) {
+    acc += hq.v[__ffs(mine) - 1];
+    mine &= mine - 1;
+  }
+  __syncwarp();
+}
+
+// Appends cnt terms of this lane (tri, tri + 1, ... for a cap; the single
+// leaf ~slot when tri < 0) after the lower lanes' terms of this step,
+// flushing every time the queue fills.  All 32 lanes call it together.
+__device__ __forceinline__ void enqueue64(const HierDev& H, Hier64Queue& hq, int cnt, int tri,
+                                          int& nq, unsigned& mine, double& acc) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  int incl = cnt;
+  for (int d = 1; d < 32; d <<= 1) {
+    const int y = __shfl_up_sync(full, incl, d);
+    if (lane >= d) incl += y;
+  }
+  const int total = __shfl_sync(full, incl, 31);
+  const int excl = incl - cnt;
+  for (int done = 0; done < total;) {
+    const int take = min(32 - nq, total - done);
+    const int k0 = max(0, done - excl), k1 = min(cnt, done + take - excl);
+    for (int k = k0; k < k1; ++k) {
+      const int pos = nq + excl + k - done;
+      hq.e[pos] = make_int2(tri >= 0 ? tri + k : tri, lane);
+      mine |= 1u << pos;
+    }
+    nq += take;
+    done += take;
+    if (nq == 32) {
+      flush_queue64(H, hq, 32, mine, acc);
+      nq = 0;
+      mine = 0;
+    }
+  }
+}
+
 // Plain FP64 walk, the reference's (WindingNumberTree.h:261-336): a node's
 // cap for a point strictly outside its FP64 box (the conservative test of
 // WindingNumberAABB.h:253-268) when the cap has fewer triangles than the
 // node, else its children; leaf and cap triangles in FP64 with the
-// reference's formula (solid_angle.cpp:16-54).  Same warp walk, subtree
-// split and partial sums as hier_walk_kernel.
+// reference's formula (solid_angle.cpp:16-54), through the warp's queue.
+// Same warp walk, subtree split and partial sums as hier_walk_kernel.
 __global__ void __launch_bounds__(kT, 4) hier_walk64_kernel(HierDev H, const double* __restrict__ Q,
                                                          int64_t nQ,
                                                          const int32_t* __restrict__ perm,
@@ -742,40 +806,52 @@ __global__ void __launch_bounds__(kT, 4) hier_walk64_kernel(HierDev H, const dou
   const int64_t q = valid ? (perm ? perm[i] : i) : 0;
   const double px = valid ? Q[q * 3] : 0.0, py = valid ? Q[q * 3 + 1] : 0.0,
                pz = valid ? Q[q * 3 + 2] : 0.0;
+  __shared__ Hier64Queue hqs[kT / 32];
+  Hier64Queue& hq = hqs[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  hq.q[lane][0] = px;
+  hq.q[lane][1] = py;
+  hq.q[lane][2] = pz;
   auto outside = [&](int x) {
     const double* b = H.box64 + (int64_t)x * 6;
     return px < b[0] || px > b[3] || py < b[1] || py > b[4] || pz < b[2] || pz > b[5];
   };
-  auto add_cap = [&](int meta, int cn, double& acc) {
-    for (int k = 0; k < cn; ++k) acc += tri64_term(H.caps64 + ((int64_t)meta + k) * 9, px, py, pz);
-  };
   double acc = 0.0;
+  int nq = 0;         // warp-uniform
+  unsigned mine = 0;  // this lane's queue positions
   int resume = valid ? x0 : 0x7fffffff;
-  if (ranges && valid) {
+  if (ranges) {
     // outside the root's box: the root's cap alone, in subtree 0
     const int meta0 = __float_as_int(H.nodes[0].hi.w);
-    if (meta0 >= 0 && outside(0)) {
-      if (blockIdx.y == 0) add_cap(meta0, H.capn[0], acc);
+    int cnt = 0;
+    if (valid && meta0 >= 0 && outside(0)) {
+      if (blockIdx.y == 0) cnt = H.capn[0];
       resume = 0x7fffffff;
     }
+    enqueue64(H, hq, cnt, meta0, nq, mine, acc);
   }
   int x = x0;
   while (x < x1) {
+    int cnt = 0, tri = 0;
     if (x >= resume) {
       const NodeH nd = H.nodes[x];
       const int meta = __float_as_int(nd.hi.w);
       if (meta <= -2) {
-        acc += tri64_term(H.tris64 + (int64_t)(-2 - meta) * 9, px, py, pz);
+        cnt = 1;
+        tri = ~(-2 - meta);
         resume = x + 1;
       } else if (meta >= 0 && outside(x)) {
-        add_cap(meta, H.capn[x], acc);
+        cnt = H.capn[x];
+        tri = meta;
         resume = __float_as_int(nd.lo.w);
       } else {
         resume = x + 1;
       }
     }
+    if (__any_sync(0xffffffffu, cnt > 0)) enqueue64(H, hq, cnt, tri, nq, mine, acc);
     x = __reduce_min_sync(0xffffffffu, resume);
   }
+  if (nq) flush_queue64(H, hq, nq, mine, acc);
   if (!valid) return;
   if (part) {
     part[(int64_t)blockIdx.y * nQ + q] = acc;
