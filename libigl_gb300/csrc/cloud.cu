@@ -395,6 +395,57 @@ __device__ __forceinline__ float near_radius2(double area, double eps, double cm
   return (float)(r * r * 1.0001);
 }
 
+// expansion_eval (fast_winding_number.cpp:174-228) with loc = CM - q = r u,
+// |u| = 1, and E1(u,v) = EC[3 + u + 3v], E2(i,u,v) = EC[12 + 9i + u + 3v]:
+//   4 pi W = (u.EC[0..2]) / r^2
+//          + sum_uv E1(u,v) (delta_uv - 3 u_u u_v) / r^3
+//          + sum_iuv E2(i,u,v) (15 u_i u_u u_v - 3 (delta_uv u_i + delta_ui u_v
+//                                                  + delta_vi u_u)) / r^4.
+// With |u|^2 = 1 the second bracket is the quadratic form
+// Q(u) = sum_uv (tr E1 delta_uv - 3 E1(u,v)) u_u u_v and the third the cubic
+// form K(u) = 15 sum E2(i,u,v) u_i u_u u_v - 3 (u.w) |u|^2, with
+// w_k = sum_j E2(k,j,j) + E2(j,j,k) + E2(j,k,j).  Both are harmonic (their
+// Laplacians vanish identically), so Q_zz = -Q_xx - Q_yy and
+// K_xzz = -3 K_xxx - K_xyy, K_yzz = -3 K_yyy - K_xxy, K_zzz = -(K_xxz + K_yyz) / 3,
+// and the record keeps 3 + 5 + 7 coefficients (monomial coefficients, 1/(4 pi)
+// folded in), formed in FP64 and rounded once.
+__device__ void pack_cloud32(CloudNodeF& R, const double* ec, int num_terms) {
+  const double s = 1.0 / kPi4;
+  double q[5] = {0, 0, 0, 0, 0};  // xx, yy, xy, xz, yz
+  double k[7] = {0, 0, 0, 0, 0, 0, 0};  // xxx, yyy, xxy, xxz, xyy, yyz, xyz
+  if (num_terms > 3) {
+    auto E1 = [&](int u, int v) { return ec[3 + u + 3 * v]; };
+    const double tr = E1(0, 0) + E1(1, 1) + E1(2, 2);
+    q[0] = (tr - 3 * E1(0, 0)) * s;
+    q[1] = (tr - 3 * E1(1, 1)) * s;
+    q[2] = -3 * (E1(0, 1) + E1(1, 0)) * s;
+    q[3] = -3 * (E1(0, 2) + E1(2, 0)) * s;
+    q[4] = -3 * (E1(1, 2) + E1(2, 1)) * s;
+  }
+  if (num_terms > 12) {
+    auto E2 = [&](int i, int u, int v) { return ec[12 + 9 * i + u + 3 * v]; };
+    double w[3];
+    for (int a = 0; a < 3; ++a) {
+      w[a] = 0;
+      for (int j = 0; j < 3; ++j) w[a] += E2(a, j, j) + E2(j, j, a) + E2(j, a, j);
+    }
+    // sum of E2 over the distinct orderings of {a, a, b}
+    auto S2 = [&](int a, int b) { return E2(a, a, b) + E2(a, b, a) + E2(b, a, a); };
+    k[0] = (15 * E2(0, 0, 0) - 3 * w[0]) * s;
+    k[1] = (15 * E2(1, 1, 1) - 3 * w[1]) * s;
+    k[2] = (15 * S2(0, 1) - 3 * w[1]) * s;  // u_x^2 u_y
+    k[3] = (15 * S2(0, 2) - 3 * w[2]) * s;  // u_x^2 u_z
+    k[4] = (15 * S2(1, 0) - 3 * w[0]) * s;  // u_y^2 u_x
+    k[5] = (15 * S2(1, 2) - 3 * w[2]) * s;  // u_y^2 u_z
+    k[6] = 15 * (E2(0, 1, 2) + E2(0, 2, 1) + E2(1, 0, 2) + E2(1, 2, 0) + E2(2, 0, 1) +
+                 E2(2, 1, 0)) * s;          // u_x u_y u_z
+  }
+  R.b = make_float4((float)(ec[0] * s), (float)(ec[1] * s), (float)(ec[2] * s), (float)q[0]);
+  R.c = make_float4((float)q[1], (float)q[2], (float)q[3], (float)q[4]);
+  R.d = make_float4((float)k[0], (float)k[1], (float)k[2], (float)k[3]);
+  R.e = make_float4((float)k[4], (float)k[5], (float)k[6], 0.f);
+}
+
 __global__ void emit_nodes_kernel(LayoutIn in, CloudNodeF* __restrict__ nf,
                                   CloudNodeD* __restrict__ nd) {
   const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -418,10 +469,8 @@ __global__ void emit_nodes_kernel(LayoutIn in, CloudNodeF* __restrict__ nf,
   nd[p] = D;
   CloudNodeF Fr;
   Fr.a = make_float4((float)D.cm[0], (float)D.cm[1], (float)D.cm[2], (float)D.r);
-  float e[40];
-  for (int k = 0; k < 39; ++k) e[k] = (float)D.ec[k];
-  e[39] = near_radius2(in.area[c], in.eps, in.cmax);
-  for (int k = 0; k < 10; ++k) Fr.e[k] = make_float4(e[4 * k], e[4 * k + 1], e[4 * k + 2], e[4 * k + 3]);
+  pack_cloud32(Fr, D.ec, in.num_terms);
+  Fr.e.w = near_radius2(in.area[c], in.eps, in.cmax);
   Fr.l = D.l;
   nf[p] = Fr;
 }
@@ -497,50 +546,27 @@ __device__ __forceinline__ T expansion(const T* ec, T lx, T ly, T lz, T r, int n
   return wn;
 }
 
-// The FP32 form of expansion<float> for the mixed walk: the same terms with
-// one reciprocal square root in place of its divisions (c3 = 1/(4 pi r^3),
-// c5 = c3 / r^2, c7 = c5 / r^2).
-__device__ __forceinline__ float expansion_f32(const float* ec, float lx, float ly, float lz,
-                                               float r2, int num_terms) {
-  const float ir = rsqrtf(r2);
-  const float ir2 = ir * ir;
-  const float c3 = ir2 * ir * kInvPi4F;
-  float wn = (lx * ec[0] + ly * ec[1] + lz * ec[2]) * c3;
-  if (num_terms > 3) {
-    const float c5 = c3 * ir2;
-    const float s = -3.f * c5;
-    const float l[3] = {lx, ly, lz};
-    float acc = 0.f;
-#pragma unroll
-    for (int v = 0; v < 3; ++v)
-#pragma unroll
-      for (int u = 0; u < 3; ++u) {
-        float sd = (l[u] * l[v]) * s;
-        if (u == v) sd += c3;
-        acc += sd * ec[3 + u + 3 * v];
-      }
-    wn += acc;
-    if (num_terms > 12) {
-      const float c7 = c5 * ir2;
-#pragma unroll
-      for (int i = 0; i < 3; ++i) {
-        float acc3 = 0.f;
-#pragma unroll
-        for (int v = 0; v < 3; ++v)
-#pragma unroll
-          for (int u = 0; u < 3; ++u) {
-            float rcd = 0.f;
-            if (u == v) rcd += l[i];
-            if (u == i) rcd += l[v];
-            if (v == i) rcd += l[u];
-            const float ltl = l[u] * l[v] * c7;
-            acc3 += (15.f * l[i] * ltl + s * rcd) * ec[12 + i * 9 + u + 3 * v];
-          }
-        wn += acc3;
-      }
-    }
+// FP32 expansion from a packed record (pack_cloud32): loc = CM - q,
+// r2 = |loc|^2; W = (u.N + (Q(u) + K(u)/r)/r) / r^2 with u = loc/r.
+__device__ __forceinline__ float expansion_packed32(float4 b, float4 c, float4 d, float4 e,
+                                                    float lx, float ly, float lz, float r2,
+                                                    int num_terms) {
+  const float ir = rsqrtf(r2), ir2 = ir * ir;
+  const float ux = lx * ir, uy = ly * ir, uz = lz * ir;
+  const float lin = fmaf(ux, b.x, fmaf(uy, b.y, uz * b.z));
+  if (num_terms <= 3) return ir2 * lin;
+  const float x2 = ux * ux, y2 = uy * uy, z2 = uz * uz, yz = uy * uz;
+  const float qzz = -(b.w + c.x);
+  float s = fmaf(ux, fmaf(b.w, ux, fmaf(c.y, uy, c.z * uz)), fmaf(c.x, y2, fmaf(qzz, z2, c.w * yz)));
+  if (num_terms > 12) {
+    const float kxzz = -fmaf(3.f, d.x, e.x), kyzz = -fmaf(3.f, d.y, d.z);
+    const float kzzz = -(d.w + e.y) * (1.f / 3.f);
+    const float kx = fmaf(d.x, x2, fmaf(e.x, y2, fmaf(kxzz, z2, e.z * yz)));
+    const float ky = fmaf(d.z, x2, fmaf(d.y, y2, kyzz * z2));
+    const float kz = fmaf(d.w, x2, fmaf(e.y, y2, kzzz * z2));
+    s = fmaf(ir, fmaf(ux, kx, fmaf(uy, ky, uz * kz)), s);
   }
-  return wn;
+  return ir2 * fmaf(ir, s, lin);
 }
 
 // The reference's test `|CM - q| > beta R` (:265-266), FP64, pinned order.
@@ -658,8 +684,15 @@ __global__ void __launch_bounds__(128, 8) cloud_eval_mixed_kernel(CloudEvalParam
   int node = 0;
   const unsigned full = 0xffffffffu;
   while (node < prm.nnodes) {
+    // the whole record in three 256-bit loads (96-byte records, 32-byte
+    // aligned base)
     const CloudNodeF* r = prm.nf + node;
-    const int4 l = __ldg(&r->l);
+    float4 a, rb, rc, rd, re, lf;
+    ldg256(&r->a, a, rb);
+    ldg256(&r->c, rc, rd);
+    ldg256(&r->e, re, lf);
+    const int4 l = make_int4(__float_as_int(lf.x), __float_as_int(lf.y), __float_as_int(lf.z),
+                             __float_as_int(lf.w));
     const bool visit = node >= resume;
     bool open = false;
     if (l.w != 0) {  // leaf (the node, hence the branch, is warp-uniform)
@@ -686,7 +719,6 @@ __global__ void __launch_bounds__(128, 8) cloud_eval_mixed_kernel(CloudEvalParam
     } else {
       bool want = false;
       if (visit) {
-        const float4 a = __ldg(&r->a);
         const float dx = a.x - fx, dy = a.y - fy, dz = a.z - fz;
         const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
         const float br = prm.beta_f * a.w;
@@ -697,20 +729,10 @@ __global__ void __launch_bounds__(128, 8) cloud_eval_mixed_kernel(CloudEvalParam
           far = far64(nq.q[lane][0], nq.q[lane][1], nq.q[lane][2], rd->cm, rd->r, prm.beta);
         }
         if (far) {
-          const float rn2 = __ldg(&r->e[9]).w;
-          if (r2 <= rn2) {  // strong expansion close to the query: FP64
+          if (r2 <= re.w) {  // strong expansion close to the query: FP64
             want = true;
           } else {
-            float ec[40];
-#pragma unroll
-            for (int k = 0; k < 10; ++k) {
-              const float4 e = __ldg(&r->e[k]);
-              ec[4 * k] = e.x;
-              ec[4 * k + 1] = e.y;
-              ec[4 * k + 2] = e.z;
-              ec[4 * k + 3] = e.w;
-            }
-            acc += expansion_f32(ec, dx, dy, dz, r2, prm.num_terms);
+            acc += expansion_packed32(rb, rc, rd, re, dx, dy, dz, r2, prm.num_terms);
           }
           resume = l.x;
         } else {
@@ -1022,6 +1044,9 @@ void cloud_build(gwn_cloud_impl& c, const gwn_octree_impl& t, const double* N, c
   }
   c.nnodes = nnodes;
   c.nf.alloc((size_t)std::max<int64_t>(nnodes, 1));
+  // the walk reads records with 256-bit loads
+  if (reinterpret_cast<uintptr_t>(c.nf.get()) % 32)
+    throw Error(GWN_ERR_INTERNAL, "cloud records are not 32-byte aligned");
   c.nd.alloc((size_t)std::max<int64_t>(nnodes, 1));
   finish_extent(c, st);
   LayoutIn in{val.get(), nullptr, nullptr, key.get(), nnodes, t.start.get(), t.count.get(), t.ch.get(),
@@ -1120,6 +1145,9 @@ void cloud_build_arrays(gwn_cloud_impl& c, const double* P, const double* N, con
   slot_d.upload(slot_point.data(), (size_t)nslots, st);
   for (int32_t sp : slot_point) GWN_REQUIRE(sp >= 0 && sp < nP, "point index out of range");
   c.nf.alloc((size_t)std::max<int64_t>(nnodes, 1));
+  // the walk reads records with 256-bit loads
+  if (reinterpret_cast<uintptr_t>(c.nf.get()) % 32)
+    throw Error(GWN_ERR_INTERNAL, "cloud records are not 32-byte aligned");
   c.nd.alloc((size_t)std::max<int64_t>(nnodes, 1));
   DevBuf<int64_t> start_d((size_t)ncells, st);
   GWN_CUDA(cudaMemcpyAsync(start_d.get(), pi_off_d, (size_t)ncells * 8, cudaMemcpyDeviceToDevice, st));

@@ -9,14 +9,20 @@
 
 namespace gwn {
 
-// 192-byte FP32 traversal record.
-//   a: CM xyz, R        e[0..9]: EC[0..38], then the squared FP64 near-field radius
+// 96-byte FP32 traversal record, 32-byte aligned (read as three 256-bit loads):
+//   a: CM xyz, R
+//   b: N xyz, Q_xx     c: Q_yy, Q_xy, Q_xz, Q_yz
+//   d: K_xxx, K_yyy, K_xxy, K_xxz     e: K_xyy, K_yyz, K_xyz, squared FP64 near-field radius
 //   l: skip (one past subtree), first point slot, point count, leaf flag
-struct __align__(16) CloudNodeF {
-  float4 a;
-  float4 e[10];
+// N, Q, K: the expansion of the cell in the unit direction u = (CM - q)/r,
+// W = (u.N + Q(u)/r + K(u)/r^2) / r^2, with Q and K harmonic (Q_zz and
+// K_xzz, K_yzz, K_zzz follow from the others); formed by pack_cloud32
+// (cloud.cu) from EC.
+struct __align__(32) CloudNodeF {
+  float4 a, b, c, d, e;
   int4 l;
 };
+static_assert(sizeof(CloudNodeF) == 96, "three 32-byte halves per record");
 
 // FP64 traversal record.
 struct __align__(16) CloudNodeD {
