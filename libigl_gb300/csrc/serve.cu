@@ -170,7 +170,11 @@ __global__ void __launch_bounds__(128, 8) serve_walk_kernel(ServeHeader* __restr
                                                          double* __restrict__ dW,
                                                          int2* __restrict__ refine,
                                                          unsigned* __restrict__ counters) {
-  __shared__ soupwalk::NearQueue near_q[4];
+  // a warp walks either precision at a time: the two queues share memory
+  __shared__ union WarpQueue {
+    soupwalk::NearQueue near;
+    soupwalk::Fp64Queue fp64;
+  } warp_q[4];
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const uint32_t na = dh->n_aligned;
@@ -211,14 +215,16 @@ __global__ void __launch_bounds__(128, 8) serve_walk_kernel(ServeHeader* __restr
       float acc;
       double acc64;
       soupwalk::WalkCounters c;
-      soupwalk::walk_mixed<false>(prm, valid, qx, qy, qz, acc, acc64, c, near_q[threadIdx.x >> 5]);
+      soupwalk::walk_mixed<false>(prm, valid, qx, qy, qz, acc, acc64, c,
+                                  warp_q[threadIdx.x >> 5].near);
       w = soupwalk::mixed_result(acc, acc64);
       if (valid && fabs(w - 0.5) <= soupwalk::kBand) {
         const unsigned s = atomicAdd(&counters[1], 1u);
         refine[s] = make_int2(r, j);
       }
     } else {
-      w = soupwalk::walk_fp64(prm, valid, qx, qy, qz) * soupwalk::kInv4Pi;
+      w = soupwalk::walk_fp64(prm, valid, qx, qy, qz, warp_q[threadIdx.x >> 5].fp64) *
+          soupwalk::kInv4Pi;
     }
     if (valid) dW[R.out_off + j] = w;
   }
@@ -670,6 +676,7 @@ bool gwn_server::form_and_launch(SrvSlot& s, std::unique_lock<std::mutex>& lk) {
     d.prm.cmax = (float)t.cmax;
     d.prm.status = nullptr;
     d.prm.ref32 = t.tree == GWN_TREE_REFERENCE;
+    d.prm.fp64_queue = t.moments_bounded;
     for (int k = 0; k < 3; ++k) {
       // the query box: the mesh box grown by a quarter on each side
       const double e = std::max(t.hi[k] - t.lo[k], 1e-30);

@@ -481,8 +481,20 @@ __global__ void __launch_bounds__(128) soup_eval_fp64_kernel(EvalParams prm, con
   int64_t qi = 0;
   double qx = 0, qy = 0, qz = 0;
   if (valid) soupwalk::read_query(Q, perm, list, i, qi, qx, qy, qz);
-  const double acc = soupwalk::walk_fp64(prm, valid, qx, qy, qz);
+  __shared__ soupwalk::Fp64Queue fp64_q[4];
+  const double acc = soupwalk::walk_fp64(prm, valid, qx, qy, qz, fp64_q[threadIdx.x >> 5]);
   if (valid) W[qi] = (WT)(acc * kInv4Pi);
+}
+
+__global__ void moments_bounded_kernel(const SoupNodeD* __restrict__ nd, int64_t n,
+                                       unsigned* __restrict__ unbounded) {
+  const int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  bool bad = false;
+  if (x < n) {
+    const double* m = nd[x].N;  // N .. c2: the 19 moments after P, maxP2
+    for (int k = 0; k < 19; ++k) bad |= !(fabs(m[k]) <= 1e100);
+  }
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(unbounded, 1u);
 }
 
 template <typename WT>
@@ -494,6 +506,22 @@ __global__ void fill_zero_kernel(WT* w, int64_t n) {
 }  // namespace
 
 // ------------------------------------------------------------------ build --
+void soup_check_moments(gwn_soup_impl& s, cudaStream_t st) {
+  s.moments_bounded = true;
+  if (s.nnodes == 0) return;
+  static_assert(offsetof(SoupNodeD, c2) + 6 * sizeof(double) - offsetof(SoupNodeD, N) ==
+                    19 * sizeof(double),
+                "the 19 moments are contiguous");
+  DevBuf<unsigned> flag(1, st);
+  flag.zero(st);
+  launch_kernel(moments_bounded_kernel, (unsigned)((s.nnodes + 255) / 256), 256, 0, st,
+                (const SoupNodeD*)s.nd.get(), s.nnodes, flag.get());
+  unsigned h = 0;
+  GWN_CUDA(cudaMemcpyAsync(&h, flag.get(), sizeof(h), cudaMemcpyDeviceToHost, st));
+  GWN_CUDA(cudaStreamSynchronize(st));
+  s.moments_bounded = h == 0;
+}
+
 void soup_build(gwn_soup_impl& s, const double* V, int64_t nV, const int32_t* F, int64_t nF,
                 int order, bool host_mode, cudaStream_t st) {
   GWN_REQUIRE(order >= 0 && order <= 2, "order must be 0, 1 or 2");
@@ -592,6 +620,7 @@ void soup_build(gwn_soup_impl& s, const double* V, int64_t nV, const int32_t* F,
   }
   s.eps = kNearFrac * sqrt(diag2);
   s.cmax = cmax;
+  soup_check_moments(s, st);
   s.bytes = s.nf.bytes() + s.nd.bytes() + s.tf.bytes() + s.td.bytes() + s.tri_index.bytes() +
             s.snode.bytes();
 }
@@ -621,6 +650,7 @@ static void soup_eval_t(const gwn_soup_impl& s, float beta, const void* Qv, int6
   prm.cmax = (float)s.cmax;
   prm.status = nullptr;
   prm.ref32 = s.tree == GWN_TREE_REFERENCE;
+  prm.fp64_queue = s.moments_bounded;
   QueryOrder qo;
   {
     PhaseTimer ph("order_queries", st);
@@ -672,6 +702,7 @@ void soup_walk_stats(const gwn_soup_impl& s, float beta, const double* Q, int64_
   prm.cmax = (float)s.cmax;
   prm.status = nullptr;
   prm.ref32 = s.tree == GWN_TREE_REFERENCE;
+  prm.fp64_queue = s.moments_bounded;
   QueryOrder qo;
   order_queries(Q, GWN_F64, nQ, s.lo, s.hi, qo, st);
   DevBuf<double> W((size_t)nQ, st);

@@ -118,6 +118,10 @@ struct gwn_soup_impl {
   // outward to FP32, and the children (internal index, or ~slot for a leaf):
   //   {lo_l.xyz, left}, {hi_l.xyz, right}, {lo_r.xyz, 0}, {hi_r.xyz, 0}.
   DevMem<float4> snode;
+  // every FP64 moment finite and within 1e100 in magnitude: then no far
+  // field at |q - P|^2 >= 1e-100 can overflow, and the plain FP64 walk may
+  // queue its far fields (soup_walk.cuh)
+  bool moments_bounded = false;
   size_t bytes = 0;
 };
 
@@ -140,6 +144,8 @@ void soup_build_ref(gwn_soup_impl& s, const double* V, int64_t nV, const int32_t
 // slot-ordered FP64 corners), for the closest-point search; the search
 // tree's triangle ids are the reference soup's leaf slots.
 void soup_build_search(const gwn_soup_impl& ref, gwn_soup_impl& search, cudaStream_t st);
+// Sets s.moments_bounded from the FP64 records (one reduction, one host read).
+void soup_check_moments(gwn_soup_impl& s, cudaStream_t st);
 // I[q] <- map[I[q]] where I[q] >= 0.
 void soup_remap_index(const int32_t* map, int32_t* I, int64_t n, cudaStream_t st);
 // Instrumented mixed walk over FP64 device queries: out7 = {warp steps,

@@ -1760,6 +1760,7 @@ void soup_build_ref(gwn_soup_impl& s, const double* V, int64_t nV, const int32_t
     s.eps = kNearFrac * sqrt(diag2);
     s.cmax = cmax;
   }
+  soup_check_moments(s, st);
   if (host_mode) status.check(st, "soup_build");
   s.bytes = s.nf.bytes() + s.nd.bytes() + s.tf.bytes() + s.td.bytes() + s.tri_index.bytes() +
             s.ref_child.bytes();

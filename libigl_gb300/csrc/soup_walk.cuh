@@ -10,6 +10,7 @@
 
 #include <cuda_runtime.h>
 
+#include <climits>
 #include <cstdint>
 
 #include "bh_common.cuh"
@@ -156,6 +157,7 @@ struct EvalParams {
   float cmax;      // max |coordinate| of any node centre
   unsigned* status;
   int ref32;       // open test: the reference's FP32 one (GWN_TREE_REFERENCE)
+  int fp64_queue = 0;  // moments bounded: the FP64 walk queues its far fields
 };
 
 // The reference's descend test (FWNFS.h:7176-7193) on its FP32 data: q cast
@@ -375,17 +377,76 @@ __device__ __forceinline__ double mixed_result(float acc, double acc64) {
   return acc64 != 0.0 ? ((double)acc + acc64) * kInv4Pi : (double)(acc * kInv4PiF);
 }
 
-// Plain FP64 warp-coherent walk (same calling rule as walk_mixed); returns
-// the solid-angle sum.
+// Per-warp queue of the plain FP64 walk's terms.  The FP64 pipe charges a
+// warp instruction the same for 1 or 32 lanes, and a far field or a
+// triangle term arises for the lanes that reach it at one step, so the walk
+// appends (term, lane) here and the warp evaluates 32 terms at a time, one
+// per lane; each lane adds its own values by its bit mask of queue
+// positions, in queue order, which is its walk order: its sum, term by term,
+// is the one it would form alone.  A far field is queued only when it cannot
+// be non-finite (bounded moments, |q - P|^2 >= 1e-100: every product stays
+// within range), because a non-finite one descends instead
+// (FWNFS.h:7247-7251); any other far field is evaluated where it arises and
+// its value queued.
+constexpr int kQueuedValue = INT_MIN;  // entry holding a value, not a term
+
+struct Fp64Queue {
+  int2 e[32];       // .x: node (far field), ~slot (triangle) or kQueuedValue; .y: lane
+  double q[32][3];  // each lane's query
+  double v[32];     // values
+};
+
+__device__ __forceinline__ void flush_fp64(const EvalParams& prm, Fp64Queue& fq, int n,
+                                           unsigned mine, double& acc) {
+  const int lane = threadIdx.x & 31;
+  __syncwarp();
+  if (lane < n) {
+    const int2 e = fq.e[lane];
+    if (e.x != kQueuedValue) {
+      const double qx = fq.q[e.y][0], qy = fq.q[e.y][1], qz = fq.q[e.y][2];
+      double v;
+      if (e.x >= 0) {
+        const SoupNodeD* r = prm.nd + e.x;
+        const double dx = qx - r->P[0], dy = qy - r->P[1], dz = qz - r->P[2];
+        const double r2 = dx * dx + dy * dy + dz * dz;
+        v = far_field<double>(load_far(r), dx, dy, dz, r2, prm.order);
+      } else {
+        const double* t = prm.td + (int64_t)(~e.x) * 9;
+        v = tri_solid_angle<double>(t[0] - qx, t[1] - qy, t[2] - qz, t[3] - qx, t[4] - qy,
+                                    t[5] - qz, t[6] - qx, t[7] - qy, t[8] - qz);
+      }
+      fq.v[lane] = v;
+    }
+  }
+  __syncwarp();
+  while (mine) {
+    acc += fq.v[__ffs(mine) - 1];
+    mine &= mine - 1;
+  }
+  __syncwarp();
+}
+
+// Plain FP64 warp-coherent walk (same calling rule as walk_mixed, with the
+// warp's Fp64Queue); returns the solid-angle sum.
 __device__ __forceinline__ double walk_fp64(const EvalParams& prm, bool valid, double qx,
-                                            double qy, double qz) {
+                                            double qy, double qz, Fp64Queue& fq) {
+  const int lane = threadIdx.x & 31;
+  fq.q[lane][0] = qx;
+  fq.q[lane][1] = qy;
+  fq.q[lane][2] = qz;
+  const unsigned lt_mask = (1u << lane) - 1u;
   double acc = 0.0;
+  int nq = 0;         // warp-uniform
+  unsigned mine = 0;  // this lane's queue positions
   int resume = valid ? 0 : 0x7fffffff;
   int node = 0;
   const unsigned full = 0xffffffffu;
   while (node < prm.nnodes) {
     const SoupNodeD* r = prm.nd + node;
     bool open = false;
+    bool push = false;
+    int term = 0;
+    double value = 0.0;
     if (node >= resume) {
       const long long link = r->link;
       const bool leaf = link < 0;
@@ -396,22 +457,29 @@ __device__ __forceinline__ double walk_fp64(const EvalParams& prm, bool valid, d
                                            __ldg(&prm.nf[node].a), prm.beta2f)
                               : open_test64(qx, qy, qz, r->P[0], r->P[1], r->P[2], r->maxP2,
                                             prm.beta2d);
-        const double dx = qx - r->P[0], dy = qy - r->P[1], dz = qz - r->P[2];
-        const double r2 = dx * dx + dy * dy + dz * dz;
         if (!near) {
-          const double om = far_field<double>(load_far(r), dx, dy, dz, r2, prm.order);
-          if (isfinite(om)) {
-            acc += om;
+          const double dx = qx - r->P[0], dy = qy - r->P[1], dz = qz - r->P[2];
+          const double r2 = dx * dx + dy * dy + dz * dz;
+          if (prm.fp64_queue && r2 >= 1e-100) {
+            push = true;
+            term = node;
             resume = leaf ? node + 1 : (int)link;
           } else {
-            near = true;
+            const double om = far_field<double>(load_far(r), dx, dy, dz, r2, prm.order);
+            if (isfinite(om)) {
+              push = true;
+              term = kQueuedValue;
+              value = om;
+              resume = leaf ? node + 1 : (int)link;
+            } else {
+              near = true;
+            }
           }
         }
         if (near) {
           if (leaf) {
-            const double* t = prm.td + (int64_t)(~link) * 9;
-            acc += tri_solid_angle<double>(t[0] - qx, t[1] - qy, t[2] - qz, t[3] - qx, t[4] - qy,
-                                           t[5] - qz, t[6] - qx, t[7] - qy, t[8] - qz);
+            push = true;
+            term = (int)link;  // ~slot
             resume = node + 1;
           } else {
             open = true;
@@ -419,10 +487,27 @@ __device__ __forceinline__ double walk_fp64(const EvalParams& prm, bool valid, d
         }
       }
     }
+    const unsigned m = __ballot_sync(full, push);
+    if (m) {
+      const int k = __popc(m);
+      if (nq + k > 32) {
+        flush_fp64(prm, fq, nq, mine, acc);
+        nq = 0;
+        mine = 0;
+      }
+      if (push) {
+        const int pos = nq + __popc(m & lt_mask);
+        fq.e[pos] = make_int2(term, lane);
+        if (term == kQueuedValue) fq.v[pos] = value;
+        mine |= 1u << pos;
+      }
+      nq += k;
+    }
     // a lane that opens the node wants node + 1, every other lane is past
     // the node (resume > node): the warp goes to the smallest of them
     node = __reduce_min_sync(full, open ? node + 1 : resume);
   }
+  if (nq) flush_fp64(prm, fq, nq, mine, acc);
   return acc;
 }
 
