@@ -407,20 +407,21 @@ __device__ __forceinline__ float near_radius2(double area, double eps, double cm
 // w_k = sum_j E2(k,j,j) + E2(j,j,k) + E2(j,k,j).  Both are harmonic (their
 // Laplacians vanish identically), so Q_zz = -Q_xx - Q_yy and
 // K_xzz = -3 K_xxx - K_xyy, K_yzz = -3 K_yyy - K_xxy, K_zzz = -(K_xxz + K_yyz) / 3,
-// and the record keeps 3 + 5 + 7 coefficients (monomial coefficients, 1/(4 pi)
-// folded in), formed in FP64 and rounded once.
-__device__ void pack_cloud32(CloudNodeF& R, const double* ec, int num_terms) {
+// and the records keep 3 + 5 + 7 coefficients (monomial coefficients,
+// 1/(4 pi) folded in), formed in FP64 (the FP64 record) and rounded once (the
+// FP32 record).
+__device__ void pack_cloud(const double* ec, int num_terms, double* pk) {
   const double s = 1.0 / kPi4;
-  double q[5] = {0, 0, 0, 0, 0};  // xx, yy, xy, xz, yz
-  double k[7] = {0, 0, 0, 0, 0, 0, 0};  // xxx, yyy, xxy, xxz, xyy, yyz, xyz
+  for (int k = 0; k < 15; ++k) pk[k] = 0;
+  for (int d = 0; d < 3; ++d) pk[d] = ec[d] * s;
   if (num_terms > 3) {
     auto E1 = [&](int u, int v) { return ec[3 + u + 3 * v]; };
     const double tr = E1(0, 0) + E1(1, 1) + E1(2, 2);
-    q[0] = (tr - 3 * E1(0, 0)) * s;
-    q[1] = (tr - 3 * E1(1, 1)) * s;
-    q[2] = -3 * (E1(0, 1) + E1(1, 0)) * s;
-    q[3] = -3 * (E1(0, 2) + E1(2, 0)) * s;
-    q[4] = -3 * (E1(1, 2) + E1(2, 1)) * s;
+    pk[3] = (tr - 3 * E1(0, 0)) * s;         // Q_xx
+    pk[4] = (tr - 3 * E1(1, 1)) * s;         // Q_yy
+    pk[5] = -3 * (E1(0, 1) + E1(1, 0)) * s;  // Q_xy
+    pk[6] = -3 * (E1(0, 2) + E1(2, 0)) * s;  // Q_xz
+    pk[7] = -3 * (E1(1, 2) + E1(2, 1)) * s;  // Q_yz
   }
   if (num_terms > 12) {
     auto E2 = [&](int i, int u, int v) { return ec[12 + 9 * i + u + 3 * v]; };
@@ -431,19 +432,15 @@ __device__ void pack_cloud32(CloudNodeF& R, const double* ec, int num_terms) {
     }
     // sum of E2 over the distinct orderings of {a, a, b}
     auto S2 = [&](int a, int b) { return E2(a, a, b) + E2(a, b, a) + E2(b, a, a); };
-    k[0] = (15 * E2(0, 0, 0) - 3 * w[0]) * s;
-    k[1] = (15 * E2(1, 1, 1) - 3 * w[1]) * s;
-    k[2] = (15 * S2(0, 1) - 3 * w[1]) * s;  // u_x^2 u_y
-    k[3] = (15 * S2(0, 2) - 3 * w[2]) * s;  // u_x^2 u_z
-    k[4] = (15 * S2(1, 0) - 3 * w[0]) * s;  // u_y^2 u_x
-    k[5] = (15 * S2(1, 2) - 3 * w[2]) * s;  // u_y^2 u_z
-    k[6] = 15 * (E2(0, 1, 2) + E2(0, 2, 1) + E2(1, 0, 2) + E2(1, 2, 0) + E2(2, 0, 1) +
-                 E2(2, 1, 0)) * s;          // u_x u_y u_z
+    pk[8] = (15 * E2(0, 0, 0) - 3 * w[0]) * s;   // K_xxx
+    pk[9] = (15 * E2(1, 1, 1) - 3 * w[1]) * s;   // K_yyy
+    pk[10] = (15 * S2(0, 1) - 3 * w[1]) * s;     // K_xxy: u_x^2 u_y
+    pk[11] = (15 * S2(0, 2) - 3 * w[2]) * s;     // K_xxz
+    pk[12] = (15 * S2(1, 0) - 3 * w[0]) * s;     // K_xyy: u_y^2 u_x
+    pk[13] = (15 * S2(1, 2) - 3 * w[2]) * s;     // K_yyz
+    pk[14] = 15 * (E2(0, 1, 2) + E2(0, 2, 1) + E2(1, 0, 2) + E2(1, 2, 0) + E2(2, 0, 1) +
+                   E2(2, 1, 0)) * s;             // K_xyz
   }
-  R.b = make_float4((float)(ec[0] * s), (float)(ec[1] * s), (float)(ec[2] * s), (float)q[0]);
-  R.c = make_float4((float)q[1], (float)q[2], (float)q[3], (float)q[4]);
-  R.d = make_float4((float)k[0], (float)k[1], (float)k[2], (float)k[3]);
-  R.e = make_float4((float)k[4], (float)k[5], (float)k[6], 0.f);
 }
 
 __global__ void emit_nodes_kernel(LayoutIn in, CloudNodeF* __restrict__ nf,
@@ -462,15 +459,23 @@ __global__ void emit_nodes_kernel(LayoutIn in, CloudNodeF* __restrict__ nf,
   CloudNodeD D;
   for (int d = 0; d < 3; ++d) D.cm[d] = in.CM[(int64_t)c * 3 + d];
   D.r = in.R[c];
-  for (int k = 0; k < 39; ++k) D.ec[k] = k < in.num_terms ? in.EC[(int64_t)c * in.num_terms + k] : 0.0;
+  {
+    double ec[39];
+    for (int k = 0; k < 39; ++k) ec[k] = k < in.num_terms ? in.EC[(int64_t)c * in.num_terms + k] : 0.0;
+    pack_cloud(ec, in.num_terms, D.pk);
+  }
   D.pad = 0;
   const int first = in.first_by_pos ? in.first_by_pos[p] : (int)in.start[c];
   D.l = make_int4((int)skip, first, in.count[c], leaf ? 1 : 0);
   nd[p] = D;
   CloudNodeF Fr;
   Fr.a = make_float4((float)D.cm[0], (float)D.cm[1], (float)D.cm[2], (float)D.r);
-  pack_cloud32(Fr, D.ec, in.num_terms);
-  Fr.e.w = near_radius2(in.area[c], in.eps, in.cmax);
+  const double* pk = D.pk;
+  Fr.b = make_float4((float)pk[0], (float)pk[1], (float)pk[2], (float)pk[3]);
+  Fr.c = make_float4((float)pk[4], (float)pk[5], (float)pk[6], (float)pk[7]);
+  Fr.d = make_float4((float)pk[8], (float)pk[9], (float)pk[10], (float)pk[11]);
+  Fr.e = make_float4((float)pk[12], (float)pk[13], (float)pk[14],
+                     near_radius2(in.area[c], in.eps, in.cmax));
   Fr.l = D.l;
   nf[p] = Fr;
 }
@@ -502,51 +507,29 @@ __device__ __forceinline__ double dipole64(double lx, double ly, double lz, doub
   return (lx * ax + ly * ay + lz * az) / (kPi4 * (ln * ln * ln));
 }
 
-// expansion_eval, fast_winding_number.cpp:174-228; loc = CM - q.  T float/double.
-template <typename T>
-__device__ __forceinline__ T expansion(const T* ec, T lx, T ly, T lz, T r, int num_terms) {
-  const T pi4 = T(kPi4);
-  const T r3 = pi4 * r * r * r;
-  T wn = (lx * ec[0] + ly * ec[1] + lz * ec[2]) / r3;
-  if (num_terms > 3) {
-    const T r5 = r3 * r * r;
-    const T d = T(1) / r3;
-    const T s = T(-3) / r5;
-    const T l[3] = {lx, ly, lz};
-    T acc = 0;
-#pragma unroll
-    for (int v = 0; v < 3; ++v)
-#pragma unroll
-      for (int u = 0; u < 3; ++u) {
-        T sd = (l[u] * l[v]) * s;
-        if (u == v) sd += d;
-        acc += sd * ec[3 + u + 3 * v];
-      }
-    wn += acc;
-    if (num_terms > 12) {
-      const T r7 = r5 * r * r;
-#pragma unroll
-      for (int i = 0; i < 3; ++i) {
-        T acc3 = 0;
-#pragma unroll
-        for (int v = 0; v < 3; ++v)
-#pragma unroll
-          for (int u = 0; u < 3; ++u) {
-            T rcd = 0;
-            if (u == v) rcd += l[i];
-            if (u == i) rcd += l[v];
-            if (v == i) rcd += l[u];
-            const T ltl = l[u] * (l[v] / r7);
-            acc3 += (T(15) * l[i] * ltl + s * rcd) * ec[12 + i * 9 + u + 3 * v];
-          }
-        wn += acc3;
-      }
-    }
+// FP64 expansion from a packed record (pack_cloud), loc = CM - q: the same
+// forms as the FP32 walk's, in FP64.
+__device__ __forceinline__ double expansion_packed64(const double* pk, double lx, double ly,
+                                                     double lz, int num_terms) {
+  const double ir = 1.0 / sqrt(lx * lx + ly * ly + lz * lz), ir2 = ir * ir;
+  const double ux = lx * ir, uy = ly * ir, uz = lz * ir;
+  const double lin = ux * pk[0] + uy * pk[1] + uz * pk[2];
+  if (num_terms <= 3) return ir2 * lin;
+  const double x2 = ux * ux, y2 = uy * uy, z2 = uz * uz, yz = uy * uz;
+  const double qzz = -(pk[3] + pk[4]);
+  double s = ux * (pk[3] * ux + pk[5] * uy + pk[6] * uz) + pk[4] * y2 + qzz * z2 + pk[7] * yz;
+  if (num_terms > 12) {
+    const double kxzz = -(3 * pk[8] + pk[12]), kyzz = -(3 * pk[9] + pk[10]);
+    const double kzzz = -(pk[11] + pk[13]) / 3;
+    const double kx = pk[8] * x2 + pk[12] * y2 + kxzz * z2 + pk[14] * yz;
+    const double ky = pk[10] * x2 + pk[9] * y2 + kyzz * z2;
+    const double kz = pk[11] * x2 + pk[13] * y2 + kzzz * z2;
+    s += ir * (ux * kx + uy * ky + uz * kz);
   }
-  return wn;
+  return ir2 * (lin + ir * s);
 }
 
-// FP32 expansion from a packed record (pack_cloud32): loc = CM - q,
+// FP32 expansion from a packed record (pack_cloud): loc = CM - q,
 // r2 = |loc|^2; W = (u.N + (Q(u) + K(u)/r)/r) / r^2 with u = loc/r.
 __device__ __forceinline__ float expansion_packed32(float4 b, float4 c, float4 d, float4 e,
                                                     float lx, float ly, float lz, float r2,
@@ -599,29 +582,30 @@ __device__ __forceinline__ void read_q(const QT* Q, const int32_t* perm, const i
   z = (double)Q[qi * 3 + 2];
 }
 
-// Per-warp queue of FP64 near-field terms of the mixed walk: code >= 0 is a
-// point slot (exact dipole term), code < 0 is ~node (the node's expansion in
-// FP64).  Lanes append the terms they need and the warp evaluates up to 32
-// queued terms at once, one per lane, so each FP64 instruction serves the
-// whole warp; each lane still adds its own terms in walk order.  The lanes'
-// FP64 queries live here too (read only at FP64 re-checks and flushes), and
-// the walk runs 8 blocks of 128 threads per SM (64 registers; with the
-// division-free FP32 terms, 18.2 -> 17.4 ms for C3's 8M queries against 6).
+// Per-warp queue of FP64 terms: code >= 0 is a point slot (exact dipole
+// term), code < 0 is ~node (the node's expansion in FP64).  Lanes append the
+// terms they need and the warp evaluates up to 32 queued terms at once, one
+// per lane, so each FP64 instruction serves the whole warp; each lane adds
+// its own values by its bit mask of queue positions, in queue order, which
+// is its walk order.  The mixed walk queues its FP64 near-field terms here,
+// the plain FP64 walk every term.  The lanes' FP64 queries live here too
+// (read only at FP64 re-checks and flushes), and the mixed walk runs 8
+// blocks of 128 threads per SM (64 registers; with the division-free FP32
+// terms, 18.2 -> 17.4 ms for C3's 8M queries against 6).
 struct CloudNearQueue {
   int2 e[32];
   double q[32][3];  // each lane's FP64 query
+  double v[32];     // the values of one flush
 };
 
-__device__ __forceinline__ void flush_cloud64(const CloudEvalParams& prm,
-                                              const CloudNearQueue& q, int n, double& acc64) {
-  const unsigned full = 0xffffffffu;
+__device__ __forceinline__ void flush_cloud64(const CloudEvalParams& prm, CloudNearQueue& q,
+                                              int n, unsigned mine, double& acc64) {
   const int lane = threadIdx.x & 31;
   __syncwarp();
-  int2 e = make_int2(0, lane);
-  if (lane < n) e = q.e[lane];
-  const double ox = q.q[e.y][0], oy = q.q[e.y][1], oz = q.q[e.y][2];
-  double v = 0.0;
   if (lane < n) {
+    const int2 e = q.e[lane];
+    const double ox = q.q[e.y][0], oy = q.q[e.y][1], oz = q.q[e.y][2];
+    double v;
     if (e.x >= 0) {
       const double* pd = prm.pd + (int64_t)e.x * 6;
       v = dipole64(pd[0] - ox, pd[1] - oy, pd[2] - oz, pd[3], pd[4], pd[5]);
@@ -629,32 +613,71 @@ __device__ __forceinline__ void flush_cloud64(const CloudEvalParams& prm,
       const CloudNodeD* rd = prm.nd + ~e.x;
       const double lx = __dsub_rn(rd->cm[0], ox), ly = __dsub_rn(rd->cm[1], oy),
                    lz = __dsub_rn(rd->cm[2], oz);
-      v = expansion<double>(rd->ec, lx, ly, lz, sqrt(lx * lx + ly * ly + lz * lz),
-                            prm.num_terms);
+      v = expansion_packed64(rd->pk, lx, ly, lz, prm.num_terms);
     }
+    q.v[lane] = v;
   }
-  for (int k = 0; k < n; ++k) {
-    const double vk = __shfl_sync(full, v, k);
-    const int ok = __shfl_sync(full, e.y, k);
-    if (ok == lane) acc64 += vk;
+  __syncwarp();
+  while (mine) {
+    acc64 += q.v[__ffs(mine) - 1];
+    mine &= mine - 1;
   }
   __syncwarp();
 }
 
+// Appends this lane's term `code` if `want` (all 32 lanes call together).
 __device__ __forceinline__ void queue_cloud64(const CloudEvalParams& prm, CloudNearQueue& q,
-                                              int& nqueued, bool want, int code,
+                                              int& nqueued, unsigned& mine, bool want, int code,
                                               double& acc64) {
   const unsigned full = 0xffffffffu;
   const unsigned m = __ballot_sync(full, want);
   if (!m) return;
   const int k = __popc(m);
   if (nqueued + k > 32) {
-    flush_cloud64(prm, q, nqueued, acc64);
+    flush_cloud64(prm, q, nqueued, mine, acc64);
     nqueued = 0;
+    mine = 0;
   }
   const int lane = threadIdx.x & 31;
-  if (want) q.e[nqueued + __popc(m & ((1u << lane) - 1u))] = make_int2(code, lane);
+  if (want) {
+    const int pos = nqueued + __popc(m & ((1u << lane) - 1u));
+    q.e[pos] = make_int2(code, lane);
+    mine |= 1u << pos;
+  }
   nqueued += k;
+}
+
+// Appends cnt dipole terms of this lane (point slots first, first + 1, ...)
+// after the lower lanes' terms, flushing whenever the queue fills (all 32
+// lanes call together).
+__device__ __forceinline__ void queue_points64(const CloudEvalParams& prm, CloudNearQueue& q,
+                                               int& nqueued, unsigned& mine, int cnt, int first,
+                                               double& acc64) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  int incl = cnt;
+  for (int d = 1; d < 32; d <<= 1) {
+    const int y = __shfl_up_sync(full, incl, d);
+    if (lane >= d) incl += y;
+  }
+  const int total = __shfl_sync(full, incl, 31);
+  const int excl = incl - cnt;
+  for (int done = 0; done < total;) {
+    const int take = min(32 - nqueued, total - done);
+    const int k0 = max(0, done - excl), k1 = min(cnt, done + take - excl);
+    for (int k = k0; k < k1; ++k) {
+      const int pos = nqueued + excl + k - done;
+      q.e[pos] = make_int2(first + k, lane);
+      mine |= 1u << pos;
+    }
+    nqueued += take;
+    done += take;
+    if (nqueued == 32) {
+      flush_cloud64(prm, q, 32, mine, acc64);
+      nqueued = 0;
+      mine = 0;
+    }
+  }
 }
 
 template <typename QT, typename WT>
@@ -665,7 +688,8 @@ __global__ void __launch_bounds__(128, 8) cloud_eval_mixed_kernel(CloudEvalParam
                                                                unsigned* __restrict__ refine_count) {
   __shared__ CloudNearQueue near_q[4];
   CloudNearQueue& nq = near_q[threadIdx.x >> 5];
-  int nqueued = 0;  // warp-uniform
+  int nqueued = 0;    // warp-uniform
+  unsigned mine = 0;  // this lane's queue positions
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const bool valid = i < nQ;
   int64_t qi = 0;
@@ -711,7 +735,7 @@ __global__ void __launch_bounds__(128, 8) cloud_eval_mixed_kernel(CloudEvalParam
             acc += fmaf(lx, an.x, fmaf(ly, an.y, lz * an.z)) * (ir * ir * ir * kInvPi4F);
           }
         }
-        queue_cloud64(prm, nq, nqueued, want, (int)slot, acc64);
+        queue_cloud64(prm, nq, nqueued, mine, want, (int)slot, acc64);
       }
       if (visit) resume = l.x;
     } else if (node == 0) {
@@ -739,13 +763,13 @@ __global__ void __launch_bounds__(128, 8) cloud_eval_mixed_kernel(CloudEvalParam
           open = true;
         }
       }
-      queue_cloud64(prm, nq, nqueued, want, ~node, acc64);
+      queue_cloud64(prm, nq, nqueued, mine, want, ~node, acc64);
     }
     // a lane that opens the node wants node + 1, every other lane is past
     // the node (resume > node): the warp goes to the smallest of them
     node = __reduce_min_sync(full, open ? node + 1 : resume);
   }
-  if (nqueued) flush_cloud64(prm, nq, nqueued, acc64);
+  if (nqueued) flush_cloud64(prm, nq, nqueued, mine, acc64);
   if (!valid) return;
   const double w = acc64 != 0.0 ? (double)acc + acc64 : (double)acc;
   W[qi] = (WT)w;
@@ -768,6 +792,15 @@ __global__ void __launch_bounds__(128) cloud_eval_fp64_kernel(CloudEvalParams pr
   int64_t qi = 0;
   double qx = 0, qy = 0, qz = 0;
   if (valid) read_q(Q, perm, list, i, qi, qx, qy, qz);
+  // every term through the warp's FP64 queue (see CloudNearQueue)
+  __shared__ CloudNearQueue fp64_q[4];
+  CloudNearQueue& fq = fp64_q[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  fq.q[lane][0] = qx;
+  fq.q[lane][1] = qy;
+  fq.q[lane][2] = qz;
+  int nqueued = 0;    // warp-uniform
+  unsigned mine = 0;  // this lane's queue positions
   double acc = 0.0;
   int resume = valid ? 0 : 0x7fffffff;
   int node = 0;
@@ -775,30 +808,30 @@ __global__ void __launch_bounds__(128) cloud_eval_fp64_kernel(CloudEvalParams pr
   while (node < prm.nnodes) {
     const CloudNodeD* r = prm.nd + node;
     const int4 l = r->l;
+    const bool visit = node >= resume;
     bool open = false;
-    if (node >= resume) {
-      if (l.w) {
-        for (int j = 0; j < l.z; ++j) {
-          const double* pd = prm.pd + ((int64_t)l.y + j) * 6;
-          acc += dipole64(pd[0] - qx, pd[1] - qy, pd[2] - qz, pd[3], pd[4], pd[5]);
+    if (l.w) {  // leaf (the node, hence the branch, is warp-uniform)
+      queue_points64(prm, fq, nqueued, mine, visit ? l.z : 0, l.y, acc);
+      if (visit) resume = l.x;
+    } else if (node == 0) {
+      open = visit;
+    } else {
+      bool want = false;
+      if (visit) {
+        if (far64(qx, qy, qz, r->cm, r->r, prm.beta)) {
+          want = true;
+          resume = l.x;
+        } else {
+          open = true;
         }
-        resume = l.x;
-      } else if (node == 0) {
-        open = true;
-      } else if (far64(qx, qy, qz, r->cm, r->r, prm.beta)) {
-        const double lx = __dsub_rn(r->cm[0], qx), ly = __dsub_rn(r->cm[1], qy),
-                     lz = __dsub_rn(r->cm[2], qz);
-        const double rr = sqrt(lx * lx + ly * ly + lz * lz);
-        acc += expansion<double>(r->ec, lx, ly, lz, rr, prm.num_terms);
-        resume = l.x;
-      } else {
-        open = true;
       }
+      queue_cloud64(prm, fq, nqueued, mine, want, ~node, acc);
     }
     // a lane that opens the node wants node + 1, every other lane is past
     // the node (resume > node): the warp goes to the smallest of them
     node = __reduce_min_sync(full, open ? node + 1 : resume);
   }
+  if (nqueued) flush_cloud64(prm, fq, nqueued, mine, acc);
   if (valid) W[qi] = (WT)acc;
 }
 
@@ -838,8 +871,7 @@ __global__ void __launch_bounds__(128) cloud_refine_warp_kernel(CloudEvalParams 
         if (lane == 0) {
           const double lx = __dsub_rn(r->cm[0], qx), ly = __dsub_rn(r->cm[1], qy),
                        lz = __dsub_rn(r->cm[2], qz);
-          const double rr = sqrt(lx * lx + ly * ly + lz * lz);
-          acc += expansion<double>(r->ec, lx, ly, lz, rr, prm.num_terms);
+          acc += expansion_packed64(r->pk, lx, ly, lz, prm.num_terms);
         }
         node = l.x;
       } else {

@@ -16,7 +16,7 @@ namespace gwn {
 //   l: skip (one past subtree), first point slot, point count, leaf flag
 // N, Q, K: the expansion of the cell in the unit direction u = (CM - q)/r,
 // W = (u.N + Q(u)/r + K(u)/r^2) / r^2, with Q and K harmonic (Q_zz and
-// K_xzz, K_yzz, K_zzz follow from the others); formed by pack_cloud32
+// K_xzz, K_yzz, K_zzz follow from the others); formed by pack_cloud
 // (cloud.cu) from EC.
 struct __align__(32) CloudNodeF {
   float4 a, b, c, d, e;
@@ -24,10 +24,12 @@ struct __align__(32) CloudNodeF {
 };
 static_assert(sizeof(CloudNodeF) == 96, "three 32-byte halves per record");
 
-// FP64 traversal record.
+// FP64 traversal record: CM, R, the packed expansion pk (the FP32 record's
+// b..e coefficients in FP64: N xyz, Q_xx, Q_yy, Q_xy, Q_xz, Q_yz, K_xxx,
+// K_yyy, K_xxy, K_xxz, K_xyy, K_yyz, K_xyz), links as in CloudNodeF.
 struct __align__(16) CloudNodeD {
   double cm[3], r;
-  double ec[39];
+  double pk[15];
   double pad;
   int4 l;
 };
