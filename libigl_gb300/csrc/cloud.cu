@@ -311,11 +311,51 @@ __device__ __forceinline__ void small_cell_moments(CsrView v, int64_t c, int32_t
   for (int k = 0; k < NT - 3; ++k) row[3 + k] = acc[k];
 }
 
-// One block of 128 threads handles 128 consecutive cells; the EC rows are
-// staged in shared memory per warp and written out coalesced (each warp's 32
-// rows are one contiguous block of EC).
+// Small non-empty cells grouped by point count (a counting sort on
+// 1..kSmallCell): the lanes of a warp then loop over the same number of
+// points, where consecutive cell ids (mostly empty cells, and counts from 1
+// to 64 side by side) left two lanes in three idle on the FP64 pipe.
+__global__ void small_hist_kernel(const int32_t* __restrict__ count, int64_t ncells,
+                                  unsigned* __restrict__ hist) {
+  __shared__ unsigned h[kSmallCell + 1];
+  for (int k = threadIdx.x; k <= kSmallCell; k += blockDim.x) h[k] = 0;
+  __syncthreads();
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c < ncells) {
+    const int32_t n = count[c];
+    if (n > 0 && n <= kSmallCell) atomicAdd(&h[n], 1u);
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k <= kSmallCell; k += blockDim.x)
+    if (h[k]) atomicAdd(&hist[k], h[k]);
+}
+
+// hist[0..kSmallCell] -> exclusive offsets, total in hist[kSmallCell + 1]
+// (one thread; 65 entries)
+__global__ void small_offsets_kernel(unsigned* __restrict__ hist) {
+  unsigned run = 0;
+  for (int k = 0; k <= kSmallCell; ++k) {
+    const unsigned v = hist[k];
+    hist[k] = run;
+    run += v;
+  }
+  hist[kSmallCell + 1] = run;
+}
+
+__global__ void small_scatter_kernel(const int32_t* __restrict__ count, int64_t ncells,
+                                     unsigned* __restrict__ next, int32_t* __restrict__ list) {
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  const int32_t n = count[c];
+  if (n > 0 && n <= kSmallCell) list[atomicAdd(&next[n], 1u)] = (int32_t)c;
+}
+
+// One thread per listed small cell (both passes over the cell's points in
+// list order); each warp stages its 32 EC rows in shared memory and writes
+// them row by row, each row one coalesced store of NT doubles.
 template <int NT>
-__global__ void __launch_bounds__(128) small_cells_kernel(CsrView v, int64_t ncells,
+__global__ void __launch_bounds__(128) small_cells_kernel(CsrView v, const int32_t* __restrict__ list,
+                                                          int64_t n,
                                                           const double* __restrict__ P,
                                                           const double* __restrict__ N,
                                                           const double* __restrict__ A,
@@ -324,20 +364,20 @@ __global__ void __launch_bounds__(128) small_cells_kernel(CsrView v, int64_t nce
                                                           double* __restrict__ EC,
                                                           double* __restrict__ area) {
   __shared__ double rows[4][32 * NT];
+  __shared__ int32_t cells[4][32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t c0 = (blockIdx.x * (int64_t)blockDim.x) + warp * 32;  // first cell of the warp
-  const int64_t c = c0 + lane;
-  const int32_t cnt = c < ncells ? v.count[c] : 0;
-  const bool mine = cnt > 0 && cnt <= kSmallCell;
-  const unsigned small_mask = __ballot_sync(0xffffffffu, mine);
-  if (small_mask == 0u) return;  // the whole warp: no small cell
-  if (mine) small_cell_moments<NT>(v, c, cnt, P, N, A, CM, R, area, rows[warp] + lane * NT);
+  const int64_t i0 = (blockIdx.x * (int64_t)blockDim.x) + warp * 32;  // first entry of the warp
+  if (i0 >= n) return;  // the whole warp
+  const int64_t i = i0 + lane;
+  const int32_t c = i < n ? list[i] : -1;
+  cells[warp][lane] = c;
+  if (c >= 0)
+    small_cell_moments<NT>(v, c, v.count[c], P, N, A, CM, R, area, rows[warp] + lane * NT);
   __syncwarp();
-  // coalesced write of the small cells' rows
-  double* out = EC + c0 * NT;
-  for (int e = lane; e < 32 * NT; e += 32) {
-    const int row = e / NT;
-    if (c0 + row < ncells && ((small_mask >> row) & 1u)) out[e] = rows[warp][e];
+  const int nrows = n - i0 < 32 ? (int)(n - i0) : 32;
+  for (int r = 0; r < nrows; ++r) {
+    double* out = EC + (int64_t)cells[warp][r] * NT;
+    for (int e = lane; e < NT; e += 32) out[e] = rows[warp][r * NT + e];
   }
 }
 
@@ -937,10 +977,20 @@ void precompute(gwn_cloud_impl& c, const CsrView& v, int64_t ncells, const doubl
   DevBuf<unsigned> nch((size_t)ncells, st), cbase((size_t)ncells, st);
   launch_kernel(chunk_count_kernel, blocks(ncells), 256, 0, st, v.count, ncells, nch.get());
   exclusive_scan_u32(nch.get(), cbase.get(), ncells, st);
-  unsigned last_n = 0, last_b = 0;
+  // the small cells' list, grouped by point count
+  DevBuf<unsigned> hist(kSmallCell + 2, st);
+  hist.zero(st);
+  launch_kernel(small_hist_kernel, blocks(ncells), 256, 0, st, v.count, ncells, hist.get());
+  launch_kernel(small_offsets_kernel, 1, 1, 0, st, hist.get());
+  unsigned last_n = 0, last_b = 0, nsmall = 0;
   GWN_CUDA(cudaMemcpyAsync(&last_n, nch.get() + ncells - 1, 4, cudaMemcpyDeviceToHost, st));
   GWN_CUDA(cudaMemcpyAsync(&last_b, cbase.get() + ncells - 1, 4, cudaMemcpyDeviceToHost, st));
+  GWN_CUDA(cudaMemcpyAsync(&nsmall, hist.get() + kSmallCell + 1, 4, cudaMemcpyDeviceToHost, st));
   GWN_CUDA(cudaStreamSynchronize(st));
+  DevBuf<int32_t> small((size_t)std::max<unsigned>(nsmall, 1u), st);
+  if (nsmall)
+    launch_kernel(small_scatter_kernel, blocks(ncells), 256, 0, st, v.count, ncells, hist.get(),
+                  small.get());
   const int64_t nchunks = (int64_t)last_n + last_b;
   DevBuf<int32_t> chunk_cell((size_t)std::max<int64_t>(nchunks, 1), st);
   launch_kernel(chunk_fill_kernel, blocks(ncells), 256, 0, st, nch.get(), cbase.get(), ncells, chunk_cell.get());
@@ -970,15 +1020,18 @@ void precompute(gwn_cloud_impl& c, const CsrView& v, int64_t ncells, const doubl
     launch_kernel(combine2_kernel, blocks(nchunks * 32), 256, 0, st, (const int32_t*)chunk_cell.get(),
                   (const unsigned*)cbase.get(), (const unsigned*)nch.get(), nchunks,
                   (const double*)part.get(), c.num_terms, c.R.get(), c.EC.get());
-  if (c.num_terms == 39)
-    launch_kernel(small_cells_kernel<39>, blocks(ncells, 128), 128, 0, st, v, ncells, P, N, A,
-                  c.CM.get(), c.R.get(), c.EC.get(), c.area.get());
-  else if (c.num_terms == 12)
-    launch_kernel(small_cells_kernel<12>, blocks(ncells, 128), 128, 0, st, v, ncells, P, N, A,
-                  c.CM.get(), c.R.get(), c.EC.get(), c.area.get());
-  else
-    launch_kernel(small_cells_kernel<3>, blocks(ncells, 128), 128, 0, st, v, ncells, P, N, A,
-                  c.CM.get(), c.R.get(), c.EC.get(), c.area.get());
+  if (nsmall) {
+    const int32_t* sl = small.get();
+    if (c.num_terms == 39)
+      launch_kernel(small_cells_kernel<39>, blocks(nsmall, 128), 128, 0, st, v, sl, (int64_t)nsmall,
+                    P, N, A, c.CM.get(), c.R.get(), c.EC.get(), c.area.get());
+    else if (c.num_terms == 12)
+      launch_kernel(small_cells_kernel<12>, blocks(nsmall, 128), 128, 0, st, v, sl, (int64_t)nsmall,
+                    P, N, A, c.CM.get(), c.R.get(), c.EC.get(), c.area.get());
+    else
+      launch_kernel(small_cells_kernel<3>, blocks(nsmall, 128), 128, 0, st, v, sl, (int64_t)nsmall,
+                    P, N, A, c.CM.get(), c.R.get(), c.EC.get(), c.area.get());
+  }
 }
 
 __global__ void count_nonempty_kernel(const int32_t* __restrict__ count, int64_t n,
