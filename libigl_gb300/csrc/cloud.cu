@@ -315,15 +315,24 @@ __device__ __forceinline__ void small_cell_moments(CsrView v, int64_t c, int32_t
 // 1..kSmallCell): the lanes of a warp then loop over the same number of
 // points, where consecutive cell ids (mostly empty cells, and counts from 1
 // to 64 side by side) left two lanes in three idle on the FP64 pipe.
-__global__ void small_hist_kernel(const int32_t* __restrict__ count, int64_t ncells,
-                                  unsigned* __restrict__ hist) {
+// 4,096 cells per block (256 threads x 16): the global counters then take
+// one atomic per block and count instead of one per cell, since thousands of
+// same-address atomics serialize.
+constexpr int kListThreads = 256, kListPer = 16;
+constexpr int64_t kListCells = (int64_t)kListThreads * kListPer;
+
+__global__ void __launch_bounds__(kListThreads) small_hist_kernel(const int32_t* __restrict__ count,
+                                                                  int64_t ncells,
+                                                                  unsigned* __restrict__ hist) {
   __shared__ unsigned h[kSmallCell + 1];
   for (int k = threadIdx.x; k <= kSmallCell; k += blockDim.x) h[k] = 0;
   __syncthreads();
-  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (c < ncells) {
-    const int32_t n = count[c];
-    if (n > 0 && n <= kSmallCell) atomicAdd(&h[n], 1u);
+  for (int j = 0; j < kListPer; ++j) {
+    const int64_t c = blockIdx.x * kListCells + (int64_t)j * kListThreads + threadIdx.x;
+    if (c < ncells) {
+      const int32_t n = count[c];
+      if (n > 0 && n <= kSmallCell) atomicAdd(&h[n], 1u);
+    }
   }
   __syncthreads();
   for (int k = threadIdx.x; k <= kSmallCell; k += blockDim.x)
@@ -342,12 +351,30 @@ __global__ void small_offsets_kernel(unsigned* __restrict__ hist) {
   hist[kSmallCell + 1] = run;
 }
 
-__global__ void small_scatter_kernel(const int32_t* __restrict__ count, int64_t ncells,
-                                     unsigned* __restrict__ next, int32_t* __restrict__ list) {
-  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (c >= ncells) return;
-  const int32_t n = count[c];
-  if (n > 0 && n <= kSmallCell) list[atomicAdd(&next[n], 1u)] = (int32_t)c;
+__global__ void __launch_bounds__(kListThreads) small_scatter_kernel(const int32_t* __restrict__ count,
+                                                                     int64_t ncells,
+                                                                     unsigned* __restrict__ next,
+                                                                     int32_t* __restrict__ list) {
+  __shared__ unsigned h[kSmallCell + 1], base[kSmallCell + 1];
+  for (int k = threadIdx.x; k <= kSmallCell; k += blockDim.x) h[k] = 0;
+  __syncthreads();
+  int32_t n[kListPer];
+  unsigned rank[kListPer];
+#pragma unroll
+  for (int j = 0; j < kListPer; ++j) {
+    const int64_t c = blockIdx.x * kListCells + (int64_t)j * kListThreads + threadIdx.x;
+    n[j] = c < ncells ? count[c] : 0;
+    rank[j] = (n[j] > 0 && n[j] <= kSmallCell) ? atomicAdd(&h[n[j]], 1u) : 0u;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k <= kSmallCell; k += blockDim.x)
+    base[k] = h[k] ? atomicAdd(&next[k], h[k]) : 0u;
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < kListPer; ++j) {
+    const int64_t c = blockIdx.x * kListCells + (int64_t)j * kListThreads + threadIdx.x;
+    if (n[j] > 0 && n[j] <= kSmallCell) list[base[n[j]] + rank[j]] = (int32_t)c;
+  }
 }
 
 // One thread per listed small cell (both passes over the cell's points in
@@ -980,7 +1007,8 @@ void precompute(gwn_cloud_impl& c, const CsrView& v, int64_t ncells, const doubl
   // the small cells' list, grouped by point count
   DevBuf<unsigned> hist(kSmallCell + 2, st);
   hist.zero(st);
-  launch_kernel(small_hist_kernel, blocks(ncells), 256, 0, st, v.count, ncells, hist.get());
+  const unsigned list_blocks = (unsigned)((ncells + kListCells - 1) / kListCells);
+  launch_kernel(small_hist_kernel, list_blocks, kListThreads, 0, st, v.count, ncells, hist.get());
   launch_kernel(small_offsets_kernel, 1, 1, 0, st, hist.get());
   unsigned last_n = 0, last_b = 0, nsmall = 0;
   GWN_CUDA(cudaMemcpyAsync(&last_n, nch.get() + ncells - 1, 4, cudaMemcpyDeviceToHost, st));
@@ -989,8 +1017,8 @@ void precompute(gwn_cloud_impl& c, const CsrView& v, int64_t ncells, const doubl
   GWN_CUDA(cudaStreamSynchronize(st));
   DevBuf<int32_t> small((size_t)std::max<unsigned>(nsmall, 1u), st);
   if (nsmall)
-    launch_kernel(small_scatter_kernel, blocks(ncells), 256, 0, st, v.count, ncells, hist.get(),
-                  small.get());
+    launch_kernel(small_scatter_kernel, list_blocks, kListThreads, 0, st, v.count, ncells,
+                  hist.get(), small.get());
   const int64_t nchunks = (int64_t)last_n + last_b;
   DevBuf<int32_t> chunk_cell((size_t)std::max<int64_t>(nchunks, 1), st);
   launch_kernel(chunk_fill_kernel, blocks(ncells), 256, 0, st, nch.get(), cbase.get(), ncells, chunk_cell.get());
