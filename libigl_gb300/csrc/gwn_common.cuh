@@ -217,6 +217,24 @@ struct DeviceStatus {
   void check(cudaStream_t s, const char* where) const;
 };
 
+// A few pinned host words for small device-to-host reads (a copy into
+// pageable memory is staged through a driver buffer on every call).
+class PinnedWords {
+ public:
+  explicit PinnedWords(size_t n) {
+    GWN_CUDA(cudaMallocHost(reinterpret_cast<void**>(&p_), n * sizeof(unsigned)));
+  }
+  ~PinnedWords() {
+    if (p_) cudaFreeHost(p_);
+  }
+  PinnedWords(const PinnedWords&) = delete;
+  PinnedWords& operator=(const PinnedWords&) = delete;
+  unsigned* get() const { return p_; }
+
+ private:
+  unsigned* p_ = nullptr;
+};
+
 // Optional per-phase timing of the calling thread's ABI calls (CUDA events
 // recorded on the launch stream).  Off unless gwn_profile_enable(1).
 struct PhaseTimer {

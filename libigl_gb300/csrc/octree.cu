@@ -252,6 +252,22 @@ __global__ void state_flag_kernel(const unsigned* __restrict__ child_state, int6
   if (i < n) flag[i] = child_state[i] == v ? 1u : 0u;
 }
 
+// The level's totals in one word array, read by the host with one copy:
+// {last child state, new segments before the last child, chains before it,
+//  last entry's flag, entries before it}.
+__global__ void level_totals_kernel(const unsigned* __restrict__ child_state,
+                                    const unsigned* __restrict__ child_newseg,
+                                    const unsigned* __restrict__ child_chainslot, int64_t K8,
+                                    const unsigned* __restrict__ eflag,
+                                    const unsigned* __restrict__ epos, int64_t M,
+                                    unsigned* __restrict__ out) {
+  out[0] = child_state[K8 - 1];
+  out[1] = child_newseg[K8 - 1];
+  out[2] = child_chainslot[K8 - 1];
+  out[3] = eflag[M - 1];
+  out[4] = epos[M - 1];
+}
+
 // Next level's segment table and the chain list.
 __global__ void next_segments_kernel(int64_t K8, const unsigned* __restrict__ child_state,
                                      const unsigned* __restrict__ child_newseg,
@@ -515,6 +531,8 @@ void octree_build(gwn_octree_impl& t, const double* P, int64_t n, bool host_mode
   }
   bool had_chain = false;
   int levels = 0;
+  DevBuf<unsigned> totals_d(8, st);
+  PinnedWords totals_h(8);
   while (K > 0) {
     ++levels;
     const int64_t K8 = (int64_t)K * 8;
@@ -554,14 +572,16 @@ void octree_build(gwn_octree_impl& t, const double* P, int64_t n, bool host_mode
     DevBuf<unsigned> eflag((size_t)M, st), epos((size_t)M, st);
     launch_kernel(entry_flag_kernel, blocks(M), 256, 0, st, key.get(), M, child_state.get(), eflag.get());
     exclusive_scan_u32(eflag.get(), epos.get(), M, st);
-    // totals
-    unsigned last_state = 0, last_newseg = 0, last_chain = 0, last_eflag = 0, last_epos = 0;
-    GWN_CUDA(cudaMemcpyAsync(&last_state, child_state.get() + K8 - 1, 4, cudaMemcpyDeviceToHost, st));
-    GWN_CUDA(cudaMemcpyAsync(&last_newseg, child_newseg.get() + K8 - 1, 4, cudaMemcpyDeviceToHost, st));
-    GWN_CUDA(cudaMemcpyAsync(&last_chain, child_chainslot.get() + K8 - 1, 4, cudaMemcpyDeviceToHost, st));
-    GWN_CUDA(cudaMemcpyAsync(&last_eflag, eflag.get() + M - 1, 4, cudaMemcpyDeviceToHost, st));
-    GWN_CUDA(cudaMemcpyAsync(&last_epos, epos.get() + M - 1, 4, cudaMemcpyDeviceToHost, st));
+    // totals: one small kernel and one copy into pinned memory per level
+    launch_kernel(level_totals_kernel, 1, 1, 0, st, (const unsigned*)child_state.get(),
+                  (const unsigned*)child_newseg.get(), (const unsigned*)child_chainslot.get(), K8,
+                  (const unsigned*)eflag.get(), (const unsigned*)epos.get(), M, totals_d.get());
+    GWN_CUDA(cudaMemcpyAsync(totals_h.get(), totals_d.get(), 5 * sizeof(unsigned),
+                             cudaMemcpyDeviceToHost, st));
     GWN_CUDA(cudaStreamSynchronize(st));
+    const unsigned last_state = totals_h.get()[0], last_newseg = totals_h.get()[1],
+                   last_chain = totals_h.get()[2], last_eflag = totals_h.get()[3],
+                   last_epos = totals_h.get()[4];
     const int nK = (int)(last_newseg + (last_state == 1u ? 1u : 0u));
     const int nChains = (int)(last_chain + (last_state == 2u ? 1u : 0u));
     const int64_t nM = (int64_t)last_epos + last_eflag;

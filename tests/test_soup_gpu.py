@@ -219,3 +219,4 @@ def test_tree_builder_corner_cases(cuda):
     a = (np.arange(29)[:, None] * 30 + np.arange(29)[None, :]).ravel()
     Ff = np.concatenate([np.stack([a, a + 30, a + 1], 1), np.stack([a + 1, a + 30, a + 31], 1)])
     _check_tree(np.ascontiguousarray(Vf), np.ascontiguousarray(Ff, dtype=np.int32), Q * 0.8 + 0.3)
+
