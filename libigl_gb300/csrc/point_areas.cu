@@ -115,24 +115,27 @@ __device__ void sym3_eigen(double a[3][3], double d[3], double v[3][3]) {
 }
 
 // The reference's share of triangle (X, Y, Z) for vertex X
-// (point_areas.cpp:122-150), plane coordinates.
+// (point_areas.cpp:122-150), plane coordinates: side lengths x, y, z opposite
+// X, Y, Z, the cosines by the law of cosines (the same numerators, so the
+// same obtuse-angle cases), barycentric weights of the circumcentre
+// x cos X : y cos Y : z cos Z, Heron's area in the reference's form.  One
+// division serves the three cosines and one the weights (the FP64 pipe is
+// this kernel's bound), where the reference divides six times.
 __device__ double voronoi_share(double xx, double xy, double yx, double yy, double zx,
                                 double zy) {
-  const double x = hypot(yx - zx, yy - zy);
-  const double y = hypot(xx - zx, xy - zy);
-  const double z = hypot(yx - xx, yy - xy);
-  const double cosX = (z * z + y * y - x * x) / (2 * y * z);
-  const double cosY = (z * z + x * x - y * y) / (2 * x * z);
-  const double cosZ = (x * x + y * y - z * z) / (2 * y * x);
-  double b0 = x * cosX, b1 = y * cosY, b2 = z * cosZ;
-  const double bs = b0 + b1 + b2;
-  b0 /= bs;
-  b1 /= bs;
-  b2 /= bs;
+  const double ax = yx - zx, ay = yy - zy, bx = xx - zx, by = xy - zy;
+  const double cx = yx - xx, cy = yy - xy;
+  const double x = sqrt(ax * ax + ay * ay), y = sqrt(bx * bx + by * by),
+               z = sqrt(cx * cx + cy * cy);
+  const double inv = 1.0 / (2 * x * y * z);  // cos X = (z^2 + y^2 - x^2) / (2 y z), ...
+  const double cosX = (z * z + y * y - x * x) * (x * inv);
+  const double cosY = (z * z + x * x - y * y) * (y * inv);
+  const double cosZ = (x * x + y * y - z * z) * (z * inv);
   const double full = 0.25 * sqrt((x + (y + z)) * (z - (x - y)) * (z + (x - y)) * (x + (y - z)));
   if (cosX < 0) return 0.5 * full;
   if (cosY < 0 || cosZ < 0) return 0.25 * full;
-  return (b1 * full + b2 * full) / 2;
+  const double b1 = y * cosY, b2 = z * cosZ;
+  return 0.5 * full * ((b1 + b2) / (x * cosX + b1 + b2));
 }
 
 // orientation of (b - a) x (c - a): > 0 when c is left of a -> b
