@@ -25,7 +25,9 @@ constexpr float kInv4PiF = 0.079577471545947667884f;
 constexpr double kInv4Pi = 0.079577471545947667884;
 
 // Far field of one node about its average point, FWNFS.h:7195-7251, with
-// (dx,dy,dz) = q - P and r2 = |q - P|^2, on the FP64 records.
+// (dx,dy,dz) = q - P and r2 = |q - P|^2: the reference's expression, in FP64
+// on the FP64 records (the FP32 walk evaluates the packed forms of
+// pack_far32 instead, far_field32 below).
 template <typename T>
 struct Far {
   T N[3], Nii[3], Nxy_yx, Nyz_zy, Nzx_xz, Niii[3], perm, c2[6];
@@ -33,16 +35,9 @@ struct Far {
 
 template <typename T>
 __device__ __forceinline__ T far_field(const Far<T>& m, T dx, T dy, T dz, T r2, int order) {
-  // m1 = 1/|q-P|, m2 = m1^2 (FP64: 1/r2 then sqrt, as the reference;
-  // FP32: one reciprocal square root)
-  T m1, m2;
-  if (sizeof(T) == 4) {
-    m1 = g_rsqrt(r2);
-    m2 = m1 * m1;
-  } else {
-    m2 = T(1) / r2;
-    m1 = g_sqrt(m2);
-  }
+  // m2 = 1/|q-P|^2, m1 = sqrt(m2), as the reference
+  const T m2 = T(1) / r2;
+  const T m1 = g_sqrt(m2);
   const T qx = dx * m1, qy = dy * m1, qz = dz * m1;
   T omega = -m2 * (qx * m.N[0] + qy * m.N[1] + qz * m.N[2]);
   if (order >= 1) {
