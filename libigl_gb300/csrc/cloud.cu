@@ -462,54 +462,6 @@ __device__ __forceinline__ float near_radius2(double area, double eps, double cm
   return (float)(r * r * 1.0001);
 }
 
-// expansion_eval (fast_winding_number.cpp:174-228) with loc = CM - q = r u,
-// |u| = 1, and E1(u,v) = EC[3 + u + 3v], E2(i,u,v) = EC[12 + 9i + u + 3v]:
-//   4 pi W = (u.EC[0..2]) / r^2
-//          + sum_uv E1(u,v) (delta_uv - 3 u_u u_v) / r^3
-//          + sum_iuv E2(i,u,v) (15 u_i u_u u_v - 3 (delta_uv u_i + delta_ui u_v
-//                                                  + delta_vi u_u)) / r^4.
-// With |u|^2 = 1 the second bracket is the quadratic form
-// Q(u) = sum_uv (tr E1 delta_uv - 3 E1(u,v)) u_u u_v and the third the cubic
-// form K(u) = 15 sum E2(i,u,v) u_i u_u u_v - 3 (u.w) |u|^2, with
-// w_k = sum_j E2(k,j,j) + E2(j,j,k) + E2(j,k,j).  Both are harmonic (their
-// Laplacians vanish identically), so Q_zz = -Q_xx - Q_yy and
-// K_xzz = -3 K_xxx - K_xyy, K_yzz = -3 K_yyy - K_xxy, K_zzz = -(K_xxz + K_yyz) / 3,
-// and the records keep 3 + 5 + 7 coefficients (monomial coefficients,
-// 1/(4 pi) folded in), formed in FP64 (the FP64 record) and rounded once (the
-// FP32 record).
-__device__ void pack_cloud(const double* ec, int num_terms, double* pk) {
-  const double s = 1.0 / kPi4;
-  for (int k = 0; k < 15; ++k) pk[k] = 0;
-  for (int d = 0; d < 3; ++d) pk[d] = ec[d] * s;
-  if (num_terms > 3) {
-    auto E1 = [&](int u, int v) { return ec[3 + u + 3 * v]; };
-    const double tr = E1(0, 0) + E1(1, 1) + E1(2, 2);
-    pk[3] = (tr - 3 * E1(0, 0)) * s;         // Q_xx
-    pk[4] = (tr - 3 * E1(1, 1)) * s;         // Q_yy
-    pk[5] = -3 * (E1(0, 1) + E1(1, 0)) * s;  // Q_xy
-    pk[6] = -3 * (E1(0, 2) + E1(2, 0)) * s;  // Q_xz
-    pk[7] = -3 * (E1(1, 2) + E1(2, 1)) * s;  // Q_yz
-  }
-  if (num_terms > 12) {
-    auto E2 = [&](int i, int u, int v) { return ec[12 + 9 * i + u + 3 * v]; };
-    double w[3];
-    for (int a = 0; a < 3; ++a) {
-      w[a] = 0;
-      for (int j = 0; j < 3; ++j) w[a] += E2(a, j, j) + E2(j, j, a) + E2(j, a, j);
-    }
-    // sum of E2 over the distinct orderings of {a, a, b}
-    auto S2 = [&](int a, int b) { return E2(a, a, b) + E2(a, b, a) + E2(b, a, a); };
-    pk[8] = (15 * E2(0, 0, 0) - 3 * w[0]) * s;   // K_xxx
-    pk[9] = (15 * E2(1, 1, 1) - 3 * w[1]) * s;   // K_yyy
-    pk[10] = (15 * S2(0, 1) - 3 * w[1]) * s;     // K_xxy: u_x^2 u_y
-    pk[11] = (15 * S2(0, 2) - 3 * w[2]) * s;     // K_xxz
-    pk[12] = (15 * S2(1, 0) - 3 * w[0]) * s;     // K_xyy: u_y^2 u_x
-    pk[13] = (15 * S2(1, 2) - 3 * w[2]) * s;     // K_yyz
-    pk[14] = 15 * (E2(0, 1, 2) + E2(0, 2, 1) + E2(1, 0, 2) + E2(1, 2, 0) + E2(2, 0, 1) +
-                   E2(2, 1, 0)) * s;             // K_xyz
-  }
-}
-
 __global__ void emit_nodes_kernel(LayoutIn in, CloudNodeF* __restrict__ nf,
                                   CloudNodeD* __restrict__ nd) {
   const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
