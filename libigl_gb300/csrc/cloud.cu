@@ -962,14 +962,14 @@ void precompute(gwn_cloud_impl& c, const CsrView& v, int64_t ncells, const doubl
   const unsigned list_blocks = (unsigned)((ncells + kListCells - 1) / kListCells);
   launch_kernel(small_hist_kernel, list_blocks, kListThreads, 0, st, v.count, ncells, hist.get());
   launch_kernel(small_offsets_kernel, 1, 1, 0, st, hist.get());
-  PinnedWords sizes_h(3);
-  GWN_CUDA(cudaMemcpyAsync(sizes_h.get(), nch.get() + ncells - 1, 4, cudaMemcpyDeviceToHost, st));
-  GWN_CUDA(cudaMemcpyAsync(sizes_h.get() + 1, cbase.get() + ncells - 1, 4, cudaMemcpyDeviceToHost,
+  unsigned* sizes_h = pinned_words();
+  GWN_CUDA(cudaMemcpyAsync(sizes_h, nch.get() + ncells - 1, 4, cudaMemcpyDeviceToHost, st));
+  GWN_CUDA(cudaMemcpyAsync(sizes_h + 1, cbase.get() + ncells - 1, 4, cudaMemcpyDeviceToHost,
                            st));
-  GWN_CUDA(cudaMemcpyAsync(sizes_h.get() + 2, hist.get() + kSmallCell + 1, 4,
+  GWN_CUDA(cudaMemcpyAsync(sizes_h + 2, hist.get() + kSmallCell + 1, 4,
                            cudaMemcpyDeviceToHost, st));
   GWN_CUDA(cudaStreamSynchronize(st));
-  const unsigned last_n = sizes_h.get()[0], last_b = sizes_h.get()[1], nsmall = sizes_h.get()[2];
+  const unsigned last_n = sizes_h[0], last_b = sizes_h[1], nsmall = sizes_h[2];
   DevBuf<int32_t> small((size_t)std::max<unsigned>(nsmall, 1u), st);
   if (nsmall)
     launch_kernel(small_scatter_kernel, list_blocks, kListThreads, 0, st, v.count, ncells,

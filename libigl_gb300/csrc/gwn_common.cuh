@@ -217,23 +217,22 @@ struct DeviceStatus {
   void check(cudaStream_t s, const char* where) const;
 };
 
-// A few pinned host words for small device-to-host reads (a copy into
-// pageable memory is staged through a driver buffer on every call).
-class PinnedWords {
- public:
-  explicit PinnedWords(size_t n) {
-    GWN_CUDA(cudaMallocHost(reinterpret_cast<void**>(&p_), n * sizeof(unsigned)));
-  }
-  ~PinnedWords() {
-    if (p_) cudaFreeHost(p_);
-  }
-  PinnedWords(const PinnedWords&) = delete;
-  PinnedWords& operator=(const PinnedWords&) = delete;
-  unsigned* get() const { return p_; }
-
- private:
-  unsigned* p_ = nullptr;
-};
+// 64 pinned host words for small device-to-host reads (a copy into pageable
+// memory is staged by the driver on every call), one buffer per host thread
+// kept for the thread's life: pinning memory costs more than the copies it
+// speeds up.  A caller uses the words between its copy and its stream
+// synchronization, and calls on one thread do not overlap.
+inline unsigned* pinned_words() {
+  struct Buf {
+    unsigned* p = nullptr;
+    ~Buf() {
+      if (p) cudaFreeHost(p);
+    }
+  };
+  thread_local Buf b;
+  if (!b.p) GWN_CUDA(cudaMallocHost(reinterpret_cast<void**>(&b.p), 64 * sizeof(unsigned)));
+  return b.p;
+}
 
 // Optional per-phase timing of the calling thread's ABI calls (CUDA events
 // recorded on the launch stream).  Off unless gwn_profile_enable(1).

@@ -946,8 +946,12 @@ void hier_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, HierT
   DevBuf<unsigned long long> mm(6, st);
   init_minmax(mm.get(), 3, st);
   launch_kernel(mesh_bbox_kernel, std::min<unsigned>(nblk(nV), 1024u), kT, 0, st, V, nV, mm.get());
-  unsigned long long mmh[6];
-  GWN_CUDA(cudaMemcpyAsync(mmh, mm.get(), sizeof(mmh), cudaMemcpyDeviceToHost, st));
+  // small host reads go through pinned words (a copy into pageable memory
+  // is staged by the driver on every call)
+  unsigned* pin = pinned_words();
+  unsigned long long* mmh = reinterpret_cast<unsigned long long*>(pin);
+  GWN_CUDA(cudaMemcpyAsync(mmh, mm.get(), 6 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                           st));
   GWN_CUDA(cudaStreamSynchronize(st));
   double diag2 = 0;
   for (int d = 0; d < 3; ++d) {
@@ -1008,10 +1012,10 @@ void hier_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, HierT
                   (int32_t*)nullptr);
     GWN_CUDA(cudaMemsetAsync(cnt.get() + m, 0, sizeof(uint32_t), st));
     exclusive_scan_u32(cnt.get(), cnt.get(), m + 1, st);
-    uint32_t tot = 0;
-    GWN_CUDA(cudaMemcpyAsync(&tot, cnt.get() + m, sizeof(tot), cudaMemcpyDeviceToHost, st));
+    GWN_CUDA(cudaMemcpyAsync(pin + 12, cnt.get() + m, sizeof(uint32_t),
+                             cudaMemcpyDeviceToHost, st));
     GWN_CUDA(cudaStreamSynchronize(st));
-    nrec = tot;
+    nrec = pin[12];
   }
   DevBuf<uint32_t> cap_off((size_t)nn, st), cap_cnt((size_t)nn, st);
   cap_off.zero(st);
@@ -1042,8 +1046,8 @@ void hier_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, HierT
     launch_kernel(record_mult_kernel, nblk(nrec + 1), kT, 0, st, (const int32_t*)rnet.get(),
                   (const int32_t*)order.get(), nrec, mult.get());
     exclusive_scan_u32(mult.get(), mult.get(), nrec + 1, st);
-    uint32_t tot = 0;
-    GWN_CUDA(cudaMemcpyAsync(&tot, mult.get() + nrec, sizeof(tot), cudaMemcpyDeviceToHost, st));
+    GWN_CUDA(cudaMemcpyAsync(pin + 13, mult.get() + nrec, sizeof(uint32_t),
+                             cudaMemcpyDeviceToHost, st));
     first_rec.alloc((size_t)nn, st);
     launch_kernel(first_record_kernel, nblk(nrec), kT, 0, st, (const int32_t*)order.get(),
                   (const int32_t*)rnode.get(), nrec, first_rec.get(), (const uint32_t*)mult.get(),
@@ -1052,7 +1056,7 @@ void hier_build(const double* V, int64_t nV, const int32_t* F, int64_t nF, HierT
                   (const int32_t*)rnode.get(), nrec, (const uint32_t*)mult.get(),
                   (const uint32_t*)cap_off.get(), cap_cnt.get());
     GWN_CUDA(cudaStreamSynchronize(st));
-    ncap = tot;
+    ncap = pin[13];
   }
   ph_part = std::make_unique<PhaseTimer>("hier_build_emit", st);
   h.nnodes = nn;

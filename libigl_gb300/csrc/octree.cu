@@ -532,7 +532,7 @@ void octree_build(gwn_octree_impl& t, const double* P, int64_t n, bool host_mode
   bool had_chain = false;
   int levels = 0;
   DevBuf<unsigned> totals_d(8, st);
-  PinnedWords totals_h(8);
+  unsigned* totals_h = pinned_words();
   while (K > 0) {
     ++levels;
     const int64_t K8 = (int64_t)K * 8;
@@ -576,12 +576,12 @@ void octree_build(gwn_octree_impl& t, const double* P, int64_t n, bool host_mode
     launch_kernel(level_totals_kernel, 1, 1, 0, st, (const unsigned*)child_state.get(),
                   (const unsigned*)child_newseg.get(), (const unsigned*)child_chainslot.get(), K8,
                   (const unsigned*)eflag.get(), (const unsigned*)epos.get(), M, totals_d.get());
-    GWN_CUDA(cudaMemcpyAsync(totals_h.get(), totals_d.get(), 5 * sizeof(unsigned),
+    GWN_CUDA(cudaMemcpyAsync(totals_h, totals_d.get(), 5 * sizeof(unsigned),
                              cudaMemcpyDeviceToHost, st));
     GWN_CUDA(cudaStreamSynchronize(st));
-    const unsigned last_state = totals_h.get()[0], last_newseg = totals_h.get()[1],
-                   last_chain = totals_h.get()[2], last_eflag = totals_h.get()[3],
-                   last_epos = totals_h.get()[4];
+    const unsigned last_state = totals_h[0], last_newseg = totals_h[1],
+                   last_chain = totals_h[2], last_eflag = totals_h[3],
+                   last_epos = totals_h[4];
     const int nK = (int)(last_newseg + (last_state == 1u ? 1u : 0u));
     const int nChains = (int)(last_chain + (last_state == 2u ? 1u : 0u));
     const int64_t nM = (int64_t)last_epos + last_eflag;
