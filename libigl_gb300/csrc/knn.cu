@@ -164,7 +164,9 @@ __device__ __forceinline__ float cell_lower_bound(float4 lo, float4 hi, float fx
   return fmaxf(d - 1e-6f * (S + d), 0.f);
 }
 
-template <typename QT>
+// KMAX: the heap's capacity (k <= KMAX), so that small k keep a small
+// per-thread frame in local memory.
+template <typename QT, int KMAX>
 __global__ void __launch_bounds__(128) knn_octree_kernel(KnnTree t, const QT* __restrict__ Q,
                                                          int64_t nQ,
                                                          const int32_t* __restrict__ perm, int k,
@@ -177,23 +179,25 @@ __global__ void __launch_bounds__(128) knn_octree_kernel(KnnTree t, const QT* __
   const double qx = (double)Q[q * 3], qy = (double)Q[q * 3 + 1], qz = (double)Q[q * 3 + 2];
   const float fx = (float)qx, fy = (float)qy, fz = (float)qz;
   const float S = fmaxf(fabsf(fx), fmaxf(fabsf(fy), fabsf(fz))) + t.cmax;
-  double hd[kKnnMaxK];
-  int32_t hi[kKnnMaxK];
+  double hd[KMAX];
+  int32_t hi[KMAX];
   Heap heap{hd, hi, 0, k};
   // FP32 upper bound of the k-th distance once the heap is full (pruning
   // only what is strictly farther)
   float kbound = INFINITY;
+  // the stack holds cells only: a popped cell's bound is computed again from
+  // its box (the same value as when it was pushed), which keeps the
+  // thread's frame in local memory small
   int stk[kKnnStack];
-  float slb[kKnnStack];
   int sp = 0;
-  stk[sp] = 0;
-  slb[sp] = 0.f;
-  ++sp;
+  stk[sp++] = 0;  // the root, bound 0
   while (sp > 0) {
-    --sp;
-    const int c = stk[sp];
-    const float lb = slb[sp];
-    if (lb > kbound) continue;
+    const int c = stk[--sp];
+    if (c != 0) {
+      const float lb = cell_lower_bound(__ldg(&t.box[2 * (int64_t)c]),
+                                        __ldg(&t.box[2 * (int64_t)c + 1]), fx, fy, fz, S);
+      if (lb > kbound) continue;
+    }
     if (t.ch[(int64_t)c * 8] < 0) {  // leaf: its first point (knn.cpp:121-125)
       const int32_t p = t.perm[t.start[c]];
       heap.offer(point_dist(t.P, p, qx, qy, qz), p);
@@ -222,11 +226,7 @@ __global__ void __launch_bounds__(128) knn_octree_kernel(KnnTree t, const QT* __
       overflow[atomicAdd(n_overflow, 1u)] = (int32_t)q;
       return;
     }
-    for (int j = 0; j < m; ++j) {
-      stk[sp] = cc[j];
-      slb[sp] = cl[j];
-      ++sp;
-    }
+    for (int j = 0; j < m; ++j) stk[sp++] = cc[j];
   }
   heap.write_sorted(I + q * k);
 }
@@ -333,9 +333,17 @@ static void knn_t(const gwn_octree_impl& tree, const QT* Q, int64_t nQ, int64_t 
   DevBuf<int32_t> over((size_t)nQ, st);
   DevBuf<unsigned> nover(1, st);
   nover.zero(st);
-  launch_kernel(knn_octree_kernel<QT>, (unsigned)((nQ + 127) / 128), 128, 0, st, t, Q, nQ,
-                (const int32_t*)(qo.active ? qo.perm.get() : nullptr), (int)kk, I, over.get(),
-                nover.get());
+  const int32_t* qperm = qo.active ? qo.perm.get() : nullptr;
+  const unsigned grid = (unsigned)((nQ + 127) / 128);
+  if (kk <= 16)
+    launch_kernel(knn_octree_kernel<QT, 16>, grid, 128, 0, st, t, Q, nQ, qperm, (int)kk, I,
+                  over.get(), nover.get());
+  else if (kk <= 32)
+    launch_kernel(knn_octree_kernel<QT, 32>, grid, 128, 0, st, t, Q, nQ, qperm, (int)kk, I,
+                  over.get(), nover.get());
+  else
+    launch_kernel(knn_octree_kernel<QT, kKnnMaxK>, grid, 128, 0, st, t, Q, nQ, qperm, (int)kk, I,
+                  over.get(), nover.get());
   unsigned no = 0;
   GWN_CUDA(cudaMemcpyAsync(&no, nover.get(), 4, cudaMemcpyDeviceToHost, st));
   GWN_CUDA(cudaStreamSynchronize(st));
