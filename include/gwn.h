@@ -433,6 +433,9 @@ int gwn_eytzinger_winding_number(const double* P, int64_t nP, const double* V, i
  *  - gwn_server_create: hbm_budget_bytes bounds the device bytes of resident
  *    trees; a tree is built when a request first needs it, and the least
  *    recently used trees with no request in flight are evicted to make room.
+ *    Builds run on builder threads with their own streams, so batches of
+ *    resident meshes keep running while a cold mesh builds; its requests
+ *    join a batch once its tree is ready.
  *    max_batch_queries bounds the queries of one batch (each request's
  *    count is padded to a multiple of 32); `slots` batches may be on the
  *    device at once.  A worker thread forms a batch from the pending
