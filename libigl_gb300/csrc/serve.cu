@@ -6,7 +6,8 @@
 // igl::fast_winding_number(bvh, accuracy_scale, Q, W)
 // (include/igl/fast_winding_number.cpp:418-455) computes for its mesh, the
 // tree being the one igl::fast_winding_number(V, F, order, bvh) (:380-416)
-// stands for (built here by soup_build, as gwn_soup_build does).
+// stands for (built here as gwn_soup_build builds it: GWN_SOUP_TREE_DEFAULT,
+// the reference's own tree).
 //
 //  admission  a mesh is built on the device the first time a request needs
 //             it; resident trees are limited to an HBM budget, and the least
@@ -215,8 +216,9 @@ __global__ void __launch_bounds__(128, 8) serve_walk_kernel(ServeHeader* __restr
       float acc;
       double acc64;
       soupwalk::WalkCounters c;
-      soupwalk::walk_mixed<false>(prm, valid, qx, qy, qz, acc, acc64, c,
-                                  warp_q[threadIdx.x >> 5].near);
+      // every served tree is of the default kind (the builder below)
+      soupwalk::walk_mixed<false, GWN_SOUP_TREE_DEFAULT>(prm, valid, qx, qy, qz, acc, acc64, c,
+                                                         warp_q[threadIdx.x >> 5].near);
       w = soupwalk::mixed_result(acc, acc64);
       if (valid && fabs(w - 0.5) <= soupwalk::kBand) {
         const unsigned s = atomicAdd(&counters[1], 1u);
