@@ -612,7 +612,10 @@ void run_exact(const ExactArgs& a, cudaStream_t st) {
 // behind, so calls that overlap on the GPU (different streams) race; calls
 // on one stream are ordered.  The first call on a device looks up the
 // array's device address (cudaGetSymbolAddress, with that device current);
-// make that first call before any stream capture.
+// make that first call before any stream capture.  The address is kept for
+// the life of the process: it does not survive cudaDeviceReset or any other
+// teardown of the device's primary context, after which the entry point must
+// not be called.
 // ---------------------------------------------------------------------------
 namespace {
 
