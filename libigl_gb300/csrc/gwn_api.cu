@@ -351,6 +351,7 @@ int gwn_soup_eval(const gwn_soup* soup, float accuracy_scale, const void* Q, int
     check_precision(precision);
     check_mem(mem);
     ensure_device();
+    check_device_of(soup->impl.device);
     cudaStream_t st = as_stream(stream);
     StagedBytes dQ(Q, (size_t)nQ * 3 * dtype_size(q_dtype), mem, st);
     StagedBytes dW(W, (size_t)nQ * dtype_size(w_dtype), mem, st, false);
@@ -369,7 +370,10 @@ int gwn_soup_walk_stats(const gwn_soup* soup, float accuracy_scale, const double
   return guarded("gwn_soup_walk_stats", [&] {
     GWN_REQUIRE(soup && counters, "null argument");
     GWN_REQUIRE(nQ >= 0 && nQ < (int64_t(1) << 31), "0 <= nQ < 2^31");
+    GWN_REQUIRE(nQ == 0 || Q, "Q must be non-null");
+    GWN_REQUIRE(std::isfinite(accuracy_scale), "accuracy_scale must be finite");
     check_mem(mem);
+    ensure_device();
     check_device_of(soup->impl.device);
     cudaStream_t st = nullptr;
     Staged<double> dQ(Q, (size_t)nQ * 3, mem, st);
@@ -541,8 +545,13 @@ int gwn_cloud_eval(const gwn_cloud* cloud, double beta, const void* Q, int q_dty
 
 void gwn_cloud_free(gwn_cloud* cloud) { delete cloud; }
 
-static void check_csr(const int64_t* pi_offsets, const int32_t* CH, int64_t ncells, int64_t nP) {
+// The caller's octree arrays (igl::octree's point_indices as CSR, CH): checked
+// on the host before anything reaches the device.
+static void check_csr(const double* P, const double* N, const double* A, int64_t nP,
+                      const int64_t* pi_offsets, const int32_t* pi_indices, const int32_t* CH,
+                      int64_t ncells) {
   GWN_REQUIRE(ncells >= 1, "the octree needs at least the root cell");
+  GWN_REQUIRE(nP == 0 || (P && N && A), "P, N and A must be non-null");
   GWN_REQUIRE(pi_offsets[0] == 0, "pi_offsets[0] must be 0");
   for (int64_t c = 0; c < ncells; ++c) {
     GWN_REQUIRE(pi_offsets[c + 1] >= pi_offsets[c], "pi_offsets must be non-decreasing");
@@ -550,7 +559,10 @@ static void check_csr(const int64_t* pi_offsets, const int32_t* CH, int64_t ncel
       for (int k = 0; k < 8; ++k)
         GWN_REQUIRE(CH[c * 8 + k] > 0 && CH[c * 8 + k] < ncells, "CH child id out of range");
   }
-  (void)nP;
+  const int64_t nidx = pi_offsets[ncells];
+  GWN_REQUIRE(nidx == 0 || pi_indices, "pi_indices must be non-null");
+  for (int64_t j = 0; j < nidx; ++j)
+    GWN_REQUIRE(pi_indices[j] >= 0 && pi_indices[j] < nP, "point index out of range");
 }
 
 int gwn_cloud_precompute_arrays(const double* P, const double* N, const double* A, int64_t nP,
@@ -561,10 +573,8 @@ int gwn_cloud_precompute_arrays(const double* P, const double* N, const double* 
     GWN_REQUIRE(nP >= 0 && ncells >= 1, "nP >= 0 and ncells >= 1");
     GWN_REQUIRE(pi_offsets && CH && CM && R && EC, "null argument");
     GWN_REQUIRE(order >= 0 && order <= 2, "expansion order must be 0, 1 or 2");
-    check_csr(pi_offsets, CH, ncells, nP);
+    check_csr(P, N, A, nP, pi_offsets, pi_indices, CH, ncells);
     const int64_t nidx = pi_offsets[ncells];
-    for (int64_t j = 0; j < nidx; ++j)
-      GWN_REQUIRE(pi_indices[j] >= 0 && pi_indices[j] < nP, "point index out of range");
     ensure_device();
     cudaStream_t st = nullptr;
     Staged<double> dP(P, (size_t)nP * 3, GWN_HOST, st), dN(N, (size_t)nP * 3, GWN_HOST, st),
@@ -594,10 +604,8 @@ int gwn_cloud_eval_arrays(const double* P, const double* N, const double* A, int
     GWN_REQUIRE(nQ == 0 || (Q && W), "Q and W must be non-null");
     GWN_REQUIRE(order >= 0 && order <= 2, "expansion order must be 0, 1 or 2");
     check_precision(precision);
-    check_csr(pi_offsets, CH, ncells, nP);
+    check_csr(P, N, A, nP, pi_offsets, pi_indices, CH, ncells);
     const int64_t nidx = pi_offsets[ncells];
-    for (int64_t j = 0; j < nidx; ++j)
-      GWN_REQUIRE(pi_indices[j] >= 0 && pi_indices[j] < nP, "point index out of range");
     ensure_device();
     cudaStream_t st = nullptr;
     Staged<double> dP(P, (size_t)nP * 3, GWN_HOST, st), dN(N, (size_t)nP * 3, GWN_HOST, st),

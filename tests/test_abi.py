@@ -78,3 +78,56 @@ def test_mesh_arguments_refused_before_any_device_work(gwn_lib):
     # the wait-injection hook validates its argument without a device
     assert L.gwn_debug_fail_next_waits(-1) == 1
     assert L.gwn_debug_fail_next_waits(0) == 0
+
+
+def test_octree_arrays_refused_before_any_device_work(gwn_lib):
+    """The array forms of the cloud precompute and evaluation check the
+    caller's octree (CSR point lists, CH) and its point arrays on the host,
+    so a null or out-of-range argument is an error before any launch."""
+    import ctypes as C
+    import numpy as np
+    L = gwn_lib
+    P = np.zeros((2, 3))
+    N = np.zeros((2, 3))
+    A = np.ones(2)
+    off = np.array([0, 2], dtype=np.int64)      # one cell holding both points
+    idx = np.array([0, 1], dtype=np.int32)
+    CH = np.full(8, -1, dtype=np.int32)
+    CM, R, EC = np.zeros(3), np.zeros(1), np.zeros(39)
+    Q, W = np.zeros(3), np.zeros(1)
+
+    def ptr(a):
+        return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+    def pre(P_, N_, A_, off_, idx_, CH_):
+        return L.gwn_cloud_precompute_arrays(ptr(P_), ptr(N_), ptr(A_), 2, ptr(off_), ptr(idx_),
+                                             ptr(CH_), 1, 2, ptr(CM), ptr(R), ptr(EC))
+
+    def ev(P_, N_, A_, off_, idx_, CH_):
+        return L.gwn_cloud_eval_arrays(ptr(P_), ptr(N_), ptr(A_), 2, ptr(off_), ptr(idx_),
+                                       ptr(CH_), 1, ptr(CM), ptr(R), ptr(EC), 2, ptr(Q), 1, 2.0,
+                                       ptr(W), 0)
+
+    for call in (pre, ev):
+        assert call(P, N, A, off, None, CH) == 1
+        assert b"pi_indices must be non-null" in L.gwn_last_error()
+        assert call(None, N, A, off, idx, CH) == 1
+        assert b"P, N and A must be non-null" in L.gwn_last_error()
+        assert call(P, N, A, off, np.array([0, 2], dtype=np.int32), CH) == 1
+        assert b"point index out of range" in L.gwn_last_error()
+        CH_bad = np.array([5, 1, 1, 1, 1, 1, 1, 1], dtype=np.int32)
+        assert call(P, N, A, off, idx, CH_bad) == 1
+        assert b"CH child id out of range" in L.gwn_last_error()
+
+
+def test_soup_walk_stats_refuses_null_queries(gwn_lib):
+    """A non-null handle is not dereferenced before the argument checks."""
+    import ctypes as C
+    L = gwn_lib
+    counters = (C.c_ulonglong * 7)()
+    fake = C.c_void_p(1)
+    assert L.gwn_soup_walk_stats(fake, 2.0, None, 4, 0, counters) == 1
+    assert b"Q must be non-null" in L.gwn_last_error()
+    q = (C.c_double * 3)()
+    assert L.gwn_soup_walk_stats(fake, float("inf"), q, 1, 0, counters) == 1
+    assert b"accuracy_scale must be finite" in L.gwn_last_error()
