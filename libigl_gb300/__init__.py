@@ -95,6 +95,23 @@ class _Arg:
         return tuple(self.obj.shape)
 
 
+def _need_rows(a, cols: int, name: str, rows: int | None = None):
+    """Raise ValueError unless ``a`` (an _Arg) is a rows x cols matrix (any
+    number of rows when ``rows`` is None): the C ABI reads rows * cols
+    elements from the pointer it is given."""
+    shape = a.shape
+    if len(shape) != 2 or shape[1] != cols or (rows is not None and shape[0] != rows):
+        want = f"{rows if rows is not None else '#'} x {cols}"
+        raise ValueError(f"{name} must be {want}, got shape {shape}")
+
+
+def _need_len(a, n: int, name: str):
+    """Raise ValueError unless ``a`` holds exactly n elements."""
+    size = int(np.prod(a.shape)) if len(a.shape) else 1
+    if size != n:
+        raise ValueError(f"{name} must hold {n} elements, got shape {tuple(a.shape)}")
+
+
 def _same_mem(*args):
     mems = {a.mem for a in args}
     if len(mems) != 1:
@@ -378,6 +395,8 @@ class CloudExpansion:
         Na = _Arg(Nrm, np.float64)
         Aa = _Arg(np.asarray(A).reshape(-1) if not _is_torch_cuda(A) else A.reshape(-1),
                   np.float64)
+        _need_rows(Na, 3, "N", tree.num_points)
+        _need_len(Aa, tree.num_points, "A")
         h = C.c_void_p()
         stream = _stream_ptr() if Na.mem == N.GWN_DEVICE else None
         N.check(L.gwn_cloud_build(tree._h, None, Na.ptr, Aa.ptr, int(order), Na.mem, stream,
@@ -428,15 +447,38 @@ def _f64(a):
     return np.ascontiguousarray(a, dtype=np.float64)
 
 
+def _octree_arrays(P, Nrm, A, pi_offsets, pi_indices, CH):
+    """The caller's cloud and octree arrays as contiguous host arrays, with
+    the shapes the C ABI reads checked first."""
+    P, Nrm, A = _f64(P), _f64(Nrm), _f64(np.asarray(A).reshape(-1))
+    off = np.ascontiguousarray(pi_offsets, np.int64).reshape(-1)
+    idx = np.ascontiguousarray(pi_indices, np.int32).reshape(-1)
+    CH = np.ascontiguousarray(CH, np.int32)
+    if P.ndim != 2 or P.shape[1] != 3:
+        raise ValueError(f"P must be #P x 3, got shape {P.shape}")
+    if Nrm.shape != P.shape:
+        raise ValueError(f"N must be {P.shape[0]} x 3, got shape {Nrm.shape}")
+    if A.shape[0] != P.shape[0]:
+        raise ValueError(f"A must hold {P.shape[0]} elements, got {A.shape[0]}")
+    if CH.ndim != 2 or CH.shape[1] != 8 or CH.shape[0] < 1:
+        raise ValueError(f"CH must be #cells x 8 with at least the root, got shape {CH.shape}")
+    if off.shape[0] != CH.shape[0] + 1:
+        raise ValueError(f"pi_offsets must hold #cells + 1 = {CH.shape[0] + 1} entries, "
+                         f"got {off.shape[0]}")
+    if idx.shape[0] < off[-1]:
+        raise ValueError(f"pi_indices must hold pi_offsets[-1] = {off[-1]} entries, "
+                         f"got {idx.shape[0]}")
+    return P, Nrm, A, off, idx, CH
+
+
 def fast_winding_number_cloud_precompute(P, Nrm, A, pi_offsets, pi_indices, CH, order: int = 2):
     """igl::fast_winding_number(P,N,A,point_indices,CH,expansion_order,CM,R,EC)
     over caller-held octree arrays (host memory).  Returns (CM, R, EC) with
     #cells rows."""
-    P, Nrm, A = _f64(P), _f64(Nrm), _f64(np.asarray(A).reshape(-1))
-    off = np.ascontiguousarray(pi_offsets, np.int64)
-    idx = np.ascontiguousarray(pi_indices, np.int32)
-    CH = np.ascontiguousarray(CH, np.int32)
+    P, Nrm, A, off, idx, CH = _octree_arrays(P, Nrm, A, pi_offsets, pi_indices, CH)
     nc = CH.shape[0]
+    if order not in (0, 1, 2):
+        raise ValueError("order must be 0, 1 or 2")
     nt = {0: 3, 1: 12, 2: 39}[order]
     CM, R, EC = np.empty((nc, 3)), np.empty(nc), np.empty((nc, nt))
     p = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
@@ -450,12 +492,17 @@ def fast_winding_number_cloud(P, Nrm, A, pi_offsets, pi_indices, CH, CM, R, EC, 
     """igl::fast_winding_number(P,N,A,point_indices,CH,CM,R,EC,Q,beta,WN) over
     caller-held arrays (host memory); CM/R/EC may carry the reference's
     8*#cells rows, only the first #cells are read."""
-    P, Nrm, A, Q = _f64(P), _f64(Nrm), _f64(np.asarray(A).reshape(-1)), _f64(Q)
-    off = np.ascontiguousarray(pi_offsets, np.int64)
-    idx = np.ascontiguousarray(pi_indices, np.int32)
-    CH = np.ascontiguousarray(CH, np.int32)
+    P, Nrm, A, off, idx, CH = _octree_arrays(P, Nrm, A, pi_offsets, pi_indices, CH)
+    Q = _f64(Q)
+    if Q.ndim != 2 or Q.shape[1] != 3:
+        raise ValueError(f"Q must be #Q x 3, got shape {Q.shape}")
     nc = CH.shape[0]
-    CM, R, EC = _f64(CM)[:nc], _f64(np.asarray(R).reshape(-1))[:nc], _f64(EC)[:nc]
+    CM, R, EC = _f64(CM), _f64(np.asarray(R).reshape(-1)), _f64(EC)
+    if CM.ndim != 2 or CM.shape[1] != 3 or CM.shape[0] < nc or R.shape[0] < nc:
+        raise ValueError(f"CM must be at least {nc} x 3 and R hold at least {nc} entries")
+    if EC.ndim != 2 or EC.shape[1] not in (3, 12, 39) or EC.shape[0] < nc:
+        raise ValueError(f"EC must be at least {nc} x (3, 12 or 39), got shape {EC.shape}")
+    CM, R, EC = np.ascontiguousarray(CM[:nc]), R[:nc], np.ascontiguousarray(EC[:nc])
     order = {3: 0, 12: 1, 39: 2}[EC.shape[1]]
     W = np.empty(Q.shape[0])
     p = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
@@ -487,6 +534,8 @@ def point_areas(P, I, N, return_T: bool = False):
     Ia = _Arg(I, np.int32, allowed=(np.int32,))
     Na = _Arg(N, np.float64)
     mem = _same_mem(Pa, Ia, Na)
+    _need_rows(Pa, 3, "P")
+    _need_rows(Na, 3, "N", Pa.shape[0])
     if len(Ia.shape) != 2 or Ia.shape[0] != Pa.shape[0]:
         raise ValueError("I must be #P x k")
     n, k = Ia.shape
@@ -508,6 +557,9 @@ def fast_winding_number_cloud_points(P, Nrm, Q, order: int = 2, beta: float = 2.
     Na = _Arg(Nrm, np.float64)
     Qa = _Arg(Q)
     mem = _same_mem(Pa, Na, Qa)
+    _need_rows(Pa, 3, "P")
+    _need_rows(Na, 3, "N", Pa.shape[0])
+    _need_rows(Qa, 3, "Q")
     wdt = np.dtype(out_dtype) if out_dtype is not None else Qa.np_dtype
     W = _empty_like_mem(mem, (Qa.shape[0],), wdt, like=Qa)
     stream = _stream_ptr() if mem == NV.GWN_DEVICE else None
@@ -524,6 +576,10 @@ def knn(P, V, k: int):
     index); the octree of V is built inside.  Host arrays or CUDA tensors."""
     Pa, Va = _Arg(P, np.float64), _Arg(V, np.float64)
     _same_mem(Pa, Va)
+    _need_rows(Pa, 3, "P")
+    _need_rows(Va, 3, "V")
+    if int(k) < 0:
+        raise ValueError("k must be non-negative")
     cols = min(int(k), Va.shape[0])
     I = _empty_like_mem(Pa.mem, (Pa.shape[0], cols), np.int32, like=Pa)
     stream = _stream_ptr() if Pa.mem == N.GWN_DEVICE else None
@@ -628,6 +684,13 @@ def eytzinger_aabb_winding_number(P, V, E, B1, B2, leaf, I, Cc, precision="mixed
     _same_mem(Pa, Va, B1a, B2a, Ea, La, Ia, Ca)
     if len(Pa.shape) != 2 or Pa.shape[1] != 2 or (Va.shape[0] and Va.shape[1:] != (2,)):
         raise ValueError("P and V must be #P x 2 / #V x 2")
+    if Ea.shape[0] and Ea.shape[1:] != (2,):
+        raise ValueError(f"E must be #E x 2, got shape {Ea.shape}")
+    slots = La.shape[0]
+    if slots:
+        _need_rows(B1a, 2, "B1", slots)
+        _need_rows(B2a, 2, "B2", slots)
+        _need_len(Ca, slots + 1, "C")
     n = Pa.shape[0]
     W = _empty_like_mem(Pa.mem, (n,), np.float64, like=Pa)
     stream = _stream_ptr() if Pa.mem == N.GWN_DEVICE else None
@@ -683,7 +746,7 @@ def signed_distance(P, V, F, sign_type=SIGNED_DISTANCE_TYPE_DEFAULT, lower_bound
     return (S, I, Cp, Nm) if return_normals else (S, I, Cp)
 
 
-# ------------------------------------------------------------- profiling --
+# ---------------------------------------------------------- swept volume --
 def _affine_rows(transforms):
     T = np.asarray(transforms, dtype=np.float64)
     if T.ndim == 2 and T.shape[1] == 12:
@@ -720,6 +783,7 @@ def swept_volume_signed_distance(V, F, transforms, sign_type, GV, res, h, isolev
     if S0 is not None:
         S0a = _Arg(S0, np.float64)
         _same_mem(Ga, S0a)
+        _need_len(S0a, n, "S0")
         S0p = S0a.ptr
     stream = _stream_ptr() if Ga.mem == N.GWN_DEVICE else None
     N.check(N.load().gwn_swept_volume_signed_distance(
@@ -743,6 +807,7 @@ def flood_fill(res, S):
     return S
 
 
+# ------------------------------------------------------------- profiling --
 def profile_enable(on: bool = True, accumulate: bool = False) -> None:
     """Record CUDA events around each phase of this thread's calls (of the
     last call only, or, with ``accumulate``, of every call until the next
