@@ -234,7 +234,9 @@ def cloud_fwn(P, N, A, Q, order: int = 2, beta: float = 2.0, nthreads: int = 0):
 
 
 class SoupPort:
-    """CPU restatement of the HDK soup FWN (oracle/soup_port.cpp)."""
+    """CPU restatement of the reference's FP32 soup FWN (oracle/soup_hdk.cpp:
+    the UT_BVH<4> build, the HDK moments and computeSolidAngle; equal to the
+    compiled reference bit for bit on the committed fixtures)."""
 
     def __init__(self, V, F, order: int = 2):
         self._V = _d(V)
