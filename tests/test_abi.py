@@ -131,3 +131,41 @@ def test_soup_walk_stats_refuses_null_queries(gwn_lib):
     q = (C.c_double * 3)()
     assert L.gwn_soup_walk_stats(fake, float("inf"), q, 1, 0, counters) == 1
     assert b"accuracy_scale must be finite" in L.gwn_last_error()
+
+
+def test_size_limits_refused_before_any_device_work(gwn_lib):
+    """Every entry point's largest accepted size is checked on the host:
+    one past it is GWN_ERR_INVALID_ARGUMENT before anything is read from the
+    arrays or launched (the small buffers below are never read)."""
+    import ctypes as C
+    L = gwn_lib
+    big31, big30 = 2 ** 31, 2 ** 30
+    buf = (C.c_double * 64)()
+    ibuf = (C.c_int32 * 64)()
+    fake = C.c_void_p(1)          # a handle that is refused before it is read
+    res = (C.c_int32 * 3)(2 ** 14, 2 ** 14, 2 ** 14)
+    cases = [
+        ("queries", lambda: L.gwn_winding_number(buf, 3, 3, ibuf, 1, buf, 1, big31, buf, 1, 1,
+                                                 0, None)),
+        ("queries", lambda: L.gwn_soup_eval(fake, 2.0, buf, 1, big31, buf, 1, 1, 0, None)),
+        ("nQ < 2^31", lambda: L.gwn_cloud_eval(fake, 2.0, buf, 1, big31, buf, 1, 1, 0, None)),
+        ("queries", lambda: L.gwn_wn_aabb_eval_precision(fake, buf, big31, buf, 1, 0, None)),
+        ("queries", lambda: L.gwn_knn(buf, big31, buf, 1, 1, ibuf, 0, None)),
+        ("queries", lambda: L.gwn_signed_distance(buf, big31, buf, 3, ibuf, 1, 2, 0.0, 1.0, buf,
+                                                  ibuf, buf, None, 0, 0, None)),
+        ("primitives", lambda: L.gwn_eytzinger_aabb(buf, buf, big30, 2, buf, buf, ibuf, 0, None)),
+        ("segments", lambda: L.gwn_eytzinger_winding_number_tree(ibuf, big30, ibuf, 2, ibuf,
+                                                                  None, 0, None)),
+        ("queries", lambda: L.gwn_eytzinger_winding_number(buf, big31, buf, 2, ibuf, 1, buf, buf,
+                                                           ibuf, 2, ibuf, 0, ibuf, buf, 0, 0,
+                                                           None)),
+        ("grid points", lambda: L.gwn_swept_volume_signed_distance(
+            buf, 3, ibuf, 1, buf, 1, 1, buf, big31, ibuf, 1.0, float("nan"), None, buf, 0, 0,
+            None)),
+        ("grid too large", lambda: L.gwn_flood_fill(res, buf, 0, None)),
+        ("no-allocation limit", lambda: L.gwn_winding_number_noalloc(buf, 3, ibuf, 65537, buf, 1,
+                                                                     buf, None, None)),
+    ]
+    for what, call in cases:
+        assert call() == 1, what
+        assert what.encode() in L.gwn_last_error(), (what, L.gwn_last_error())
