@@ -75,6 +75,8 @@ void flood_fill_run(const int32_t res[3], double* S, cudaStream_t st);
 // igl::copyleft::cgal::point_areas (point_areas.cu): A (nP) and, when T is
 // non-null, T (nP x 3) from the nP x k neighbour lists I; device pointers.
 constexpr int kPointAreasMaxK = 128;
+static_assert(kPointAreasMaxK == GWN_POINT_AREAS_MAX_K,
+              "the kernel's neighbour arrays hold the largest k the ABI accepts");
 void point_areas_run(const double* P, int64_t nP, const int32_t* I, int k, const double* N,
                      double* A, double* T, unsigned* status, cudaStream_t st);
 
