@@ -11,6 +11,11 @@
  *                 is enqueued on `stream` (a cudaStream_t, NULL = legacy
  *                 default stream) and the call returns without waiting.
  * Arrays are row-major and contiguous: V[i*3+d], F[f*3+c], Q[i*3+d].
+ * A handle (gwn_soup, gwn_octree, gwn_cloud, gwn_wn_aabb) belongs to the
+ * device that was current when it was built; a call that runs work on it
+ * (evaluation, knn, distance, export through a stream) with another device
+ * current is refused with GWN_ERR_INVALID_ARGUMENT.  Arguments are checked
+ * on the host before any device work.
  *
  * Precision modes:
  *   GWN_PLAIN_FP64 -- every term, sum and far-field expansion in FP64.
