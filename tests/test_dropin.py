@@ -27,6 +27,19 @@ def test_dropin_headers_compile(gwn_lib):
     assert os.path.exists(compile_dropin(gwn_lib))
 
 
+def test_dropin_dimension_templates_compile():
+    """igl::signed_distance instantiates with fixed-column matrix types (the
+    reference's dimension-templates case, 3-D half; compiled, not run)."""
+    os.makedirs(OUT_DIR, exist_ok=True)
+    obj = os.path.join(OUT_DIR, "dimension_templates.o")
+    subprocess.run(["g++", "-c", "-O0", "-std=c++17", "-Wall", "-Werror",
+                    "-I", os.path.join(ROOT, "tests", "dropin", "eigen_shim"),
+                    "-I", os.path.join(ROOT, "include", "igl_gb300"),
+                    os.path.join(ROOT, "tests", "dropin", "dimension_templates.cpp"),
+                    "-o", obj], check=True)
+    assert os.path.exists(obj)
+
+
 @pytest.mark.gpu
 def test_dropin_reference_tests_on_gpu(gwn_lib, cuda):
     exe = compile_dropin(gwn_lib)
