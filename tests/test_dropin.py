@@ -29,7 +29,8 @@ def test_dropin_headers_compile(gwn_lib):
 
 def test_dropin_dimension_templates_compile():
     """igl::signed_distance instantiates with fixed-column matrix types (the
-    reference's dimension-templates case, 3-D half; compiled, not run)."""
+    reference's dimension-templates case, 3-D half), and the winding-number
+    overloads with float and fixed-column types (compiled, not run)."""
     os.makedirs(OUT_DIR, exist_ok=True)
     obj = os.path.join(OUT_DIR, "dimension_templates.o")
     subprocess.run(["g++", "-c", "-O0", "-std=c++17", "-Wall", "-Werror",
