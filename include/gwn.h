@@ -452,8 +452,9 @@ int gwn_eytzinger_winding_number(const double* P, int64_t nP, const double* V, i
  *    (host, #Q, w_dtype) must stay valid until gwn_server_wait returns for
  *    it.  precision as for gwn_soup_eval.  Results equal gwn_soup_eval's on
  *    the same mesh and queries.
- *  - gwn_server_wait blocks until the request finished (timeout_s < 0: no
- *    limit; GWN_ERR_TIMEOUT when it runs out, the request stays queued),
+ *  - gwn_server_wait blocks until the request finished (timeout_s < 0 or
+ *    above 1e9: no limit; NaN is refused; GWN_ERR_TIMEOUT when it runs out,
+ *    the request stays queued),
  *    returns its status, and reports submit-to-result latency in seconds.
  *    Every submitted request must be waited for once.
  *  - gwn_server_destroy finishes every queued request, then frees the

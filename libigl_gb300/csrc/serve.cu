@@ -41,6 +41,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -1011,6 +1012,10 @@ int gwn_server_wait(gwn_server* S, int64_t request_id, double timeout_s, double*
     set_last_error("gwn_server_wait: server is null");
     return GWN_ERR_INVALID_ARGUMENT;
   }
+  if (std::isnan(timeout_s)) {  // a NaN duration has no meaning for wait_for
+    set_last_error("gwn_server_wait: timeout_s is NaN");
+    return GWN_ERR_INVALID_ARGUMENT;
+  }
   std::unique_lock<std::mutex> lk(S->mu);
   auto it = S->reqs.find(request_id);
   if (it == S->reqs.end()) {
@@ -1019,7 +1024,7 @@ int gwn_server_wait(gwn_server* S, int64_t request_id, double timeout_s, double*
   }
   SrvReq* r = it->second.get();
   const auto pred = [&] { return r->done; };
-  if (timeout_s < 0) {
+  if (timeout_s < 0 || timeout_s > 1e9) {  // no limit (1e9 s: past any clock's range use)
     S->cv_done.wait(lk, pred);
   } else if (!S->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), pred)) {
     set_last_error("gwn_server_wait: request not finished within the timeout");

@@ -169,3 +169,14 @@ def test_size_limits_refused_before_any_device_work(gwn_lib):
     for what, call in cases:
         assert call() == 1, what
         assert what.encode() in L.gwn_last_error(), (what, L.gwn_last_error())
+
+
+def test_server_wait_refuses_nan_timeout(gwn_lib):
+    """A NaN timeout is refused before the server is touched (a fake handle
+    is never read)."""
+    import ctypes as C
+    L = gwn_lib
+    assert L.gwn_server_wait(C.c_void_p(1), 1, float("nan"), None) == 1
+    assert b"NaN" in L.gwn_last_error()
+    assert L.gwn_server_wait(None, 1, 1.0, None) == 1
+    assert b"server is null" in L.gwn_last_error()
