@@ -963,6 +963,7 @@ int gwn_server_submit(gwn_server* S, int64_t mesh_id, const void* Q, int q_dtype
     GWN_REQUIRE(S != nullptr && request_id != nullptr, "server and request_id must be non-null");
     GWN_REQUIRE(nQ >= 0, "nQ must be non-negative");
     GWN_REQUIRE(nQ == 0 || (Q && W), "Q and W must be non-null");
+    GWN_REQUIRE(std::isfinite(accuracy_scale), "accuracy_scale must be finite");
     GWN_REQUIRE((nQ + 31) / 32 * 32 <= S->cap,
                 "nQ = " + std::to_string(nQ) + " exceeds the batch capacity of " +
                     std::to_string(S->cap) + " queries");

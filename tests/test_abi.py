@@ -180,3 +180,15 @@ def test_server_wait_refuses_nan_timeout(gwn_lib):
     assert b"NaN" in L.gwn_last_error()
     assert L.gwn_server_wait(None, 1, 1.0, None) == 1
     assert b"server is null" in L.gwn_last_error()
+
+
+def test_server_submit_refuses_non_finite_accuracy(gwn_lib):
+    """As gwn_soup_eval: a non-finite accuracy_scale is refused, before the
+    server is touched (a fake handle is never read)."""
+    import ctypes as C
+    L = gwn_lib
+    rid = C.c_int64(0)
+    rc = L.gwn_server_submit(C.c_void_p(1), 1, None, 1, 0, None, 1, float("inf"), 1,
+                             C.byref(rid))
+    assert rc == 1
+    assert b"accuracy_scale must be finite" in L.gwn_last_error()
