@@ -42,6 +42,41 @@ def test_single_triangle_analytic():
         assert abs(w - approx) / abs(approx) < 3.0 / d
 
 
+def test_exact_closed_forms():
+    """Closed-form solid angles (the exact path has no numeric golden vector
+    in the reference's tests): a unit square seen along its axis from
+    distance d subtends 4 asin(1 / (1 + 4 d^2)); each face of a regular
+    tetrahedron subtends pi from its centroid; a unit segment seen from
+    height h on its bisector subtends 2 atan(1 / (2 h)) (2-D).  Signs as the
+    reference's: a point on the side the face normal points to gets W < 0."""
+    Vs = np.array([[-0.5, -0.5, 0], [0.5, -0.5, 0], [0.5, 0.5, 0], [-0.5, 0.5, 0]], float)
+    Fs = np.array([[0, 1, 2], [0, 2, 3]], np.int32)   # normal +z
+    d = np.array([1e-3, 0.1, 0.5, 1.0, 10.0, 1e3])
+    W = O.winding_number(Vs, Fs, np.c_[np.zeros((d.size, 2)), d])
+    expect = -np.arcsin(1.0 / (1.0 + 4.0 * d ** 2)) / np.pi
+    np.testing.assert_allclose(W, expect, rtol=1e-13, atol=1e-17)
+    np.testing.assert_allclose(O.winding_number(Vs, Fs, np.c_[np.zeros((d.size, 2)), -d]),
+                               -expect, rtol=1e-13, atol=1e-17)
+    # regular tetrahedron, outward faces
+    T = np.array([[1, 1, 1], [1, -1, -1], [-1, 1, -1], [-1, -1, 1]], float)
+    c = T.mean(axis=0)
+    for f in ([0, 2, 1], [0, 1, 3], [0, 3, 2], [1, 2, 3]):
+        a, b, e = T[f]
+        n = np.cross(b - a, e - a)
+        if n @ (a - c) < 0:
+            b, e = e, b
+        assert abs(O.solid_angle(a, b, e, c) - 0.25) < 1e-15   # pi / (4 pi), point inside
+    # 2-D: unit segment from (-1/2, 0) to (1/2, 0)
+    V2 = np.array([[-0.5, 0.0], [0.5, 0.0]])
+    E2 = np.array([[0, 1]], np.int32)
+    h = np.array([1e-3, 0.25, 1.0, 100.0])
+    W2 = O.winding_number(V2, E2, np.c_[np.zeros(h.size), h])
+    np.testing.assert_allclose(np.abs(W2), 2.0 * np.arctan(1.0 / (2.0 * h)) / (2.0 * np.pi),
+                               rtol=1e-13)
+    W2m = O.winding_number(V2, E2, np.c_[np.zeros(h.size), -h])
+    np.testing.assert_allclose(W2m, -W2, rtol=1e-13)
+
+
 @pytest.mark.skipif(not O.ref_soup_available(), reason="reference tree not present")
 def test_reference_soup_single_tet_sign():
     r = O.RefSoup(TET_V, TET_F)
